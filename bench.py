@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark of the explicit APIC / MLS-MPM snow step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload two_balls_1m|two_balls|snowball|cube]
+
+One "step" is one full MPM step (sort, P2G with the MLS force, grid update,
+G2P with the plastic SVD and advection) over every particle of the workload.
+The metric is particle-steps per second.  Prints one JSON line (rank 0).
+
+* ours (default): the CUDA path through the C ABI.  ``value`` is timed with
+  CUDA events on the handle's stream with the particle state resident in HBM;
+  ``e2e`` times the same steps through the C ABI with the whole particle state
+  copied in from pinned host memory and back out every step; ``roofline``
+  comes from a second pass of the same steps with per-kernel CUDA events.
+  Multi-GPU (torchrun): one independent replica per GPU (the step has no
+  exchange between scenes), barrier-bracketed, max over ranks.
+* reference: the reference's CPU step on this host's cores - the headless
+  build of the reference where it is loadable here, else the C restatement of
+  it - one independent replica per core, each step a bounded sample of the
+  workload's particles on the workload's grid.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import __graft_entry__ as graft  # noqa: E402
+
+# Bytes the step must move per particle-step and per active grid cell-step
+# (FP32): the particle state read once (x 12, v 12, B 36, F_E 36, J_P 4, m 4,
+# V 4) and written once (x, v, B, F_E, J_P); per active cell P2G writes (m, mv)
+# 16 B, the grid update reads 16 and writes v 12, G2P reads v 12.
+STEP_BYTES_PER_PARTICLE = 208
+STEP_BYTES_PER_CELL = 44
+# Per kernel (FP32, what each kernel must move per particle / per active cell):
+#   P2G reads x, m, v, V, B, F_E, J_P (108 B) and adds (m, p) into its cells (16 B);
+#   G2P reads x, B, F_E, J_P (88 B) and the cell tile (16 B), writes the particle
+#   at its sorted slot (x, m, v, V, B, F_E, J_P: 108 B) and its next block key (4 B).
+KERNEL_BYTES = {"p2g": (108, 16), "g2p": (88 + 108 + 4, 16)}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", default="two_balls_1m")
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--cpu-baseline", type=int, default=1, help="time the single-core CPU baseline (rank 0, N=1)")
+    return ap.parse_args()
+
+
+def dist_init(backend):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, value, device=None):
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", str(self.gpu)], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        time.sleep(0.25)
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        loaded = [s for s in sm if smax and s > 0.5 * max(smax)] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_scene(name, seed):
+    from rd_gb300 import scenes
+    return scenes.SCENES[name](seed=seed)
+
+
+def cpu_baseline_single_core(sc, seconds_hint=20.0):
+    """The oracle (the headless reference where loadable, else the C
+    restatement) timed on one core for one full step of the workload after
+    its init; returns (particle-steps/s, kind, sample description)."""
+    orc = graft.load_oracle()
+    orc.build_oracle()
+    P = orc.Params(*sc.grid, sc.h, **{k: v for k, v in sc.material.items()})
+    if orc.ref_available():
+        sim = orc.RefSim(P, sc.x, sc.v, sc.mass, p4=1)
+        kind = "reference"
+    else:
+        sim = orc.OracleSim(P, sc.x, sc.v, sc.mass)
+        kind = "port"
+    sim.init()
+    t0 = time.perf_counter()
+    sim.step(sc.dt, 1)
+    dt = time.perf_counter() - t0
+    return sc.n / dt, kind, f"1 step of all {sc.n} particles after init, single thread ({dt:.1f} s)"
+
+
+def run_ours(args):
+    import torch
+
+    ws, rank, local = dist_init("nccl")
+    torch.cuda.set_device(local)
+    pkg = graft.load_package()
+    pkg.build()
+    sc = make_scene(args.workload, seed=rank)
+    params = pkg.make_params(*sc.grid, sc.n, sc.h, device=local, **sc.params())
+    sim = pkg.Simulation(params)
+    sim.set_particles(sc.x, sc.v, sc.mass)
+    sim.init_volumes()
+    stream = torch.cuda.ExternalStream(sim.stream(), device=local)
+
+    # warm-up, then keep the GPU busy for ~1 s so the clock record reflects load
+    sim.step(sc.dt, args.warmup)
+    sim.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        t_soak = time.perf_counter()
+        while time.perf_counter() - t_soak < 1.0:
+            sim.step(sc.dt, 50)
+            sim.synchronize()
+        barrier(ws)
+        torch.cuda.synchronize()
+        sim.synchronize()
+        l0 = sim.launch_count()
+        ev0.record(stream)
+        sim.step(sc.dt, args.steps)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        launches = sim.launch_count() - l0
+        barrier(ws)
+    ms = ev0.elapsed_time(ev1)
+    ms_max = max_over_ranks(ws, ms, device=torch.device("cuda", local))
+    value = ws * sc.n * args.steps / (ms_max / 1e3)
+    assert sim.flags() & ~pkg.FLAG_OUT_OF_DOMAIN == 0, f"device flags {sim.flags()}"
+
+    # grid occupancy for the per-cell byte terms
+    grid = sim.get_grid()
+    active_cells = int(np.count_nonzero(grid["mass"]))
+
+    # roofline pass: the same steps with per-kernel events
+    sim.set_kernel_timing(True)
+    sim.step(sc.dt, args.steps)
+    kt = sim.kernel_timing()
+    sim.set_kernel_timing(False)
+    dom = max(("p2g", "g2p"), key=lambda k: kt[k][1])
+    n_launch, tot_ms = kt[dom]
+    avg_s = tot_ms / max(n_launch, 1) / 1e3
+    bpp, bpc = KERNEL_BYTES[dom]
+    algo_bytes = bpp * sc.n + bpc * active_cells
+    peak, peak_src = measured_peak_hbm()
+    achieved = algo_bytes / avg_s / 1e9
+    step_ms = ms / args.steps
+    step_bytes = STEP_BYTES_PER_PARTICLE * sc.n + STEP_BYTES_PER_CELL * active_cells
+
+    # end to end through the C ABI with host buffers: state in, step, state out
+    fields = ("x", "v", "B", "FE", "Jp", "mass", "volume")
+    shapes = {"x": (sc.n, 3), "v": (sc.n, 3), "B": (sc.n, 9), "FE": (sc.n, 9), "Jp": (sc.n,), "mass": (sc.n,),
+              "volume": (sc.n,)}
+    host = {k: torch.empty(shapes[k], dtype=torch.float32, pin_memory=True).numpy() for k in fields}
+    sim.get_particles(fields, out=host)
+    e2e_steps = max(1, args.e2e_steps)
+    sim.synchronize()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_particles(host["x"], host["v"], host["mass"], B=host["B"], FE=host["FE"], Jp=host["Jp"],
+                          volume=host["volume"], sync=False)
+        sim.step(sc.dt, 1)
+        sim.get_particles(fields, out=host)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(ws, e2e_s, device=torch.device("cuda", local))
+    io_bytes = sum(int(np.prod(shapes[k])) * 4 for k in fields)
+    e2e_value = ws * sc.n * e2e_steps / e2e_s
+
+    out = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": sc.name, "particles_per_gpu": sc.n, "grid": list(sc.grid), "dx": sc.h,
+                   "dt": sc.dt, "material": {k: v for k, v in sc.material.items()}, "bc": "sticky walls, 3 cells",
+                   "active_cells": active_cells, "parallelism": f"{ws} independent replica(s)",
+                   "l2": f"inputs larger than L2: {2 * 7 * 16 * sc.n / 1e6:.0f} MB of particle planes per step"},
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
+                "d2h_bytes_per_step": io_bytes, "steps": e2e_steps,
+                "path": "rd_set_particles(host) + rd_step + rd_get_particles(host), pinned buffers"},
+        "roofline": {"bound": "hbm", "kernel": {"p2g": "k_p2g", "g2p": "k_g2p_fused"}[dom],
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "traffic": None,
+                     "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": avg_s * 1e6},
+        "step_roofline": {"achieved": step_bytes / (step_ms / 1e3) / 1e9, "unit": "GB/s",
+                          "frac": step_bytes / (step_ms / 1e3) / 1e9 / peak,
+                          "bytes_per_step": step_bytes},
+        "kernels_ms_per_step": {k: v[1] / max(v[0], 1) for k, v in kt.items() if v[0]},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and ws == 1 and args.cpu_baseline:
+        v, kind, sample = cpu_baseline_single_core(sc)
+        out["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": kind, "sample": sample}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    sim.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def _reference_worker(args_tuple):
+    name, seed, sample_n, steps, warmup = args_tuple
+    orc = graft.load_oracle()
+    sc = make_scene(name, seed=0)
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(sc.n, size=min(sample_n, sc.n), replace=False))
+    P = orc.Params(*sc.grid, sc.h, **{k: v for k, v in sc.material.items()})
+    x, v, m = sc.x[idx], sc.v[idx], sc.mass[idx]
+    if orc.ref_available():
+        sim, kind = orc.RefSim(P, x, v, m, p4=1), "reference"
+    else:
+        sim, kind = orc.OracleSim(P, x, v, m), "port"
+    sim.init()
+    sim.step(sc.dt, warmup)
+    t0 = time.perf_counter()
+    sim.step(sc.dt, steps)
+    return len(idx) * steps / (time.perf_counter() - t0), kind
+
+
+def run_reference(args):
+    import multiprocessing as mp
+
+    ws, rank, _ = dist_init("gloo") if int(os.environ.get("WORLD_SIZE", "1")) > 1 else (1, 0, 0)
+    if rank != 0:
+        return
+    orc = graft.load_oracle()
+    orc.build_oracle()
+    sc = make_scene(args.workload, seed=0)
+    cores = os.cpu_count() or 1
+    sample_n = min(sc.n, 16384)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_reference_worker, [(args.workload, 1000 + c, sample_n, args.steps, args.warmup)
+                                           for c in range(cores)])
+    value = float(sum(r[0] for r in res))
+    kind = res[0][1]
+    out = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": sc.name, "particles_per_gpu": sc.n, "grid": list(sc.grid), "dx": sc.h,
+                   "dt": sc.dt, "material": {k: v for k, v in sc.material.items()}},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": kind,
+                         "sample": f"{cores} independent single-threaded replicas, each stepping a random "
+                                   f"{sample_n}-particle subset of the workload on its {sc.grid[0]}^3 grid"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+/*
+ * rd_mpm.h - C ABI of the GB300 (sm_103a) explicit APIC / MLS-MPM snow step.
+ *
+ * Drop-in boundary for the simulation core of brocbyte/realtime-deformations:
+ * the class MaterialPointMethod::LagrangeEulerView
+ * (realtime-deformations/material_point_method.hpp:174-233), driven by
+ * main.cpp:48-54,192-218 and read by drawParticles through getParticles()
+ * (main.cpp:255-271).  Each entry point below names the reference interface it
+ * replaces.  Plain C: pointers, sizes and POD structs only; no exceptions cross
+ * the boundary; every call returns an rd_status.
+ *
+ * Threading: one handle is used by one host thread at a time.  Each handle owns
+ * one CUDA stream and all of its device and host buffers; there is no global
+ * mutable state (the reference's global WeightCalculator::h and __constant__
+ * devH become per-handle parameters).
+ *
+ * Element type: every floating-point array crossing the ABI is float when the
+ * handle was created with RD_FP32 and double with RD_FP64.  Matrices are 3x3
+ * row-major in the math sense, M[3*r + c] = M(r, c) (glm stores the transpose).
+ */
+#ifndef RD_MPM_H
+#define RD_MPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rd_status {
+    RD_OK = 0,
+    RD_INVALID_ARG = 1,      /* bad pointer, size or parameter */
+    RD_OOM = 2,              /* device or pinned-host allocation failed */
+    RD_CUDA_ERROR = 3,       /* a CUDA runtime call failed; see rd_last_error */
+    RD_DEVICE_FAULT_FLAG = 4,/* a kernel raised a status flag; see rd_get_flags */
+    RD_TIMEOUT = 5,          /* a bounded device wait gave up */
+    RD_NOT_SUPPORTED = 6
+} rd_status;
+
+enum { RD_FP32 = 0, RD_FP64 = 1 };
+enum { RD_HOST = 0, RD_DEVICE = 1 };
+/* Grid boundary condition applied in the grid update.  The reference has no
+ * grid boundary; it only clamps particle positions to [3h, (MAX-3)h]
+ * (material_point_method.cpp:381-388), which every mode keeps. */
+enum { RD_BC_NONE = 0, RD_BC_STICKY = 1 };
+
+/* Device status flags (sticky until rd_clear_flags). */
+enum {
+    RD_FLAG_OUT_OF_DOMAIN = 1u << 0, /* a stencil node fell outside the grid; dropped */
+    RD_FLAG_NONFINITE = 1u << 1,     /* NaN/Inf in particle state after a step */
+    RD_FLAG_BAD_WORK = 1u << 2       /* internal work-list inconsistency */
+};
+
+/* Stage ids for rd_stage, in the order main.cpp:192-218 calls them. */
+enum {
+    RD_STAGE_RASTERIZE = 0,       /* rasterizeParticlesToGrid, material_point_method.cpp:94-129 */
+    RD_STAGE_FORCES = 1,          /* computeExplicitGridForces, :235-254 */
+    RD_STAGE_GRID_VELOCITIES = 2, /* gridVelocitiesUpdate(dt), :256-262 (+ rd_params.bc) */
+    RD_STAGE_COLLISIONS = 3,      /* gridBasedCollisions(dt, {}), :298-304 (identity) */
+    RD_STAGE_DEFORMATION = 4,     /* updateDeformationGradient(dt), :306-330 */
+    RD_STAGE_PARTICLE_VELOCITIES = 5, /* updateParticleVelocities, :332-342 */
+    RD_STAGE_POSITIONS = 6,       /* updateParticlePositions(dt), :344-350 */
+    RD_STAGE_VOLUMES = 7          /* computeParticleVolumesAndDensities, :131-142 */
+};
+
+/* Replaces the LagrangeEulerView constructor arguments (material_point_method.hpp:178),
+ * the global WeightCalculator::h (material_point_method.cpp:17) and the constants
+ * hard-coded in the step (material_point_method.cpp:237-238,260,320;
+ * material_point_method.hpp:213).  rd_default_params fills the reference's values. */
+typedef struct rd_params {
+    int32_t max_i, max_j, max_k;  /* grid nodes per axis (MAX_I, MAX_J, MAX_K) */
+    int32_t num_particles;        /* particlesNum */
+    double h;                     /* cell size */
+    double E, nu, xi;             /* Young's modulus, Poisson ratio, hardening */
+    double theta_c, theta_s;      /* singular values clamped to [1-theta_c, 1+theta_s] */
+    double gravity[3];
+    int32_t bc;                   /* RD_BC_NONE (reference) or RD_BC_STICKY */
+    int32_t bc_width;             /* sticky wall width in cells (3) */
+    int32_t lagged_b;             /* 1: F update uses B of the previous G2P (reference
+                                     order, main.cpp:209-214); 0: textbook order */
+    int32_t track_fp;             /* 1: also carry the full plastic F_P (for getParticles);
+                                     0: carry J_P = det F_P only */
+    int32_t precision;            /* RD_FP32 or RD_FP64 */
+    int32_t device;               /* CUDA device ordinal */
+} rd_params;
+
+/* Particle arrays, structure of arrays (the reference's Particle,
+ * material_point_method.hpp:96-110, without the per-step neighbour list and the
+ * viewer's colour/size).  Any pointer may be NULL where noted. */
+typedef struct rd_particles {
+    void* x;      /* n x 3 positions (required on set) */
+    void* v;      /* n x 3 velocities (required on set) */
+    void* B;      /* n x 9 APIC B (C = B * DpInverse); NULL on set means 0 */
+    void* FE;     /* n x 9 elastic F; NULL on set means identity */
+    void* FP;     /* n x 9 plastic F; used only when track_fp; NULL means identity */
+    void* Jp;     /* n plastic det; NULL on set means det(FP) or 1 */
+    void* mass;   /* n (required on set) */
+    void* volume; /* n; NULL on set means 0 (call rd_init_volumes) */
+} rd_particles;
+
+typedef struct rd_handle rd_handle;
+
+void rd_default_params(rd_params* p);
+
+/* LagrangeEulerView(max_i, max_j, max_k, particlesNum), material_point_method.cpp:144-154.
+ * Allocates every device buffer once; nothing is allocated per step. */
+rd_status rd_create(const rd_params* params, rd_handle** out);
+/* ~LagrangeEulerView, material_point_method.cpp:156-158 */
+rd_status rd_destroy(rd_handle* h);
+
+/* Writes particle state (initializeParticles / writes through getParticles(),
+ * material_point_method.cpp:18-63, .hpp:181-183).  where = RD_HOST or RD_DEVICE. */
+rd_status rd_set_particles(rd_handle* h, const rd_particles* in, int where);
+/* Reads particle state in the caller's original particle order (getParticles()).
+ * Fields left NULL are skipped. */
+rd_status rd_get_particles(rd_handle* h, rd_particles* out, int where);
+
+/* rasterizeParticlesToGrid + computeParticleVolumesAndDensities, main.cpp:53-54. */
+rd_status rd_init_volumes(rd_handle* h);
+/* nsteps x (the seven stage calls of main.cpp:192-218 with no colliders), fused:
+ * sort, P2G with the MLS force, grid update, G2P with the plastic SVD. */
+rd_status rd_step(rd_handle* h, double dt, int32_t nsteps);
+/* One reference stage at the reference's granularity (RD_STAGE_*). */
+rd_status rd_stage(rd_handle* h, int32_t stage, double dt);
+
+/* Grid fields as the reference's Cell holds them after the last stage run
+ * (material_point_method.hpp:112-117): mass (cells), velocity (cells x 3),
+ * force (cells x 3, rd_stage mode only).  Dense, index i*MAX_J*MAX_K + j*MAX_K + k.
+ * After rd_step the velocity is the updated grid velocity used by G2P. */
+rd_status rd_get_grid(rd_handle* h, void* mass, void* velocity, void* force, int where);
+
+/* Headless stand-in for the viewer's position stream (main.cpp:259-271):
+ * float4 (x, y, z, size) per particle in original order, on the device, valid
+ * until the next mutating call.  Borrowed pointer. */
+rd_status rd_device_xyzs(rd_handle* h, float** xyzs);
+
+rd_status rd_get_flags(rd_handle* h, uint32_t* flags);
+rd_status rd_clear_flags(rd_handle* h);
+rd_status rd_synchronize(rd_handle* h);
+/* The handle's CUDA stream (cudaStream_t), for callers that order their own work. */
+rd_status rd_get_stream(rd_handle* h, void** stream);
+/* Copies the last error message (NUL-terminated, truncated to len). */
+rd_status rd_last_error(rd_handle* h, char* buf, size_t len);
+/* Sort diagnostic: sorts the current particles by 4x4x4-cell block (as every
+ * step does) and returns each particle's block key in original order (n) and
+ * the original index of the particle at each sorted position (n).  The key of
+ * a particle is the block of ivec3(pos / h) (material_point_method.cpp:83),
+ * linearised x-major like the grid.  Host or device arrays per `where`. */
+rd_status rd_debug_sort(rd_handle* h, uint32_t* keys, uint32_t* order, int where);
+/* Kernel ids for the per-kernel event timing below. */
+enum {
+    RD_KERNEL_KEYS = 0,     /* block keys + histogram (when not fused into G2P) */
+    RD_KERNEL_SCAN = 1,     /* scan of the block counts, work items */
+    RD_KERNEL_SCATTER = 2,  /* sorted permutation */
+    RD_KERNEL_GRID_CLEAR = 3,
+    RD_KERNEL_P2G = 4,      /* P2G with the MLS force */
+    RD_KERNEL_G2P = 5,      /* grid update + F update + G2P + advection */
+    RD_KERNEL_COUNT = 6
+};
+/* Per-kernel timing with CUDA events recorded on the handle's stream around
+ * each launch of rd_step (profiling runs; off by default).  rd_kernel_timing
+ * synchronises and returns the launches and total milliseconds accumulated
+ * since timing was enabled or last reset. */
+rd_status rd_set_kernel_timing(rd_handle* h, int enable);
+rd_status rd_kernel_timing(rd_handle* h, int kernel, uint64_t* launches, double* total_ms);
+/* Number of kernel launches issued by this handle so far. */
+rd_status rd_launch_count(rd_handle* h, uint64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RD_MPM_H */

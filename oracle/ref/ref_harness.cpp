@@ -1,0 +1,158 @@
+// Headless C harness around the reference's own MaterialPointMethod::
+// LagrangeEulerView (material_point_method.hpp:174-233).  Test infrastructure:
+// it drives the unmodified step methods in the order main.cpp:192-218 calls
+// them, with an empty collider list, and copies state in and out.
+//
+// Exchange layout: x, v are n x 3; B, FE, FP are n x 9 row-major in the math
+// sense (M[3*r + c] = M(r, c)); glm stores m[c][r] = M(r, c) (column-major).
+// Grid arrays are dense MAX_I*MAX_J*MAX_K in the reference's own index order
+// i*MAX_J*MAX_K + j*MAX_K + k (material_point_method.hpp:129-131).
+#include "material_point_method.hpp"
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+float rd_ref_E = 1.4e5f;
+float rd_ref_nu = 0.2f;
+float rd_ref_xi = 10.0f;
+float rd_ref_gy = (float)-9.8;
+double rd_ref_theta_c = 2.5f * 1e-2;
+double rd_ref_theta_s = 5.0f * 1e-3;
+int rd_ref_p4 = 0;
+
+// cudaCalc.cuh symbols referenced by the (never called) precalculateWeights.
+ftype devH;
+void cuP2G(MaterialPointMethod::Particle*, MaterialPointMethod::Cell*, int, int, int, int, ftype*) {}
+// mesh.hpp declares Mesh::draw without defining it outside the GL build.
+void Mesh::draw() {}
+
+using MaterialPointMethod::LagrangeEulerView;
+
+namespace {
+inline void to_glm(glm::mat3& g, const float* m) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) g[c][r] = m[3 * r + c];
+}
+inline void from_glm(float* m, const glm::mat3& g) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) m[3 * r + c] = g[c][r];
+}
+}  // namespace
+
+extern "C" {
+
+void rdref_set_params(float E, float nu, float xi, float gy, double theta_c, double theta_s, int p4) {
+    rd_ref_E = E;
+    rd_ref_nu = nu;
+    rd_ref_xi = xi;
+    rd_ref_gy = gy;
+    rd_ref_theta_c = theta_c;
+    rd_ref_theta_s = theta_s;
+    rd_ref_p4 = p4;
+}
+
+// h must be set before construction: DpInverse is initialised from it
+// (material_point_method.hpp:177).
+void* rdref_create(int mi, int mj, int mk, int n, float h) {
+    MaterialPointMethod::WeightCalculator::h = h;
+    auto* s = new LagrangeEulerView(mi, mj, mk, n);
+    s->setLevel(Logger::LogLevel::ERROR);
+    return s;
+}
+
+void rdref_destroy(void* p) { delete static_cast<LagrangeEulerView*>(p); }
+
+float rdref_dp_inverse(void* p) { return static_cast<LagrangeEulerView*>(p)->DpInverse[0][0]; }
+
+void rdref_set_particles(void* p, const float* x, const float* v, const float* mass,
+                         const float* B, const float* FE, const float* FP, const float* vol) {
+    auto* s = static_cast<LagrangeEulerView*>(p);
+    auto* ps = s->getParticles();
+    for (int i = 0; i < s->getNumParticles(); ++i) {
+        auto& q = ps[i];
+        q.pos = glm::vec3(x[3 * i], x[3 * i + 1], x[3 * i + 2]);
+        q.velocity = glm::vec3(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+        q.mass = mass[i];
+        if (B) to_glm(q.B, B + 9 * i); else q.B = glm::mat3(0.0f);
+        if (FE) to_glm(q.FElastic, FE + 9 * i); else q.FElastic = glm::mat3(1.0f);
+        if (FP) to_glm(q.FPlastic, FP + 9 * i); else q.FPlastic = glm::mat3(1.0f);
+        q.volume = vol ? vol[i] : 0.0f;
+    }
+}
+
+void rdref_get_particles(void* p, float* x, float* v, float* B, float* FE, float* FP, float* vol) {
+    auto* s = static_cast<LagrangeEulerView*>(p);
+    const auto* ps = s->getParticles();
+    for (int i = 0; i < s->getNumParticles(); ++i) {
+        const auto& q = ps[i];
+        for (int a = 0; a < 3; ++a) {
+            if (x) x[3 * i + a] = q.pos[a];
+            if (v) v[3 * i + a] = q.velocity[a];
+        }
+        if (B) from_glm(B + 9 * i, q.B);
+        if (FE) from_glm(FE + 9 * i, q.FElastic);
+        if (FP) from_glm(FP + 9 * i, q.FPlastic);
+        if (vol) vol[i] = q.volume;
+    }
+}
+
+void rdref_get_mass(void* p, float* mass) {
+    auto* s = static_cast<LagrangeEulerView*>(p);
+    const auto* ps = s->getParticles();
+    for (int i = 0; i < s->getNumParticles(); ++i) mass[i] = ps[i].mass;
+}
+
+// Cell fields as the reference holds them at the time of the call.
+void rdref_get_grid(void* p, float* mass, float* vel, float* force) {
+    auto* s = static_cast<LagrangeEulerView*>(p);
+    const size_t n = s->grid.grid.size();
+    for (size_t c = 0; c < n; ++c) {
+        const auto& cell = s->grid.grid[c];
+        if (mass) mass[c] = cell.mass;
+        for (int a = 0; a < 3; ++a) {
+            if (vel) vel[3 * c + a] = cell.velocity[a];
+            if (force) force[3 * c + a] = cell.force[a];
+        }
+    }
+}
+
+// Stage ids follow main.cpp:192-218; 0 = rasterize, 1 = forces, 2 = grid
+// velocities, 3 = collisions (empty list), 4 = deformation gradient,
+// 5 = particle velocities, 6 = positions, 7 = volumes (main.cpp:54).
+void rdref_stage(void* p, int stage, float dt) {
+    auto* s = static_cast<LagrangeEulerView*>(p);
+    static const std::vector<MaterialPointMethod::MeshCollider> none;
+    switch (stage) {
+        case 0: s->rasterizeParticlesToGrid(); break;
+        case 1: s->computeExplicitGridForces(); break;
+        case 2: s->gridVelocitiesUpdate(dt); break;
+        case 3: s->gridBasedCollisions(dt, none); break;
+        case 4: s->updateDeformationGradient(dt); break;
+        case 5: s->updateParticleVelocities(); break;
+        case 6: s->updateParticlePositions(dt); break;
+        case 7: s->computeParticleVolumesAndDensities(); break;
+        default: break;
+    }
+}
+
+// The reference's own particle initialiser (material_point_method.cpp:18-63):
+// a jittered 8-per-cell sphere drawn with the C library's rand(); main.cpp:52
+// runs it before seeding, i.e. with seed 1.
+void rdref_initialize_particles(void* p, unsigned seed, float ox, float oy, float oz, float vx, float vy, float vz) {
+    srand(seed);
+    static_cast<LagrangeEulerView*>(p)->initializeParticles(glm::vec3(ox, oy, oz), glm::vec3(vx, vy, vz));
+}
+
+// main.cpp:53-54
+void rdref_init(void* p) {
+    rdref_stage(p, 0, 0.0f);
+    rdref_stage(p, 7, 0.0f);
+}
+
+// main.cpp:192-218, nsteps times.
+void rdref_step(void* p, float dt, int nsteps) {
+    for (int s = 0; s < nsteps; ++s)
+        for (int st = 0; st <= 6; ++st) rdref_stage(p, st, dt);
+}
+
+}  // extern "C"

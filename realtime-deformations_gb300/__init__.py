@@ -1,0 +1,344 @@
+"""GB300 (sm_103a) explicit APIC / MLS-MPM snow step behind the C ABI of
+``include/rd_mpm.h`` - Python host side.
+
+Two layers, both thin ctypes front ends over ``librd_mpm.so`` (built in-tree
+from ``csrc/`` by :func:`build`):
+
+* :class:`Simulation` - one ``rd_handle``: particle upload/download, the fused
+  step, the reference's individual stages, the grid.
+* :class:`LagrangeEulerView` - the reference's simulation class
+  (realtime-deformations/material_point_method.hpp:174-233) with its method
+  names, so a ``main.cpp``-style driver reads the same.
+
+There is no CPU fallback: every call goes to the CUDA library and fails loudly
+(``RuntimeError``) when it is missing or returns an error.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+LIB_PATH = os.path.join(PKG_DIR, "librd_mpm.so")
+HEADER = os.path.join(REPO_DIR, "include", "rd_mpm.h")
+
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
+              "-Xcompiler", "-fPIC,-ffp-contract=off", "-shared"]
+
+RD_OK, RD_INVALID_ARG, RD_OOM, RD_CUDA_ERROR, RD_DEVICE_FAULT_FLAG, RD_TIMEOUT, RD_NOT_SUPPORTED = range(7)
+STATUS_NAMES = {0: "RD_OK", 1: "RD_INVALID_ARG", 2: "RD_OOM", 3: "RD_CUDA_ERROR",
+                4: "RD_DEVICE_FAULT_FLAG", 5: "RD_TIMEOUT", 6: "RD_NOT_SUPPORTED"}
+RD_FP32, RD_FP64 = 0, 1
+RD_HOST, RD_DEVICE = 0, 1
+RD_BC_NONE, RD_BC_STICKY = 0, 1
+FLAG_OUT_OF_DOMAIN, FLAG_NONFINITE, FLAG_BAD_WORK = 1, 2, 4
+STAGES = {"rasterize": 0, "forces": 1, "grid_velocities": 2, "collisions": 3,
+          "deformation": 4, "particle_velocities": 5, "positions": 6, "volumes": 7}
+
+# Every symbol include/rd_mpm.h declares.
+EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "rd_get_particles",
+           "rd_init_volumes", "rd_step", "rd_stage", "rd_get_grid", "rd_device_xyzs", "rd_get_flags",
+           "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort",
+           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count")
+KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p")
+
+
+def _sources():
+    return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cuh", ".h"))] + [HEADER]
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile ``csrc/rd_mpm.cu`` for sm_103a into ``librd_mpm.so`` (in-tree)."""
+    newest = max(os.path.getmtime(f) for f in _sources())
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
+        return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    cmd = ["nvcc", *NVCC_FLAGS, os.path.join(CSRC, "rd_mpm.cu"), "-o", tmp]
+    if verbose:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd, cwd=CSRC)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+class Params(ctypes.Structure):
+    """Mirror of ``rd_params``."""
+    _fields_ = [("max_i", ctypes.c_int32), ("max_j", ctypes.c_int32), ("max_k", ctypes.c_int32),
+                ("num_particles", ctypes.c_int32), ("h", ctypes.c_double), ("E", ctypes.c_double),
+                ("nu", ctypes.c_double), ("xi", ctypes.c_double), ("theta_c", ctypes.c_double),
+                ("theta_s", ctypes.c_double), ("gravity", ctypes.c_double * 3), ("bc", ctypes.c_int32),
+                ("bc_width", ctypes.c_int32), ("lagged_b", ctypes.c_int32), ("track_fp", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("device", ctypes.c_int32)]
+
+
+class _Particles(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("x", "v", "B", "FE", "FP", "Jp", "mass", "volume")]
+
+
+_LIB = None
+_LIB_LOCK = threading.Lock()
+
+
+def lib():
+    """The loaded CUDA library; raises if it has not been built."""
+    global _LIB
+    with _LIB_LOCK:
+        if _LIB is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"CUDA library not built: {LIB_PATH} (run build())")
+            L = ctypes.CDLL(LIB_PATH)
+            vp, st = ctypes.c_void_p, ctypes.c_int
+            L.rd_default_params.argtypes = [ctypes.POINTER(Params)]
+            L.rd_default_params.restype = None
+            L.rd_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(vp)]
+            L.rd_destroy.argtypes = [vp]
+            L.rd_set_particles.argtypes = [vp, ctypes.POINTER(_Particles), ctypes.c_int]
+            L.rd_get_particles.argtypes = [vp, ctypes.POINTER(_Particles), ctypes.c_int]
+            L.rd_init_volumes.argtypes = [vp]
+            L.rd_step.argtypes = [vp, ctypes.c_double, ctypes.c_int32]
+            L.rd_stage.argtypes = [vp, ctypes.c_int32, ctypes.c_double]
+            L.rd_get_grid.argtypes = [vp, vp, vp, vp, ctypes.c_int]
+            L.rd_device_xyzs.argtypes = [vp, ctypes.POINTER(vp)]
+            L.rd_get_flags.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
+            L.rd_clear_flags.argtypes = [vp]
+            L.rd_synchronize.argtypes = [vp]
+            L.rd_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+            L.rd_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+            L.rd_debug_sort.argtypes = [vp, vp, vp, ctypes.c_int]
+            L.rd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+            L.rd_set_kernel_timing.argtypes = [vp, ctypes.c_int]
+            L.rd_kernel_timing.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64),
+                                           ctypes.POINTER(ctypes.c_double)]
+            for name in EXPORTS:
+                if name != "rd_default_params":
+                    getattr(L, name).restype = st
+            _LIB = L
+    return _LIB
+
+
+def default_params() -> Params:
+    p = Params()
+    lib().rd_default_params(ctypes.byref(p))
+    return p
+
+
+def make_params(max_i, max_j, max_k, num_particles, h, *, E=1.4e5, nu=0.2, xi=10.0, theta_c=2.5e-2,
+                theta_s=5.0e-3, gravity=(0.0, -9.8, 0.0), bc=RD_BC_NONE, bc_width=3, lagged_b=1,
+                track_fp=0, precision=RD_FP32, device=0) -> Params:
+    p = Params()
+    p.max_i, p.max_j, p.max_k, p.num_particles = max_i, max_j, max_k, num_particles
+    p.h, p.E, p.nu, p.xi, p.theta_c, p.theta_s = h, E, nu, xi, theta_c, theta_s
+    p.gravity = (ctypes.c_double * 3)(*gravity)
+    p.bc, p.bc_width, p.lagged_b, p.track_fp, p.precision, p.device = bc, bc_width, lagged_b, track_fp, precision, device
+    return p
+
+
+class RDError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Simulation:
+    """One ``rd_handle``.  Arrays are numpy on the host (float32 for RD_FP32,
+    float64 for RD_FP64) or, for ``where=RD_DEVICE``, raw device pointers."""
+
+    def __init__(self, params: Params):
+        self.params = params
+        self.n = params.num_particles
+        self.dtype = np.float64 if params.precision == RD_FP64 else np.float32
+        self._h = ctypes.c_void_p()
+        L = lib()
+        s = L.rd_create(ctypes.byref(params), ctypes.byref(self._h))
+        if s != RD_OK:
+            raise RDError(s, "rd_create failed")
+
+    def close(self):
+        if self._h:
+            lib().rd_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, status, what):
+        if status != RD_OK:
+            buf = ctypes.create_string_buffer(512)
+            lib().rd_last_error(self._h, buf, 512)
+            raise RDError(status, f"{what}: {buf.value.decode(errors='replace')}")
+
+    def _arr(self, a, shape):
+        if a is None:
+            return None
+        return np.ascontiguousarray(np.asarray(a, self.dtype).reshape(shape))
+
+    def set_particles(self, x, v, mass, B=None, FE=None, FP=None, Jp=None, volume=None, sync=True):
+        """Copies host arrays in (rd_set_particles).  With sync=False the call
+        returns once the copies are queued; the arrays must stay alive and
+        unchanged until the handle's stream reaches them."""
+        n = self.n
+        arrs = {"x": self._arr(x, (n, 3)), "v": self._arr(v, (n, 3)), "B": self._arr(B, (n, 9)),
+                "FE": self._arr(FE, (n, 9)), "FP": self._arr(FP, (n, 9)), "Jp": self._arr(Jp, (n,)),
+                "mass": self._arr(mass, (n,)), "volume": self._arr(volume, (n,))}
+        ps = _Particles(**{k: (a.ctypes.data if a is not None else None) for k, a in arrs.items()})
+        self._check(lib().rd_set_particles(self._h, ctypes.byref(ps), RD_HOST), "rd_set_particles")
+        if sync:
+            self._check(lib().rd_synchronize(self._h), "rd_synchronize")
+
+    def get_particles(self, fields=("x", "v", "B", "FE", "FP", "Jp", "mass", "volume"), out=None):
+        """Copies the particle state out in the original particle order
+        (rd_get_particles).  ``out`` may supply the destination arrays."""
+        n = self.n
+        shapes = {"x": (n, 3), "v": (n, 3), "B": (n, 9), "FE": (n, 9), "FP": (n, 9), "Jp": (n,),
+                  "mass": (n,), "volume": (n,)}
+        if out is None:
+            out = {k: np.zeros(shapes[k], self.dtype) for k in fields}
+        for k in fields:
+            a = out[k]
+            if a.shape != shapes[k] or a.dtype != self.dtype or not a.flags.c_contiguous:
+                raise ValueError(f"out[{k!r}] must be a contiguous {self.dtype.__name__} array of shape {shapes[k]}")
+        ps = _Particles(**{k: (out[k].ctypes.data if k in fields else None) for k in shapes})
+        self._check(lib().rd_get_particles(self._h, ctypes.byref(ps), RD_HOST), "rd_get_particles")
+        return out
+
+    def init_volumes(self):
+        self._check(lib().rd_init_volumes(self._h), "rd_init_volumes")
+
+    def step(self, dt: float, nsteps: int = 1):
+        self._check(lib().rd_step(self._h, float(dt), int(nsteps)), "rd_step")
+
+    def stage(self, name: str, dt: float = 0.0):
+        self._check(lib().rd_stage(self._h, STAGES[name], float(dt)), f"rd_stage({name})")
+
+    def get_grid(self, force: bool = False):
+        p = self.params
+        nc = p.max_i * p.max_j * p.max_k
+        m = np.zeros(nc, self.dtype)
+        v = np.zeros((nc, 3), self.dtype)
+        f = np.zeros((nc, 3), self.dtype) if force else None
+        self._check(lib().rd_get_grid(self._h, m.ctypes.data, v.ctypes.data,
+                                      f.ctypes.data if f is not None else None, RD_HOST), "rd_get_grid")
+        out = {"mass": m, "vel": v}
+        if f is not None:
+            out["force"] = f
+        return out
+
+    def device_xyzs(self) -> int:
+        ptr = ctypes.c_void_p()
+        self._check(lib().rd_device_xyzs(self._h, ctypes.byref(ptr)), "rd_device_xyzs")
+        return ptr.value
+
+    def flags(self) -> int:
+        f = ctypes.c_uint32()
+        self._check(lib().rd_get_flags(self._h, ctypes.byref(f)), "rd_get_flags")
+        return f.value
+
+    def clear_flags(self):
+        self._check(lib().rd_clear_flags(self._h), "rd_clear_flags")
+
+    def synchronize(self):
+        self._check(lib().rd_synchronize(self._h), "rd_synchronize")
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._check(lib().rd_get_stream(self._h, ctypes.byref(s)), "rd_get_stream")
+        return s.value or 0
+
+    def debug_sort(self):
+        """(block key per particle in original order, original index per sorted slot)."""
+        keys = np.zeros(self.n, np.uint32)
+        order = np.zeros(self.n, np.uint32)
+        self._check(lib().rd_debug_sort(self._h, keys.ctypes.data, order.ctypes.data, RD_HOST), "rd_debug_sort")
+        return keys, order
+
+    def set_kernel_timing(self, enable: bool):
+        self._check(lib().rd_set_kernel_timing(self._h, int(enable)), "rd_set_kernel_timing")
+
+    def kernel_timing(self):
+        """{kernel name: (launches, total ms)} since timing was enabled."""
+        out = {}
+        for k, name in enumerate(KERNELS):
+            n, ms = ctypes.c_uint64(), ctypes.c_double()
+            self._check(lib().rd_kernel_timing(self._h, k, ctypes.byref(n), ctypes.byref(ms)), "rd_kernel_timing")
+            out[name] = (n.value, ms.value)
+        return out
+
+    def launch_count(self) -> int:
+        c = ctypes.c_uint64()
+        self._check(lib().rd_launch_count(self._h, ctypes.byref(c)), "rd_launch_count")
+        return c.value
+
+
+class LagrangeEulerView:
+    """The reference's ``MaterialPointMethod::LagrangeEulerView`` interface
+    (material_point_method.hpp:174-233) over :class:`Simulation`.
+
+    ``h`` replaces the global ``WeightCalculator::h`` that the reference reads at
+    construction (material_point_method.hpp:177).  Stage methods run the
+    corresponding GPU stage; :meth:`step` is the fused fast path that the seven
+    stage calls of main.cpp:192-218 amount to.  :meth:`getParticles` returns a
+    host copy (dict of arrays) synchronised from the device.
+    """
+
+    def __init__(self, max_i: int, max_j: int, max_k: int, particlesNum: int, h: float = 0.05, **kw):
+        self.MAX_I, self.MAX_J, self.MAX_K = max_i, max_j, max_k
+        kw.setdefault("track_fp", 1)
+        self.sim = Simulation(make_params(max_i, max_j, max_k, particlesNum, h, **kw))
+        self.h = h
+
+    def getNumParticles(self) -> int:
+        return self.sim.n
+
+    def setParticles(self, x, v, mass, **kw):
+        self.sim.set_particles(x, v, mass, **kw)
+
+    def getParticles(self):
+        return self.sim.get_particles()
+
+    def rasterizeParticlesToGrid(self):
+        self.sim.stage("rasterize")
+
+    def computeParticleVolumesAndDensities(self):
+        self.sim.stage("volumes")
+
+    def computeExplicitGridForces(self):
+        self.sim.stage("forces")
+
+    def gridVelocitiesUpdate(self, timeDelta: float):
+        self.sim.stage("grid_velocities", timeDelta)
+
+    def gridBasedCollisions(self, timeDelta: float, objects=()):
+        if len(objects):
+            raise NotImplementedError("SDF colliders are not part of this path")
+        self.sim.stage("collisions", timeDelta)
+
+    def updateDeformationGradient(self, timeDelta: float):
+        self.sim.stage("deformation", timeDelta)
+
+    def updateParticleVelocities(self):
+        self.sim.stage("particle_velocities")
+
+    def updateParticlePositions(self, timeDelta: float):
+        self.sim.stage("positions", timeDelta)
+
+    def step(self, timeDelta: float, nsteps: int = 1):
+        self.sim.step(timeDelta, nsteps)

@@ -1,0 +1,95 @@
+"""Generates the golden fixtures in this directory from the reference itself:
+the headless build of brocbyte/realtime-deformations' own LagrangeEulerView
+(oracle/ref/build_ref.sh), driven through oracle/oracle.py's RefSim.
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+Fixtures (all FP32, matrices row-major n x 9, grids as sparse cell lists):
+
+* ref_scene_20.npz - the reference's own scene (main.cpp:48-54,170): 20^3 grid,
+  h = 0.05, 2147 particles from initializeParticles((0.5, 0.6, 0.5),
+  (0, -200, 0)) with rand() seed 1, dt = 1e-5.  Inputs, volumes after the
+  init rasterize, the state after 1 step (unmodified reference) with that
+  step's grid, and after 3 steps with the plastic split of F_E itself (P4).
+* perturbed_16.npz - 512 particles in a sphere on a 16^3 grid, h = 1/16,
+  random velocities, random APIC B and near-identity F_E, F_P, dt = 1e-4:
+  the state after 1 and 2 steps (P4) and the step-1 grid.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+from oracle import oracle as orc  # noqa: E402
+
+
+def sparse_grid(g):
+    idx = np.nonzero((g["mass"] != 0) | np.any(g["force"] != 0, axis=1) | np.any(g["vel"] != 0, axis=1))[0]
+    return {"grid_idx": idx.astype(np.int32), "grid_mass": g["mass"][idx], "grid_vel": g["vel"][idx],
+            "grid_force": g["force"][idx]}
+
+
+def state(prefix, p):
+    return {f"{prefix}_{k}": v for k, v in p.items()}
+
+
+def ref_scene():
+    P = orc.Params(20, 20, 20, 0.05)
+    r = orc.RefSim(P, n=2147, p4=0)
+    r.initialize_particles((0.5, 0.6, 0.5), (0.0, -200.0, 0.0), seed=1)
+    p0 = r.particles()
+    m0 = r.masses()
+    assert np.all(m0 > 0), "initializer left particles unplaced"
+    out = {"grid": np.array([20, 20, 20]), "h": np.float32(0.05), "dt": np.float32(1e-5), "n": 2147,
+           "x0": p0["x"], "v0": p0["v"], "m0": m0}
+    r.init()
+    out["vol0"] = r.particles()["vol"]
+    r.step(1e-5, 1)
+    out.update(state("s1", r.particles()))
+    out.update(sparse_grid(r.grid()))
+    r.p4 = 1
+    r.step(1e-5, 2)
+    out.update(state("s3", r.particles()))
+    return out
+
+
+def perturbed():
+    rng = np.random.default_rng(1234)
+    n, G = 512, 16
+    h = np.float32(1.0 / G)
+    P = orc.Params(G, G, G, float(h))
+    dinv = float(orc.reference_dinv(h))
+    d = rng.normal(size=(4 * n, 3))
+    d = d / np.linalg.norm(d, axis=1, keepdims=True) * (rng.uniform(size=(4 * n, 1)) ** (1 / 3)) * 0.22
+    x = (d[:n] + np.array([0.5, 0.5, 0.5])).astype(np.float32)
+    v = rng.normal(0, 1.0, (n, 3)).astype(np.float32)
+    m = rng.uniform(0.5e-4, 1.5e-4, n).astype(np.float32)
+    B = (rng.normal(0, 0.5, (n, 9)) / dinv).astype(np.float32)
+    FE = (np.eye(3).reshape(1, 9) + rng.normal(0, 4e-3, (n, 9))).astype(np.float32)
+    FP = (np.eye(3).reshape(1, 9) + rng.normal(0, 4e-3, (n, 9))).astype(np.float32)
+    r = orc.RefSim(P, x, v, m, B, FE, FP, p4=1)
+    out = {"grid": np.array([G, G, G]), "h": h, "dt": np.float32(1e-4), "n": n,
+           "x0": x, "v0": v, "m0": m, "B0": B, "FE0": FE, "FP0": FP}
+    r.init()
+    out["vol0"] = r.particles()["vol"]
+    r.step(1e-4, 1)
+    out.update(state("s1", r.particles()))
+    out.update(sparse_grid(r.grid()))
+    r.step(1e-4, 1)
+    out.update(state("s2", r.particles()))
+    return out
+
+
+def main():
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if not orc.build_ref(root):
+        raise SystemExit("headless reference not available")
+    np.savez_compressed(os.path.join(HERE, "ref_scene_20.npz"), **ref_scene())
+    np.savez_compressed(os.path.join(HERE, "perturbed_16.npz"), **perturbed())
+
+
+if __name__ == "__main__":
+    main()

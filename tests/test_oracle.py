@@ -1,0 +1,171 @@
+"""CPU tests of the oracle itself: the C restatement against the reference's own
+outputs (committed golden fixtures, and the headless reference build where it
+exists on this machine), plus analytic known-answer checks."""
+import numpy as np
+import pytest
+
+from conftest import b_scale, golden, rel, rel_floor
+
+
+def _params(orc, g, **kw):
+    G = [int(v) for v in g["grid"]]
+    return orc.Params(*G, float(g["h"]), **kw)
+
+
+def test_weights_partition_of_unity_and_linear_reproduction(orc):
+    lib = orc._lib(np.float32)
+    rng = np.random.default_rng(0)
+    for t in rng.uniform(3.0, 60.0, 200).astype(np.float32):
+        base = int(t)
+        f = float(t) - base
+        w = [lib.orc_weight(np.float32(t - np.float32(base + o))) for o in range(-2, 3)]
+        assert w[0] == 0.0  # offset -2 of the reference's 125-node stencil
+        assert abs(sum(w) - 1.0) < 1e-6
+        assert abs(sum(wi * (o - f) for wi, o in zip(w, range(-2, 3)))) < 1e-6
+
+
+def test_svd_reconstruction(orc):
+    rng = np.random.default_rng(1)
+    mats = [rng.normal(size=(3, 3)) for _ in range(50)]
+    mats += [np.eye(3) + 1e-3 * rng.normal(size=(3, 3)) for _ in range(50)]
+    mats += [np.diag([2.0, 2.0, 0.5]), np.diag([1.0, 1.0, 1.0]), np.diag([-1.0, 2.0, 3.0]),
+             np.outer([1.0, 2.0, 3.0], [0.5, -1.0, 2.0]), np.zeros((3, 3))]
+    for F in mats:
+        W, s, Z = orc.svd3(F)
+        assert np.all(s >= 0) and np.all(np.diff(s) <= 1e-12)
+        assert np.allclose(W @ np.diag(s) @ Z.T, F, atol=1e-10 * max(1.0, np.abs(F).max()))
+        assert np.allclose(W.T @ W, np.eye(3), atol=1e-10)
+        assert np.allclose(Z.T @ Z, np.eye(3), atol=1e-10)
+
+
+def test_oracle_matches_reference_scene_golden(orc):
+    """The reference's own main.cpp scene: init volumes and rasterize are
+    bit-exact; one full step agrees to FP32 rounding."""
+    g = golden("ref_scene_20.npz")
+    o = orc.OracleSim(_params(orc, g), g["x0"], g["v0"], g["m0"])
+    o.init()
+    assert np.array_equal(o.vol, g["vol0"])
+    o.step(float(g["dt"]), 1)
+    assert np.array_equal(o.gmass[g["grid_idx"]], g["grid_mass"])
+    assert rel(o.gvel[g["grid_idx"]], g["grid_vel"]) < 1e-6
+    assert rel(o.gforce[g["grid_idx"]], g["grid_force"]) < 1e-6
+    for k, a in (("x", o.x), ("v", o.v), ("B", o.B), ("FE", o.FE), ("FP", o.FP)):
+        assert rel(a, g[f"s1_{k}"]) < 1e-6, k
+    o.step(float(g["dt"]), 2)  # P4 split from here on (the fixture's s3)
+    for k, a in (("x", o.x), ("v", o.v), ("FE", o.FE), ("FP", o.FP)):
+        assert rel(a, g[f"s3_{k}"]) < 1e-5, k
+    # a rigid fall: B is rounding noise, judged against its scale ||v|| h
+    assert rel_floor(o.B, g["s3_B"], b_scale(g["s3_v"], float(g["h"]))) < 1e-6
+
+
+def test_oracle_matches_perturbed_golden(orc):
+    g = golden("perturbed_16.npz")
+    o = orc.OracleSim(_params(orc, g), g["x0"], g["v0"], g["m0"], g["B0"], g["FE0"], g["FP0"])
+    o.init()
+    assert np.array_equal(o.vol, g["vol0"])
+    o.step(float(g["dt"]), 1)
+    assert np.array_equal(o.gmass[g["grid_idx"]], g["grid_mass"])
+    assert rel(o.gvel[g["grid_idx"]], g["grid_vel"]) < 1e-6
+    assert rel(o.gforce[g["grid_idx"]], g["grid_force"]) < 1e-6
+    for k, a in (("x", o.x), ("v", o.v), ("B", o.B), ("FE", o.FE), ("FP", o.FP)):
+        assert rel(a, g[f"s1_{k}"]) < 1e-6, k
+    o.step(float(g["dt"]), 1)
+    # Second step: F_E entered it with a 1-ulp difference (the reference splits
+    # it with Eigen's FP32 SVD, the oracle in FP64), and F - R is ~4e-3 here, so
+    # the stress and with it v and B inherit ~1e-4 relative FP32 noise.
+    for k, a, tol in (("x", o.x, 1e-6), ("v", o.v, 2e-4), ("B", o.B, 2e-4), ("FE", o.FE, 1e-5),
+                      ("FP", o.FP, 1e-5)):
+        assert rel(a, g[f"s2_{k}"]) < tol, k
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_oracle_matches_live_reference_stagewise(orc, seed):
+    if not orc.ref_available():
+        pytest.skip("headless reference not built on this machine")
+    from rd_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    G, n = 20, 700
+    h = np.float32(1.0 / G)
+    P = orc.Params(G, G, G, float(h), theta_s=7.5e-3)
+    x = scenes.uniform_ball(rng, n, (0.5, 0.55, 0.45), 0.2).astype(np.float32)
+    v = rng.normal(0, 2, (n, 3)).astype(np.float32)
+    m = np.full(n, 2e-4, np.float32)
+    B, FE, FP = scenes.perturbed_state(rng, n, 0.3, 3e-3, float(orc.reference_dinv(h)))
+    r = orc.RefSim(P, x, v, m, B, FE, FP, p4=1)
+    o = orc.OracleSim(P, x, v, m, B, FE, FP)
+    r.init()
+    o.init()
+    assert np.array_equal(r.particles()["vol"], o.vol)
+    for st, dt in (("rasterize", 0), ("forces", 0), ("grid_velocities", 1e-4), ("update_F", 1e-4),
+                   ("g2p", 0), ("advect", 1e-4)):
+        r.stage(st, dt)
+        o.stage(st, dt)
+        rg, rp = r.grid(), r.particles()
+        assert np.array_equal(rg["mass"], o.gmass), st
+        assert rel(o.gvel, rg["vel"]) < 1e-6, st
+        assert rel(o.gforce, rg["force"]) < 1e-6, st
+        for k in ("x", "v", "B", "FE", "FP"):
+            assert rel(getattr(o, k), rp[k]) < 1e-6, (st, k)
+
+
+def test_oracle_unpatched_reference_keeps_total_F_and_Jp(orc):
+    """Without P4 the reference's F_E differs (glm/Eigen transpose), but the
+    total F = F_E F_P and det F_P do not."""
+    g = golden("perturbed_16.npz")
+    o = orc.OracleSim(_params(orc, g), g["x0"], g["v0"], g["m0"], g["B0"], g["FE0"], g["FP0"])
+    o.init()
+    o.step(float(g["dt"]), 1)
+    if not orc.ref_available():
+        pytest.skip("headless reference not built on this machine")
+    r = orc.RefSim(_params(orc, g), g["x0"], g["v0"], g["m0"], g["B0"], g["FE0"], g["FP0"], p4=0)
+    r.init()
+    r.step(float(g["dt"]), 1)
+    rp = r.particles()
+    Fr = np.einsum("nij,njk->nik", rp["FE"].reshape(-1, 3, 3).astype(np.float64), rp["FP"].reshape(-1, 3, 3))
+    Fo = np.einsum("nij,njk->nik", o.FE.reshape(-1, 3, 3).astype(np.float64), o.FP.reshape(-1, 3, 3))
+    assert rel(Fo, Fr) < 1e-6
+    assert rel(o.Jp, np.linalg.det(rp["FP"].reshape(-1, 3, 3).astype(np.float64))) < 1e-5
+    assert rel(o.FE, rp["FE"]) > 1e-4  # the quirk is real
+
+
+def test_oracle_rollout_conserves_grid_mass(orc):
+    from rd_gb300 import scenes
+    sc = scenes.snowball(seed=2, n=2000, grid=32)
+    P = orc.Params(32, 32, 32, sc.h, theta_s=7.5e-3)
+    o = orc.OracleSim(P, sc.x, sc.v, sc.mass)
+    o.init()
+    total = float(np.sum(sc.mass, dtype=np.float64))
+    for _ in range(10):
+        o.step(sc.dt, 1)
+        assert abs(float(np.sum(o.gmass, dtype=np.float64)) - total) / total < 1e-6
+
+
+def test_oracle_rigid_translation(orc):
+    """Uniform velocity, B = 0, F = I, no gravity: the grid reproduces the
+    velocity and the particles advect by v dt."""
+    rng = np.random.default_rng(5)
+    n, G = 400, 24
+    h = 1.0 / G
+    x = (rng.uniform(0.3, 0.7, (n, 3))).astype(np.float32)
+    v = np.tile(np.array([0.7, -0.3, 0.2], np.float32), (n, 1))
+    P = orc.Params(G, G, G, h, gravity=(0.0, 0.0, 0.0))
+    o = orc.OracleSim(P, x, v, np.full(n, 1e-4, np.float32), dtype=np.float64)
+    o.init()
+    o.step(1e-4, 1)
+    assert np.allclose(o.v, v, atol=1e-12)
+    assert np.allclose(o.x, x.astype(np.float64) + 1e-4 * v, atol=1e-12)
+    assert np.abs(o.B).max() < 1e-12
+
+
+@pytest.mark.parametrize("steps,tol", [(1, 1e-5), (2, 5e-5)])
+def test_fp64_oracle_close_to_fp32(orc, steps, tol):
+    """The FP32 step's own error against FP64 on the stiff perturbed scene:
+    about 4e-6 in v and B after one step, 2e-5 after two (F - R ~ 4e-3)."""
+    g = golden("perturbed_16.npz")
+    o32 = orc.OracleSim(_params(orc, g), g["x0"], g["v0"], g["m0"], g["B0"], g["FE0"], g["FP0"])
+    o64 = orc.OracleSim(_params(orc, g), g["x0"], g["v0"], g["m0"], g["B0"], g["FE0"], g["FP0"], dtype=np.float64)
+    for o in (o32, o64):
+        o.init()
+        o.step(float(g["dt"]), steps)
+    for k in ("x", "v", "B", "FE", "FP"):
+        assert rel(getattr(o32, k), getattr(o64, k)) < tol, k
