@@ -9,13 +9,12 @@
 namespace rd {
 
 // Particles are bucketed by 4x4x4-cell blocks of their base cell; a work item
-// is (block key, first sorted index, count <= kWorkP).  Every stencil node of a
+// is (block key, first sorted index, count <= WorkP<T>).  Every stencil node of a
 // particle whose base cell lies in block b is inside the 7^3-node tile whose
 // origin is 4b - 1, so P2G and G2P never leave their shared-memory tile.
 constexpr int kBlk = 4;
 constexpr int kTile = kBlk + 3;
 constexpr int kTileCells = kTile * kTile * kTile;
-constexpr int kWorkP = 256;
 constexpr int kThreads = 128;
 
 template <typename T> struct DevParams {
@@ -96,7 +95,8 @@ __global__ void __launch_bounds__(256) k_keys(DevParams<T> P, const vec4<T>* __r
 constexpr int kScanK = 16;
 __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
                                                int4* __restrict__ work, uint32_t* __restrict__ nwork, int nkeys,
-                                               uint32_t n_expected, uint32_t work_cap, uint32_t* flags) {
+                                               uint32_t n_expected, uint32_t work_cap, uint32_t wp,
+                                               uint32_t* flags) {
     __shared__ uint32_t s_c[32], s_i[32];
     __shared__ uint32_t carry_c, carry_i;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ counts, ui
         for (int k = 0; k < kScanK; ++k) {
             c[k] = (k0 + k < nkeys) ? counts[k0 + k] : 0u;
             tc += c[k];
-            ti += (c[k] + kWorkP - 1) / kWorkP;
+            ti += (c[k] + wp - 1) / wp;
         }
         // inclusive warp scan of (tc, ti)
         uint32_t ic = tc, ii = ti;
@@ -139,8 +139,8 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ counts, ui
             if (key >= nkeys) break;
             cursor[key] = oc;
             counts[key] = 0u;
-            for (uint32_t j = 0; j < c[k]; j += kWorkP) {
-                const uint32_t cnt = (c[k] - j) < (uint32_t)kWorkP ? (c[k] - j) : (uint32_t)kWorkP;
+            for (uint32_t j = 0; j < c[k]; j += wp) {
+                const uint32_t cnt = (c[k] - j) < wp ? (c[k] - j) : wp;
                 if (oi < work_cap) work[oi] = make_int4(key, (int)(oc + j), (int)cnt, 0);
                 ++oi;
             }
@@ -209,11 +209,28 @@ __device__ __forceinline__ bool make_stencil(const DevParams<T>& P, const T x[3]
 // so P F^T = 2 mu (F - R) F^T + lambda (J - 1) J I.  With F = U S V^T and the
 // reference's proper rotation R = U D V^T (D = I, or diag(.., -1) on the
 // smallest singular value when det F < 0), (F - R) F^T = U (S - D) S U^T.
+// F stays within a few 1e-3 of a rotation, so s - 1 and J - 1 are formed
+// without cancellation from G = F - I (exact in floating point):
+// s_i^2 - 1 = v_i^T (G + G^T + G^T G) v_i and
+// J - 1 = tr G + (sum of the principal 2x2 minors of G) + det G.
 template <typename T>
 __device__ __forceinline__ void stress_PFt(const DevParams<T>& P, const T F[9], T Jp, T out[9]) {
     T U[9], s[3], V[9];
     svd3(F, U, s, V);
-    const T J = det3(F);
+    T G[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) G[e] = F[e];
+    G[0] -= T(1); G[4] -= T(1); G[8] -= T(1);
+    T S[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            S[3 * r + c] = (G[3 * r + c] + G[3 * c + r]) + (G[r] * G[c] + G[3 + r] * G[3 + c] + G[6 + r] * G[6 + c]);
+    const T jm1 = (G[0] + G[4] + G[8]) +
+                  ((G[0] * G[4] - G[1] * G[3]) + (G[0] * G[8] - G[2] * G[6]) + (G[4] * G[8] - G[5] * G[7])) +
+                  det3(G);
+    const T J = T(1) + jm1;
     const T hard = exp_(P.xi * (T(1) - Jp));
     const T mu = P.mu0 * hard, lam = P.lambda0 * hard;
     int kmin = 0;
@@ -222,10 +239,13 @@ __device__ __forceinline__ void stress_PFt(const DevParams<T>& P, const T F[9], 
     T dg[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const T dd = (J < T(0) && c == kmin) ? T(-1) : T(1);
-        dg[c] = T(2) * mu * (s[c] - dd) * s[c];
+        const T v0 = V[c], v1 = V[3 + c], v2 = V[6 + c];
+        const T e = v0 * (S[0] * v0 + S[1] * v1 + S[2] * v2) + v1 * (S[3] * v0 + S[4] * v1 + S[5] * v2) +
+                    v2 * (S[6] * v0 + S[7] * v1 + S[8] * v2);
+        const T sm = (J < T(0) && c == kmin) ? (s[c] + T(1)) : e / (s[c] + T(1));  // s - d
+        dg[c] = T(2) * mu * sm * s[c];
     }
-    const T iso = lam * (J - T(1)) * J;
+    const T iso = lam * jm1 * J;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -302,33 +322,125 @@ __device__ __forceinline__ bool cell_of_tile(const DevParams<T>& P, const int or
 // ---------------------------------------------------------------- P2G
 // rasterizeParticlesToGrid + computeExplicitGridForces
 // (material_point_method.cpp:94-129,235-254) for one work item per loop trip.
-// Each particle contributes w (m v + A (x_i - x_p)) with
-// A = m B D^-1 - fscale V D^-1 P F^T, and w m, to the 64 nodes of its stencil
-// in a shared-memory tile (four planes: m, qx, qy, qz); the tile is then added
-// to the grid with one 16-byte vector reduction per touched cell.
+// Particle p adds w_ip m_p to the mass and w_ip (m v + A (x_i - x_p)) to the
+// momentum of the 64 nodes i of its stencil, with
+// A = m B D^-1 - fscale V D^-1 P F^T:
 //   MOM && FORCE : fused step, q = m v + dt f       (fscale = dt)
 //   MOM only     : rasterize stage, q = m v
 //   FORCE only   : force stage, q = f                (fscale = 1, into gforce)
+//
+// Cell-owned accumulation.  Phase 1 (a thread per particle) turns each
+// particle into a shared-memory record: its 12 separable weights,
+// q' = m v + A e with e = (base - 1) h - x, h A, and m, so that node
+// base - 1 + o receives w_o (m, q' + h A o).  The records are counting-sorted
+// by base cell.  Phase 2 runs one task per (cell, x offset): a thread sums the
+// contributions of every particle of that cell to the 16 nodes of that x
+// layer in registers and adds them to the shared tile once, so the shared
+// atomics per cell are 64 rather than 256 per particle.  The tile then goes to
+// the grid with one 16-byte vector reduction per touched node.
+template <typename T> struct WorkP;
+template <> struct WorkP<float> { static constexpr int value = 512; };
+template <> struct WorkP<double> { static constexpr int value = 128; };
+
+constexpr int kRecV4 = 7;
+constexpr int kCells = kBlk * kBlk * kBlk;
+
+template <typename T> struct P2GShared {
+    T tile[4 * kTileCells];
+    vec4<T> rec[WorkP<T>::value * kRecV4];
+    int cnt[kCells];
+    int off[kCells];
+    uint16_t order[WorkP<T>::value];
+    uint8_t cellof[WorkP<T>::value];
+};
+
+template <typename T> __device__ __forceinline__ T pick4(const vec4<T>& v, int i) {
+    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// Phase 2 for one (cell, x offset) task; adds 16 nodes x (m, q) to the tile.
+template <typename T, bool MOM>
+__device__ __forceinline__ void p2g_cell_task(P2GShared<T>& S, int c, int ox) {
+    const int n_c = S.cnt[c];
+    if (n_c == 0) return;
+    const int cz = c % kBlk, cy = (c / kBlk) % kBlk, cx = c / (kBlk * kBlk);
+    T am[4][4], aq[4][4][3];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            am[a][b] = T(0);
+            aq[a][b][0] = aq[a][b][1] = aq[a][b][2] = T(0);
+        }
+    const T fox = (T)ox;
+    const int k0 = S.off[c];
+    for (int k = k0; k < k0 + n_c; ++k) {
+        const vec4<T>* r = &S.rec[(int)S.order[k] * kRecV4];
+        const vec4<T> wx4 = r[0], wy4 = r[1], wz4 = r[2], qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
+        const T wx = pick4<T>(wx4, ox);
+        const T wy[4] = {wy4.x, wy4.y, wy4.z, wy4.w};
+        const T wz[4] = {wz4.x, wz4.y, wz4.z, wz4.w};
+        // h A columns: x (a4.x, a4.y, a4.z), y (a4.w, b4.x, b4.y), z (b4.z, b4.w, c4.x)
+        T t1[3] = {qm.x + a4.x * fox, qm.y + a4.y * fox, qm.z + a4.z * fox};
+        const T ay[3] = {a4.w, b4.x, b4.y};
+        const T az[3] = {b4.z, b4.w, c4.x};
+#pragma unroll
+        for (int oy = 0; oy < 4; ++oy) {
+            const T wxy = wx * wy[oy];
+            T t3[3] = {t1[0], t1[1], t1[2]};
+#pragma unroll
+            for (int oz = 0; oz < 4; ++oz) {
+                const T w = wxy * wz[oz];
+                if (MOM) am[oy][oz] += w * qm.w;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    aq[oy][oz][q] += w * t3[q];
+                    t3[q] += az[q];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 3; ++q) t1[q] += ay[q];
+        }
+    }
+#pragma unroll
+    for (int oy = 0; oy < 4; ++oy)
+#pragma unroll
+        for (int oz = 0; oz < 4; ++oz) {
+            const int cell = ((cx + ox) * kTile + (cy + oy)) * kTile + (cz + oz);
+            if (MOM) atomicAdd(&S.tile[cell], am[oy][oz]);
+            atomicAdd(&S.tile[kTileCells + cell], aq[oy][oz][0]);
+            atomicAdd(&S.tile[2 * kTileCells + cell], aq[oy][oz][1]);
+            atomicAdd(&S.tile[3 * kTileCells + cell], aq[oy][oz][2]);
+        }
+}
+
 template <typename T, bool MOM, bool FORCE>
 __global__ void __launch_bounds__(kThreads) k_p2g(DevParams<T> P, DevBufs D) {
-    __shared__ T sm[4 * kTileCells];
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    P2GShared<T>& S = *reinterpret_cast<P2GShared<T>*>(smem_raw);
     const vec4<T>* __restrict__ pl = static_cast<const vec4<T>*>(D.pin);
     vec4<T>* __restrict__ grid = static_cast<vec4<T>*>(MOM ? D.grid : D.gforce);
     const uint32_t nw = *D.nwork;
     const size_t n = (size_t)P.n;
     for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
         const int4 it = D.work[wi];
-        for (int c = threadIdx.x; c < 4 * kTileCells; c += blockDim.x) sm[c] = T(0);
+        for (int c = threadIdx.x; c < 4 * kTileCells; c += blockDim.x) S.tile[c] = T(0);
+        for (int c = threadIdx.x; c < kCells; c += blockDim.x) S.cnt[c] = 0;
         int org[3];
         tile_origin(P, it.x, org);
+        const int count = min(it.z, min(WorkP<T>::value, P.n - it.y));
         __syncthreads();
-        const int send = min(it.y + it.z, P.n);
-        for (int s = it.y + threadIdx.x; s < send; s += blockDim.x) {
+        // phase 1: a record per particle
+        for (int j = threadIdx.x; j < count; j += blockDim.x) {
             Particle<T> p;
-            load_particle(pl, n, D.perm[s], p);
-            Stencil<T> S;
-            if (!make_stencil(P, p.x, org, S)) { raise_flag(D.flags, 4u); continue; }
-            if (!stencil_in_grid(P, S.b)) raise_flag(D.flags, 1u);
+            load_particle(pl, n, D.perm[it.y + j], p);
+            Stencil<T> St;
+            if (!make_stencil(P, p.x, org, St)) {
+                raise_flag(D.flags, 4u);
+                S.cellof[j] = 0xff;
+                continue;
+            }
+            if (!stencil_in_grid(P, St.b)) raise_flag(D.flags, 1u);
             T A[9];
             T mv[3] = {T(0), T(0), T(0)};
 #pragma unroll
@@ -346,38 +458,56 @@ __global__ void __launch_bounds__(kThreads) k_p2g(DevParams<T> P, DevBufs D) {
 #pragma unroll
                 for (int e = 0; e < 9; ++e) A[e] -= sc * G[e];
             }
+            T e3[3];
 #pragma unroll
-            for (int ox = 0; ox < 4; ++ox) {
-                T ax[3];
+            for (int a = 0; a < 3; ++a) e3[a] = (T)(St.b[a] - 1) * P.h - p.x[a];
+            T qp[3];
 #pragma unroll
-                for (int r = 0; r < 3; ++r) ax[r] = A[3 * r] * S.d[0][ox];
-#pragma unroll
-                for (int oy = 0; oy < 4; ++oy) {
-                    T axy[3];
-#pragma unroll
-                    for (int r = 0; r < 3; ++r) axy[r] = ax[r] + A[3 * r + 1] * S.d[1][oy];
-                    const T wxy = S.w[0][ox] * S.w[1][oy];
-                    const int rowc = ((S.rel[0] + ox) * kTile + (S.rel[1] + oy)) * kTile + S.rel[2];
-#pragma unroll
-                    for (int oz = 0; oz < 4; ++oz) {
-                        const T w = wxy * S.w[2][oz];
-                        const int cell = rowc + oz;
-                        T q[3];
-#pragma unroll
-                        for (int r = 0; r < 3; ++r) q[r] = mv[r] + (axy[r] + A[3 * r + 2] * S.d[2][oz]);
-                        if (MOM) atomicAdd(&sm[cell], w * p.m);
-                        atomicAdd(&sm[kTileCells + cell], w * q[0]);
-                        atomicAdd(&sm[2 * kTileCells + cell], w * q[1]);
-                        atomicAdd(&sm[3 * kTileCells + cell], w * q[2]);
-                    }
-                }
-            }
+            for (int r = 0; r < 3; ++r) qp[r] = mv[r] + (A[3 * r] * e3[0] + A[3 * r + 1] * e3[1] + A[3 * r + 2] * e3[2]);
+            vec4<T>* r = &S.rec[j * kRecV4];
+            r[0] = mk4<T>(St.w[0][0], St.w[0][1], St.w[0][2], St.w[0][3]);
+            r[1] = mk4<T>(St.w[1][0], St.w[1][1], St.w[1][2], St.w[1][3]);
+            r[2] = mk4<T>(St.w[2][0], St.w[2][1], St.w[2][2], St.w[2][3]);
+            r[3] = mk4<T>(qp[0], qp[1], qp[2], MOM ? p.m : T(0));
+            r[4] = mk4<T>(P.h * A[0], P.h * A[3], P.h * A[6], P.h * A[1]);
+            r[5] = mk4<T>(P.h * A[4], P.h * A[7], P.h * A[2], P.h * A[5]);
+            r[6] = mk4<T>(P.h * A[8], T(0), T(0), T(0));
+            const int cell = (St.rel[0] * kBlk + St.rel[1]) * kBlk + St.rel[2];
+            S.cellof[j] = (uint8_t)cell;
+            atomicAdd(&S.cnt[cell], 1);
         }
+        __syncthreads();
+        if (threadIdx.x < 32) {  // exclusive scan of the 64 cell counts
+            const int l = threadIdx.x;
+            const int a = S.cnt[2 * l], b = S.cnt[2 * l + 1];
+            int x = a + b;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (l >= o) x += y;
+            }
+            S.off[2 * l] = x - a - b;
+            S.off[2 * l + 1] = x - b;
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < kCells; c += blockDim.x) S.cnt[c] = S.off[c];  // cursor
+        __syncthreads();
+        for (int j = threadIdx.x; j < count; j += blockDim.x) {
+            const int c = S.cellof[j];
+            if (c != 0xff) S.order[atomicAdd(&S.cnt[c], 1)] = (uint16_t)j;
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < kCells; c += blockDim.x) S.cnt[c] -= S.off[c];  // counts again
+        __syncthreads();
+        // phase 2: (cell, x offset) tasks
+        for (int task = threadIdx.x; task < kCells * 4; task += blockDim.x)
+            p2g_cell_task<T, MOM>(S, task % kCells, task / kCells);
         __syncthreads();
         for (int c = threadIdx.x; c < kTileCells; c += blockDim.x) {
             size_t lin;
             if (!cell_of_tile(P, org, c, lin)) continue;
-            const vec4<T> v = mk4<T>(sm[c], sm[kTileCells + c], sm[2 * kTileCells + c], sm[3 * kTileCells + c]);
+            const vec4<T> v = mk4<T>(S.tile[c], S.tile[kTileCells + c], S.tile[2 * kTileCells + c],
+                                     S.tile[3 * kTileCells + c]);
             if (v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0)) red_add4(grid + lin, v);
         }
         __syncthreads();

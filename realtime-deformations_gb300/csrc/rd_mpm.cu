@@ -280,7 +280,7 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     }
     long t = tmark_begin(h, RD_KERNEL_SCAN);
     k_scan<<<1, 1024, 0, h->stream>>>(h->counts, h->cursor, h->work, h->nwork, h->nkeys, (uint32_t)h->n,
-                                      (uint32_t)h->work_cap, h->flags);
+                                      (uint32_t)h->work_cap, (uint32_t)WorkP<T>::value, h->flags);
     tmark_end(h, t);
     RD_TRY(launched(h, "k_scan"));
     t = tmark_begin(h, RD_KERNEL_SCATTER);
@@ -293,7 +293,7 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
 }
 
 template <typename T> unsigned persistent_grid(const rd_handle* h, int occ) {
-    const size_t max_items = (size_t)h->n / kWorkP + (size_t)std::min<int64_t>(h->nkeys, h->n) + 1;
+    const size_t max_items = (size_t)h->n / WorkP<T>::value + (size_t)std::min<int64_t>(h->nkeys, h->n) + 1;
     return (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)h->sms * occ));
 }
 
@@ -306,7 +306,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
         DevParams<T> P = make_params<T>(h, dt, (T)dt);
         DevBufs D = bufs<T>(h);
         t = tmark_begin(h, RD_KERNEL_P2G);
-        k_p2g<T, true, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, 0, h->stream>>>(P, D);
+        k_p2g<T, true, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
         tmark_end(h, t);
         RD_TRY(launched(h, "k_p2g"));
         t = tmark_begin(h, RD_KERNEL_G2P);
@@ -336,7 +336,7 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
             RD_TRY(check_cuda(h, cudaMemsetAsync(h->gforce, 0, nc * sizeof(vec4<T>), h->stream), "memset force"));
             if (h->n > 0) {
                 DevBufs D = bufs<T>(h);
-                k_p2g<T, true, false><<<persistent_grid<T>(h, h->occ_p2g), kThreads, 0, h->stream>>>(P, D);
+                k_p2g<T, true, false><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
                 RD_TRY(launched(h, "k_p2g<rasterize>"));
             }
             k_grid_normalize<T><<<cb, 256, 0, h->stream>>>(static_cast<vec4<T>*>(h->grid), nc);
@@ -349,7 +349,7 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
             if (!h->sorted) RD_TRY(sort_particles<T>(h));
             if (h->n > 0) {
                 DevBufs D = bufs<T>(h);
-                k_p2g<T, false, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, 0, h->stream>>>(P, D);
+                k_p2g<T, false, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
                 RD_TRY(launched(h, "k_p2g<forces>"));
             }
             return RD_OK;
@@ -525,7 +525,11 @@ template <typename T> rd_status init_volumes_impl(rd_handle* h) {
 
 template <typename T> rd_status occupancy(rd_handle* h) {
     int o = 0;
-    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true>, kThreads, 0), "occ"));
+    const int sm = (int)sizeof(P2GShared<T>);
+    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_p2g<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
+    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_p2g<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
+    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_p2g<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
+    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true>, kThreads, sm), "occ"));
     h->occ_p2g = std::max(1, o);
     if (h->prm.track_fp)
         RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_g2p_fused<T, true>, kThreads, 0), "occ"));
@@ -597,7 +601,8 @@ rd_status rd_create(const rd_params* params, rd_handle** out) {
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RD_CUDA_ERROR);
     const size_t n = std::max<size_t>(1, (size_t)h->n);
     const size_t v4 = 4 * h->esize;
-    h->work_cap = n / kWorkP + std::min<size_t>((size_t)h->nkeys, n) + 2;
+    const size_t wp = p.precision == RD_FP64 ? WorkP<double>::value : WorkP<float>::value;
+    h->work_cap = n / wp + std::min<size_t>((size_t)h->nkeys, n) + 2;
     struct { void** ptr; size_t bytes; } allocs[] = {
         {&h->pl[0], (size_t)h->planes * n * v4},
         {&h->pl[1], (size_t)h->planes * n * v4},

@@ -47,8 +47,7 @@ def compare_particles(got, o, h, tol, fields=("x", "v", "B", "FE", "Jp")):
         if k == "B":
             errs[k] = rel_floor(got["B"], o.B, b_scale(o.v, h))
         elif k == "Jp":
-            errs[k] = rel(got["Jp"] - 1.0, o.Jp - 1.0) if np.abs(o.Jp - 1.0).max() > 1e-6 else \
-                float(np.abs(got["Jp"] - o.Jp).max())
+            errs[k] = rel(got["Jp"], o.Jp)
         else:
             errs[k] = rel(got[k], getattr(o, k))
     bad = {k: v for k, v in errs.items() if not v < tol}
