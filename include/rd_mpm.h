@@ -119,7 +119,10 @@ rd_status rd_get_particles(rd_handle* h, rd_particles* out, int where);
 /* rasterizeParticlesToGrid + computeParticleVolumesAndDensities, main.cpp:53-54. */
 rd_status rd_init_volumes(rd_handle* h);
 /* nsteps x (the seven stage calls of main.cpp:192-218 with no colliders), fused:
- * sort, P2G with the MLS force, grid update, G2P with the plastic SVD. */
+ * per step a sort by block and one kernel that runs the grid update, G2P, the
+ * plastic SVD and advection of this step and the P2G (MLS force) of the next.
+ * The next step's grid is built with this dt; a call with a different dt
+ * rebuilds it first. */
 rd_status rd_step(rd_handle* h, double dt, int32_t nsteps);
 /* One reference stage at the reference's granularity (RD_STAGE_*). */
 rd_status rd_stage(rd_handle* h, int32_t stage, double dt);
@@ -142,11 +145,12 @@ rd_status rd_synchronize(rd_handle* h);
 rd_status rd_get_stream(rd_handle* h, void** stream);
 /* Copies the last error message (NUL-terminated, truncated to len). */
 rd_status rd_last_error(rd_handle* h, char* buf, size_t len);
-/* Sort diagnostic: sorts the current particles by 4x4x4-cell block (as every
- * step does) and returns each particle's block key in original order (n) and
- * the original index of the particle at each sorted position (n).  The key of
- * a particle is the block of ivec3(pos / h) (material_point_method.cpp:83),
- * linearised x-major like the grid.  Host or device arrays per `where`. */
+/* Sort diagnostic: sorts the current particles by cell (as every step does)
+ * and returns each particle's sort key in original order (n) and the original
+ * index of the particle at each sorted position (n).  The key of a particle
+ * with base cell b = ivec3(pos / h) (material_point_method.cpp:83) is
+ * block * 64 + cell: block = b / 4 per axis linearised x-major like the grid,
+ * cell = (b % 4) linearised the same way.  Host or device arrays per `where`. */
 rd_status rd_debug_sort(rd_handle* h, uint32_t* keys, uint32_t* order, int where);
 /* Kernel ids for the per-kernel event timing below. */
 enum {
@@ -154,8 +158,10 @@ enum {
     RD_KERNEL_SCAN = 1,     /* scan of the block counts, work items */
     RD_KERNEL_SCATTER = 2,  /* sorted permutation */
     RD_KERNEL_GRID_CLEAR = 3,
-    RD_KERNEL_P2G = 4,      /* P2G with the MLS force */
-    RD_KERNEL_G2P = 5,      /* grid update + F update + G2P + advection */
+    RD_KERNEL_P2G = 4,      /* P2G with the MLS force from the stored state (first step,
+                               or after the step size changed) */
+    RD_KERNEL_G2P2G = 5,    /* grid update + G2P + F update + advection of this step and
+                               the P2G (with the MLS force) of the next, fused */
     RD_KERNEL_COUNT = 6
 };
 /* Per-kernel timing with CUDA events recorded on the handle's stream around

@@ -46,7 +46,7 @@ EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "
            "rd_init_volumes", "rd_step", "rd_stage", "rd_get_grid", "rd_device_xyzs", "rd_get_flags",
            "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort",
            "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count")
-KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p")
+KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g")
 
 
 def _sources():

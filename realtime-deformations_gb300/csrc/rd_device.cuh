@@ -222,6 +222,102 @@ __device__ __forceinline__ void svd3(const T F[9], T U[9], T s[3], T V[9]) {
     }
 }
 
+// rsqrt with one Newton step: within about an ulp of 1/sqrt(x), so the
+// Jacobi rotations below stay orthogonal to working precision.
+__device__ __forceinline__ float rsqrt_acc(float x) {
+    const float r = rsqrtf(x);
+    return r * fmaf(-0.5f * x * r, r, 1.5f);
+}
+__device__ __forceinline__ double rsqrt_acc(double x) { return 1.0 / sqrt(x); }
+__device__ __forceinline__ float div_fast(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double div_fast(double a, double b) { return a / b; }
+
+// SVD of an F that is close to a rotation (the elastic F_E of the snow model
+// stays within the plasticity clamp): F = U diag(s) V^T together with s - 1
+// formed without cancellation.  With G = F - I (exact), the symmetric
+// S = F^T F - I = G + G^T + G^T G is small and exactly representable to its own
+// relative precision; its cyclic Jacobi eigen-decomposition (Golub & Van Loan,
+// Matrix Computations, 8.5; rotations in the form of Rutishauser) gives
+// V and e_i = s_i^2 - 1, so s_i = sqrt(1 + e_i) and s_i - 1 = e_i / (1 + s_i);
+// u_i = F v_i / s_i.  The rotation angle only needs to be approximately right
+// (an inexact angle leaves some off-diagonal for the next sweep); the cosine
+// is formed accurately from the same tangent, so every rotation is orthogonal.
+// When F is far from a rotation (|s_i^2 - 1| > 1/4) the one-sided Jacobi
+// svd3 above is used, which keeps small singular values accurate.
+template <typename T>
+__device__ __forceinline__ void svd3_near(const T F[9], T U[9], T s[3], T sm1[3], T V[9]) {
+    T G[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) G[e] = F[e];
+    G[0] -= T(1); G[4] -= T(1); G[8] -= T(1);
+    T A[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = r; c < 3; ++c) {
+            A[r][c] = (G[3 * r + c] + G[3 * c + r]) + (G[r] * G[c] + G[3 + r] * G[3 + c] + G[6 + r] * G[6 + c]);
+            A[c][r] = A[r][c];
+        }
+    const T dmax = fmax(abs_(A[0][0]), fmax(abs_(A[1][1]), abs_(A[2][2])));
+    if (!(dmax <= T(0.25))) {  // far from a rotation (or non-finite): one-sided Jacobi on F
+        svd3(F, U, s, V);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sm1[c] = s[c] - T(1);
+        return;
+    }
+    T v[3][3];  // v[row][col]
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[r][c] = (r == c) ? T(1) : T(0);
+    const T fro = sqrt_(A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2] +
+                        T(2) * (A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2]));
+    const T tol = SvdTol<T>::eps * fro;
+    for (int sweep = 0; sweep < SvdTol<T>::sweeps; ++sweep) {
+        bool rotated = false;
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0;
+            const int q = pq == 0 ? 1 : 2;
+            const int r = 3 - p - q;
+            const T apq = A[p][q];
+            if (abs_(apq) > tol) {
+                rotated = true;
+                const T theta = div_fast(A[q][q] - A[p][p], T(2) * apq);
+                const T t = div_fast(copysign(T(1), theta), abs_(theta) + sqrt_(fma(theta, theta, T(1))));
+                const T c = rsqrt_acc(fma(t, t, T(1)));
+                const T sn = t * c;
+                const T tau = div_fast(sn, T(1) + c);
+                A[p][p] -= t * apq;
+                A[q][q] += t * apq;
+                A[p][q] = A[q][p] = T(0);
+                const T arp = A[r][p], arq = A[r][q];
+                A[r][p] = A[p][r] = arp - sn * (arq + tau * arp);
+                A[r][q] = A[q][r] = arq + sn * (arp - tau * arq);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const T vkp = v[k][p], vkq = v[k][q];
+                    v[k][p] = vkp - sn * (vkq + tau * vkp);
+                    v[k][q] = vkq + sn * (vkp - tau * vkq);
+                }
+            }
+        }
+        if (!rotated) break;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const T e = A[c][c];
+        s[c] = sqrt_(T(1) + e);
+        sm1[c] = e / (T(1) + s[c]);
+        const T inv = T(1) / s[c];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            V[3 * r + c] = v[r][c];
+            U[3 * r + c] = (F[3 * r] * v[0][c] + F[3 * r + 1] * v[1][c] + F[3 * r + 2] * v[2][c]) * inv;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- misc
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;

@@ -1,6 +1,6 @@
 // sm_103a kernels of the MPM step.  One step of rd_step is
 //   k_keys (only when positions changed outside a step) -> k_scan -> k_scatter
-//   -> memset(grid) -> k_p2g<fused> -> k_g2p_fused
+//   -> memset(next grid) -> k_g2p2g (k_p2g first when the grid must be rebuilt)
 // and the stage kernels serve rd_stage, which runs the reference's seven
 // stages one by one (material_point_method.cpp:94-350).
 #pragma once
@@ -20,7 +20,7 @@ constexpr int kThreads = 128;
 template <typename T> struct DevParams {
     int M[3];      // grid nodes per axis
     int NB[3];     // blocks per axis
-    int nkeys;
+    int nkeys;     // blocks x 64 cells
     int n;         // particles
     T h, dinv, dt;
     T mu0, lambda0, xi;
@@ -40,7 +40,9 @@ struct DevBufs {
     uint32_t* counts;
     const int4* work;
     const uint32_t* nwork;
+    uint32_t work_cap;
     void* grid;        // vec4 per cell
+    void* grid_next;   // vec4 per cell: P2G of the next step (fused kernel)
     void* gforce;      // vec4 per cell (stage mode forces)
     uint32_t* flags;
 };
@@ -49,17 +51,22 @@ __device__ __forceinline__ void raise_flag(uint32_t* flags, uint32_t f) {
     if ((__ldcg(flags) & f) == 0) atomicOr(flags, f);
 }
 
-// Block key of base cell b (clamped into the grid; the caller flags
-// out-of-range particles).
+// Sort key of base cell b: the cell's 4x4x4 block (linearised x-major like
+// the grid) times 64 plus the cell's index within the block, so a block's
+// particles are contiguous and, inside the block, grouped by cell.  b is
+// clamped into the grid first; the caller flags out-of-range particles.
+constexpr int kCellsPerBlock = kBlk * kBlk * kBlk;
 template <typename T>
-__device__ __forceinline__ uint32_t block_key(const DevParams<T>& P, const int b[3]) {
-    int k[3];
+__device__ __forceinline__ uint32_t sort_key(const DevParams<T>& P, const int b[3]) {
+    int k[3], c[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        int c = b[a] < 0 ? 0 : (b[a] > P.M[a] - 1 ? P.M[a] - 1 : b[a]);
-        k[a] = c / kBlk;
+        const int v = b[a] < 0 ? 0 : (b[a] > P.M[a] - 1 ? P.M[a] - 1 : b[a]);
+        k[a] = v / kBlk;
+        c[a] = v - k[a] * kBlk;
     }
-    return ((uint32_t)k[0] * P.NB[1] + k[1]) * P.NB[2] + k[2];
+    const uint32_t blk = ((uint32_t)k[0] * P.NB[1] + k[1]) * P.NB[2] + k[2];
+    return blk * kCellsPerBlock + (uint32_t)((c[0] * kBlk + c[1]) * kBlk + c[2]);
 }
 
 template <typename T>
@@ -84,81 +91,129 @@ __global__ void __launch_bounds__(256) k_keys(DevParams<T> P, const vec4<T>* __r
     const vec4<T> x = ld_stream(pl + i);
     const int b[3] = {base_of(x.x, P.h), base_of(x.y, P.h), base_of(x.z, P.h)};
     if (!stencil_in_grid(P, b)) raise_flag(flags, 1u);
-    const uint32_t key = block_key(P, b);
+    const uint32_t key = sort_key(P, b);
     keys[i] = key;
     count_key(counts, key);
 }
 
-// Exclusive scan of the per-block counts into starts (and the scatter cursor),
-// emission of the work items, reset of the counts for the next histogram.  One
-// CTA of 1024 threads sweeps the key range in chunks of 1024 x kScanK keys.
-constexpr int kScanK = 16;
-__global__ void __launch_bounds__(1024) k_scan(uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
-                                               int4* __restrict__ work, uint32_t* __restrict__ nwork, int nkeys,
-                                               uint32_t n_expected, uint32_t work_cap, uint32_t wp,
-                                               uint32_t* flags) {
-    __shared__ uint32_t s_c[32], s_i[32];
-    __shared__ uint32_t carry_c, carry_i;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) { carry_c = 0; carry_i = 0; }
-    __syncthreads();
-    for (int chunk = 0; chunk < nkeys; chunk += 1024 * kScanK) {
-        const int k0 = chunk + tid * kScanK;
-        uint32_t c[kScanK];
-        uint32_t tc = 0, ti = 0;
+// Exclusive scan of the per-cell counts into the scatter cursor (the first
+// sorted slot of each cell), emission of the work items and reset of the
+// counts for the next histogram, over kScanTile-key tiles on all SMs:
+// k_tile_sums adds up each tile, k_scan scans one tile (16 whole blocks) per
+// CTA after summing the tiles before it.  A block of c particles becomes
+// ceil(c / wp) work items of nearly equal size; the items are appended to the
+// list through an atomic counter (their order does not matter) and the
+// counter of the next sort is cleared here.
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 4;                                 // consecutive keys per thread
+constexpr int kScanTile = kScanThreads * kScanPer;          // keys per CTA
+constexpr int kBlocksPerTile = kScanTile / kCellsPerBlock;  // 64
+constexpr int kThreadsPerBlockKeys = kCellsPerBlock / kScanPer;  // 16
+
+__device__ __forceinline__ uint4 ld4_or_zero(const uint32_t* p, int k0, int nkeys) {
+    if (k0 + kScanPer <= nkeys) return *reinterpret_cast<const uint4*>(p + k0);
+    uint4 r = make_uint4(0u, 0u, 0u, 0u);
+    if (k0 < nkeys) r.x = p[k0];
+    if (k0 + 1 < nkeys) r.y = p[k0 + 1];
+    if (k0 + 2 < nkeys) r.z = p[k0 + 2];
+    return r;
+}
+__device__ __forceinline__ void st4(uint32_t* p, int k0, int nkeys, uint4 v) {
+    if (k0 + kScanPer <= nkeys) { *reinterpret_cast<uint4*>(p + k0) = v; return; }
+    if (k0 < nkeys) p[k0] = v.x;
+    if (k0 + 1 < nkeys) p[k0 + 1] = v.y;
+    if (k0 + 2 < nkeys) p[k0 + 2] = v.z;
+}
+
+__global__ void __launch_bounds__(256) k_tile_sums(const uint32_t* __restrict__ counts, int nkeys,
+                                                   uint32_t* __restrict__ tile_sums) {
+    __shared__ uint32_t part[8];
+    const int t = blockIdx.x, tid = threadIdx.x;
+    uint32_t sum = 0;
+    for (int k = t * kScanTile + tid * kScanPer; k < min(nkeys, (t + 1) * kScanTile); k += blockDim.x * kScanPer) {
+        const uint4 v = ld4_or_zero(counts, k, nkeys);
+        sum += v.x + v.y + v.z + v.w;
+    }
 #pragma unroll
-        for (int k = 0; k < kScanK; ++k) {
-            c[k] = (k0 + k < nkeys) ? counts[k0 + k] : 0u;
-            tc += c[k];
-            ti += (c[k] + wp - 1) / wp;
-        }
-        // inclusive warp scan of (tc, ti)
-        uint32_t ic = tc, ii = ti;
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((tid & 31) == 0) part[tid >> 5] = sum;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t tot = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += part[w];
+        tile_sums[t] = tot;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
+                                                       const uint32_t* __restrict__ tile_sums, int nkeys,
+                                                       int4* __restrict__ work, uint32_t* __restrict__ nwork,
+                                                       uint32_t* __restrict__ nwork_next_sort, uint32_t n_expected,
+                                                       uint32_t work_cap, uint32_t wp, uint32_t* flags) {
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_blk[kBlocksPerTile];  // particles per block of this tile
+    __shared__ uint32_t s_off;
+    const int t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    // offset of this tile: sum of the tiles before it
+    uint32_t pre = 0;
+    for (int i = tid; i < t; i += blockDim.x) pre += tile_sums[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(0xffffffffu, pre, o);
+    if (lane == 0) s_w[wid] = pre;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t tot = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) tot += s_w[w];
+        s_off = tot;
+        if (t == 0) *nwork_next_sort = 0u;
+        if (t == (int)gridDim.x - 1 && tot + tile_sums[t] != n_expected) atomicOr(flags, 4u);
+    }
+    __syncthreads();
+    const int k0 = t * kScanTile + tid * kScanPer;
+    const uint4 c = ld4_or_zero(counts, k0, nkeys);
+    const uint32_t tc = c.x + c.y + c.z + c.w;
+    // particles of this thread's block: the 16 threads of a block are 16 aligned lanes
+    uint32_t bsum = tc;
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
+    if ((tid & (kThreadsPerBlockKeys - 1)) == 0) s_blk[tid / kThreadsPerBlockKeys] = bsum;
+    uint32_t ic = tc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, ic, o);
+        if (lane >= o) ic += y;
+    }
+    __syncthreads();
+    if (lane == 31) s_w[wid] = ic;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t wc = s_w[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t yc = __shfl_up_sync(0xffffffffu, ic, o), yi = __shfl_up_sync(0xffffffffu, ii, o);
-            if (lane >= o) { ic += yc; ii += yi; }
+            const uint32_t y = __shfl_up_sync(0xffffffffu, wc, o);
+            if (lane >= o) wc += y;
         }
-        if (lane == 31) { s_c[wid] = ic; s_i[wid] = ii; }
-        __syncthreads();
-        if (wid == 0) {
-            uint32_t wc = s_c[lane], wi = s_i[lane];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t yc = __shfl_up_sync(0xffffffffu, wc, o), yi = __shfl_up_sync(0xffffffffu, wi, o);
-                if (lane >= o) { wc += yc; wi += yi; }
-            }
-            s_c[lane] = wc; s_i[lane] = wi;
-        }
-        __syncthreads();
-        uint32_t oc = carry_c + (wid ? s_c[wid - 1] : 0u) + ic - tc;
-        uint32_t oi = carry_i + (wid ? s_i[wid - 1] : 0u) + ii - ti;
-#pragma unroll
-        for (int k = 0; k < kScanK; ++k) {
-            const int key = k0 + k;
-            if (key >= nkeys) break;
-            cursor[key] = oc;
-            counts[key] = 0u;
-            for (uint32_t j = 0; j < c[k]; j += wp) {
-                const uint32_t cnt = (c[k] - j) < wp ? (c[k] - j) : wp;
-                if (oi < work_cap) work[oi] = make_int4(key, (int)(oc + j), (int)cnt, 0);
-                ++oi;
-            }
-            oc += c[k];
-        }
-        __syncthreads();
-        if (tid == 1023) {
-            carry_c += s_c[31];
-            carry_i += s_i[31];
-        }
-        __syncthreads();
+        s_w[lane] = wc;  // inclusive prefix over warps
     }
-    if (tid == 0) {
-        // A histogram that does not add up to n would index past the buffers:
-        // run no work items and report it instead.
-        const bool bad = carry_c != n_expected || carry_i > work_cap;
-        *nwork = bad ? 0u : carry_i;
-        if (bad) atomicOr(flags, 4u);
+    __syncthreads();
+    const uint32_t st0 = s_off + (wid ? s_w[wid - 1] : 0u) + ic - tc;
+    st4(cursor, k0, nkeys, make_uint4(st0, st0 + c.x, st0 + c.x + c.y, st0 + c.x + c.y + c.z));
+    st4(counts, k0, nkeys, make_uint4(0u, 0u, 0u, 0u));
+    // the first thread of each block emits the block's work items
+    if ((tid & (kThreadsPerBlockKeys - 1)) == 0) {
+        const int b = tid / kThreadsPerBlockKeys;
+        const uint32_t bc = s_blk[b];
+        const uint32_t ni = (bc + wp - 1) / wp;
+        if (ni) {
+            uint32_t oi = atomicAdd(nwork, ni);
+            uint32_t st = st0;
+            for (uint32_t j = 0; j < ni; ++j, ++oi) {
+                const uint32_t cnt = bc / ni + (j < bc % ni ? 1u : 0u);
+                if (oi < work_cap) work[oi] = make_int4(t * kBlocksPerTile + b, (int)st, (int)cnt, 0);
+                else atomicOr(flags, 4u);
+                st += cnt;
+            }
+        }
     }
 }
 
@@ -188,8 +243,11 @@ template <typename T> struct Stencil {
     T d[3][4];     // x_i - x_p per axis, (base + o) h - x as the reference computes it
 };
 
+// Weights and offsets of the stencil of x; rel = base - 1 - org must lie in
+// [0, rmax] for the stencil to fit the tile with origin org.
 template <typename T>
-__device__ __forceinline__ bool make_stencil(const DevParams<T>& P, const T x[3], const int org[3], Stencil<T>& S) {
+__device__ __forceinline__ bool make_stencil(const DevParams<T>& P, const T x[3], const int org[3], Stencil<T>& S,
+                                             int rmax = kTile - 4) {
     bool ok = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -199,7 +257,7 @@ __device__ __forceinline__ bool make_stencil(const DevParams<T>& P, const T x[3]
 #pragma unroll
         for (int o = 0; o < 4; ++o) S.d[a][o] = (T)(S.b[a] - 1 + o) * P.h - x[a];
         S.rel[a] = S.b[a] - 1 - org[a];
-        ok = ok && S.rel[a] >= 0 && S.rel[a] <= kTile - 4;
+        ok = ok && S.rel[a] >= 0 && S.rel[a] <= rmax;
     }
     return ok;
 }
@@ -209,24 +267,17 @@ __device__ __forceinline__ bool make_stencil(const DevParams<T>& P, const T x[3]
 // so P F^T = 2 mu (F - R) F^T + lambda (J - 1) J I.  With F = U S V^T and the
 // reference's proper rotation R = U D V^T (D = I, or diag(.., -1) on the
 // smallest singular value when det F < 0), (F - R) F^T = U (S - D) S U^T.
-// F stays within a few 1e-3 of a rotation, so s - 1 and J - 1 are formed
-// without cancellation from G = F - I (exact in floating point):
-// s_i^2 - 1 = v_i^T (G + G^T + G^T G) v_i and
+// F stays within a few 1e-3 of a rotation, so s - 1 (svd3_near) and J - 1
+// are formed without cancellation from G = F - I (exact in floating point):
 // J - 1 = tr G + (sum of the principal 2x2 minors of G) + det G.
 template <typename T>
 __device__ __forceinline__ void stress_PFt(const DevParams<T>& P, const T F[9], T Jp, T out[9]) {
-    T U[9], s[3], V[9];
-    svd3(F, U, s, V);
+    T U[9], s[3], sm1[3], V[9];
+    svd3_near(F, U, s, sm1, V);
     T G[9];
 #pragma unroll
     for (int e = 0; e < 9; ++e) G[e] = F[e];
     G[0] -= T(1); G[4] -= T(1); G[8] -= T(1);
-    T S[9];
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-            S[3 * r + c] = (G[3 * r + c] + G[3 * c + r]) + (G[r] * G[c] + G[3 + r] * G[3 + c] + G[6 + r] * G[6 + c]);
     const T jm1 = (G[0] + G[4] + G[8]) +
                   ((G[0] * G[4] - G[1] * G[3]) + (G[0] * G[8] - G[2] * G[6]) + (G[4] * G[8] - G[5] * G[7])) +
                   det3(G);
@@ -239,10 +290,7 @@ __device__ __forceinline__ void stress_PFt(const DevParams<T>& P, const T F[9], 
     T dg[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const T v0 = V[c], v1 = V[3 + c], v2 = V[6 + c];
-        const T e = v0 * (S[0] * v0 + S[1] * v1 + S[2] * v2) + v1 * (S[3] * v0 + S[4] * v1 + S[5] * v2) +
-                    v2 * (S[6] * v0 + S[7] * v1 + S[8] * v2);
-        const T sm = (J < T(0) && c == kmin) ? (s[c] + T(1)) : e / (s[c] + T(1));  // s - d
+        const T sm = (J < T(0) && c == kmin) ? (s[c] + T(1)) : sm1[c];  // s - d
         dg[c] = T(2) * mu * sm * s[c];
     }
     const T iso = lam * jm1 * J;
@@ -254,34 +302,54 @@ __device__ __forceinline__ void stress_PFt(const DevParams<T>& P, const T F[9], 
                              U[3 * r + 2] * dg[2] * U[3 * c + 2] + (r == c ? iso : T(0));
 }
 
+// The clamped split of F_E* = U S V^T that updateDeformationGradient makes,
+// kept for the stress of the next P2G: sc = clamp(S), sc - 1 without
+// cancellation, and the sign of det F_E*.
+template <typename T> struct Split {
+    T U[9], sc[3], scm1[3], sgn;
+};
+
 // updateDeformationGradient (material_point_method.cpp:306-330) for one
 // particle: F_E* = (I + dt B D^-1) F_E = U S V^T, F_E <- U clamp(S) V^T, and
-// det F_P *= prod S / prod clamp(S) (the reference's F_P <- F_E^-1 Fhat with
-// Fhat = F_E* F_P); with the full F_P, F_P <- V (S / clamp(S)) V^T F_P.
+// det F_P *= prod over clamped i of S_i / clamp(S_i) (the reference's
+// F_P <- F_E^-1 Fhat with Fhat = F_E* F_P); with the full F_P,
+// F_P <- V (S / clamp(S)) V^T F_P.  s_i - 1 for an unclamped value comes
+// from svd3_near without cancellation.
 template <typename T, bool TRACK_FP>
-__device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T F[9], T& Jp, T FP[9]) {
+__device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T F[9], T& Jp, T FP[9],
+                                         Split<T>& sp) {
     T A[9];
 #pragma unroll
     for (int e = 0; e < 9; ++e) A[e] = Bm[e] * P.dinv * P.dt;
     A[0] += T(1); A[4] += T(1); A[8] += T(1);
     T Fs[9];
     matmul3(Fs, A, F);
-    T U[9], s[3], V[9];
-    svd3(Fs, U, s, V);
-    T sc[3];
+    T s[3], sm1[3], V[9];
+    svd3_near(Fs, sp.U, s, sm1, V);
+    T ratio = T(1);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) sc[c] = s[c] < P.lo ? P.lo : (s[c] > P.hi ? P.hi : s[c]);
+    for (int c = 0; c < 3; ++c) {
+        if (s[c] < P.lo) {
+            sp.sc[c] = P.lo; sp.scm1[c] = P.lo - T(1); ratio *= s[c] / P.lo;
+        } else if (s[c] > P.hi) {
+            sp.sc[c] = P.hi; sp.scm1[c] = P.hi - T(1); ratio *= s[c] / P.hi;
+        } else {
+            sp.sc[c] = s[c];
+            sp.scm1[c] = sm1[c];
+        }
+    }
+    sp.sgn = (det3(sp.U) * det3(V) < T(0)) ? T(-1) : T(1);
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
         for (int c = 0; c < 3; ++c)
-            F[3 * r + c] = U[3 * r] * sc[0] * V[3 * c] + U[3 * r + 1] * sc[1] * V[3 * c + 1] +
-                           U[3 * r + 2] * sc[2] * V[3 * c + 2];
-    Jp = Jp * ((s[0] * s[1] * s[2]) / (sc[0] * sc[1] * sc[2]));
+            F[3 * r + c] = sp.U[3 * r] * sp.sc[0] * V[3 * c] + sp.U[3 * r + 1] * sp.sc[1] * V[3 * c + 1] +
+                           sp.U[3 * r + 2] * sp.sc[2] * V[3 * c + 2];
+    Jp = Jp * ratio;
     if (TRACK_FP) {
         T r[3], Mv[9], out[9];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) r[c] = s[c] / sc[c];
+        for (int c = 0; c < 3; ++c) r[c] = s[c] / sp.sc[c];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -292,6 +360,35 @@ __device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T
 #pragma unroll
         for (int e = 0; e < 9; ++e) FP[e] = out[e];
     }
+}
+
+// P F^T of F = U sc V^T (the split just made), as stress_PFt computes it
+// from an SVD of F: U diag(2 mu (sc - d) sc) U^T + lambda (J - 1) J I with
+// J = sgn prod sc and J - 1 expanded in sc - 1 so nothing cancels.
+template <typename T>
+__device__ __forceinline__ void stress_from_split(const DevParams<T>& P, const Split<T>& sp, T Jp, T out[9]) {
+    const T e0 = sp.scm1[0], e1 = sp.scm1[1], e2 = sp.scm1[2];
+    const T pm1 = (e0 + e1 + e2) + (e0 * e1 + e0 * e2 + e1 * e2) + e0 * e1 * e2;  // prod sc - 1
+    const T J = sp.sgn > T(0) ? T(1) + pm1 : -(T(1) + pm1);
+    const T jm1 = sp.sgn > T(0) ? pm1 : J - T(1);
+    const T hard = exp_(P.xi * (T(1) - Jp));
+    const T mu = P.mu0 * hard, lam = P.lambda0 * hard;
+    int kmin = 0;
+#pragma unroll
+    for (int c = 1; c < 3; ++c) kmin = sp.sc[c] < sp.sc[kmin] ? c : kmin;
+    T dg[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const T sm = (J < T(0) && c == kmin) ? (sp.sc[c] + T(1)) : sp.scm1[c];
+        dg[c] = T(2) * mu * sm * sp.sc[c];
+    }
+    const T iso = lam * jm1 * J;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            out[3 * r + c] = sp.U[3 * r] * dg[0] * sp.U[3 * c] + sp.U[3 * r + 1] * dg[1] * sp.U[3 * c + 1] +
+                             sp.U[3 * r + 2] * dg[2] * sp.U[3 * c + 2] + (r == c ? iso : T(0));
 }
 
 template <typename T>
@@ -339,17 +436,21 @@ __device__ __forceinline__ bool cell_of_tile(const DevParams<T>& P, const int or
 // atomics per cell are 64 rather than 256 per particle.  The tile then goes to
 // the grid with one 16-byte vector reduction per touched node.
 template <typename T> struct WorkP;
-template <> struct WorkP<float> { static constexpr int value = 512; };
+template <> struct WorkP<float> { static constexpr int value = 256; };
 template <> struct WorkP<double> { static constexpr int value = 128; };
 
 constexpr int kRecV4 = 7;
-constexpr int kCells = kBlk * kBlk * kBlk;
 
-template <typename T> struct P2GShared {
-    T tile[4 * kTileCells];
+// Shared memory of the P2G phase for a cell space of CA^3 base cells and a
+// (CA + 3)^3-node tile.
+template <typename T, int CA> struct P2GTile {
+    static constexpr int TS = CA + 3;
+    static constexpr int TC = TS * TS * TS;
+    static constexpr int NC = CA * CA * CA;
+    T tile[4 * TC];
     vec4<T> rec[WorkP<T>::value * kRecV4];
-    int cnt[kCells];
-    int off[kCells];
+    int cnt[NC];
+    int off[NC];
     uint16_t order[WorkP<T>::value];
     uint8_t cellof[WorkP<T>::value];
 };
@@ -358,74 +459,178 @@ template <typename T> __device__ __forceinline__ T pick4(const vec4<T>& v, int i
     return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
-// Phase 2 for one (cell, x offset) task; adds 16 nodes x (m, q) to the tile.
+// The record of one particle: node base - 1 + o receives w_o (m, q' + h A o),
+// q' = m v + A e with e = (base - 1) h - x.
 template <typename T, bool MOM>
-__device__ __forceinline__ void p2g_cell_task(P2GShared<T>& S, int c, int ox) {
-    const int n_c = S.cnt[c];
-    if (n_c == 0) return;
-    const int cz = c % kBlk, cy = (c / kBlk) % kBlk, cx = c / (kBlk * kBlk);
-    T am[4][4], aq[4][4][3];
+__device__ __forceinline__ void write_record(vec4<T>* r, const Stencil<T>& St, const T x[3], const T A[9],
+                                             const T mv[3], T m, T h) {
+    T e3[3];
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+    for (int a = 0; a < 3; ++a) e3[a] = (T)(St.b[a] - 1) * h - x[a];
+    T qp[3];
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            am[a][b] = T(0);
-            aq[a][b][0] = aq[a][b][1] = aq[a][b][2] = T(0);
+    for (int r = 0; r < 3; ++r) qp[r] = mv[r] + (A[3 * r] * e3[0] + A[3 * r + 1] * e3[1] + A[3 * r + 2] * e3[2]);
+    r[0] = mk4<T>(St.w[0][0], St.w[0][1], St.w[0][2], St.w[0][3]);
+    r[1] = mk4<T>(St.w[1][0], St.w[1][1], St.w[1][2], St.w[1][3]);
+    r[2] = mk4<T>(St.w[2][0], St.w[2][1], St.w[2][2], St.w[2][3]);
+    r[3] = mk4<T>(qp[0], qp[1], qp[2], MOM ? m : T(0));
+    r[4] = mk4<T>(h * A[0], h * A[3], h * A[6], h * A[1]);
+    r[5] = mk4<T>(h * A[4], h * A[7], h * A[2], h * A[5]);
+    r[6] = mk4<T>(h * A[8], T(0), T(0), T(0));
+}
+
+// Counting sort of the records by cell: S.cnt holds the counts on entry and
+// again on exit, S.off the offsets, S.order the record index per slot.
+// Called by every thread of the block.
+template <typename T, int CA>
+__device__ __forceinline__ void sort_records(P2GTile<T, CA>& S, int count) {
+    constexpr int NC = P2GTile<T, CA>::NC;
+    constexpr int PER = (NC + 31) / 32;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int l = threadIdx.x;
+        int loc[PER];
+        int tot = 0;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int c = l * PER + k;
+            loc[k] = c < NC ? S.cnt[c] : 0;
+            tot += loc[k];
         }
-    const T fox = (T)ox;
-    const int k0 = S.off[c];
-    for (int k = k0; k < k0 + n_c; ++k) {
-        const vec4<T>* r = &S.rec[(int)S.order[k] * kRecV4];
-        const vec4<T> wx4 = r[0], wy4 = r[1], wz4 = r[2], qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
-        const T wx = pick4<T>(wx4, ox);
-        const T wy[4] = {wy4.x, wy4.y, wy4.z, wy4.w};
-        const T wz[4] = {wz4.x, wz4.y, wz4.z, wz4.w};
-        // h A columns: x (a4.x, a4.y, a4.z), y (a4.w, b4.x, b4.y), z (b4.z, b4.w, c4.x)
-        T t1[3] = {qm.x + a4.x * fox, qm.y + a4.y * fox, qm.z + a4.z * fox};
-        const T ay[3] = {a4.w, b4.x, b4.y};
-        const T az[3] = {b4.z, b4.w, c4.x};
+        int x = tot;
 #pragma unroll
-        for (int oy = 0; oy < 4; ++oy) {
-            const T wxy = wx * wy[oy];
-            T t3[3] = {t1[0], t1[1], t1[2]};
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (l >= o) x += y;
+        }
+        int run = x - tot;
 #pragma unroll
-            for (int oz = 0; oz < 4; ++oz) {
-                const T w = wxy * wz[oz];
-                if (MOM) am[oy][oz] += w * qm.w;
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    aq[oy][oz][q] += w * t3[q];
-                    t3[q] += az[q];
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 3; ++q) t1[q] += ay[q];
+        for (int k = 0; k < PER; ++k) {
+            const int c = l * PER + k;
+            if (c < NC) { S.off[c] = run; S.cnt[c] = run; }
+            run += loc[k];
         }
     }
+    __syncthreads();
+    for (int j = threadIdx.x; j < count; j += blockDim.x) {
+        const int c = S.cellof[j];
+        if (c != 0xff) S.order[atomicAdd(&S.cnt[c], 1)] = (uint16_t)j;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < NC; c += blockDim.x) S.cnt[c] -= S.off[c];
+    __syncthreads();
+}
+
+// Phase 2, warp-cooperative: the warps of the block split the cell-sorted
+// records into contiguous runs; within a warp every lane owns two of the 64
+// stencil nodes (ox = l / 8, oy = (l / 2) % 4, oz = l % 2 and l % 2 + 2) and
+// all lanes walk the run together, so each record is read by broadcast and
+// contributes to all 64 nodes at once.  A lane keeps (m, q) of its two nodes
+// in registers while consecutive records share a base cell and adds them to
+// the shared tile when the cell changes.
+template <typename T, int CA>
+__device__ __forceinline__ void p2g_flush_lane(P2GTile<T, CA>& S, int c, int ox, int oy, int oz0, const T am[2],
+                                               const T aq[2][3], bool mom) {
+    constexpr int TS = P2GTile<T, CA>::TS;
+    constexpr int TC = P2GTile<T, CA>::TC;
+    const int cz = c % CA, cy = (c / CA) % CA, cx = c / (CA * CA);
 #pragma unroll
-    for (int oy = 0; oy < 4; ++oy)
-#pragma unroll
-        for (int oz = 0; oz < 4; ++oz) {
-            const int cell = ((cx + ox) * kTile + (cy + oy)) * kTile + (cz + oz);
-            if (MOM) atomicAdd(&S.tile[cell], am[oy][oz]);
-            atomicAdd(&S.tile[kTileCells + cell], aq[oy][oz][0]);
-            atomicAdd(&S.tile[2 * kTileCells + cell], aq[oy][oz][1]);
-            atomicAdd(&S.tile[3 * kTileCells + cell], aq[oy][oz][2]);
+    for (int k = 0; k < 2; ++k) {
+        const int node = ((cx + ox) * TS + (cy + oy)) * TS + (cz + oz0 + 2 * k);
+        if (mom) atomicAdd(&S.tile[node], am[k]);
+        atomicAdd(&S.tile[TC + node], aq[k][0]);
+        atomicAdd(&S.tile[2 * TC + node], aq[k][1]);
+        atomicAdd(&S.tile[3 * TC + node], aq[k][2]);
+    }
+}
+
+template <typename T, bool MOM, int CA>
+__device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int count) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int ox = lane >> 3, oy = (lane >> 1) & 3, oz0 = lane & 1;
+    const T fx = (T)ox, fy = (T)oy, fz = (T)oz0;
+    // sorted slots holding a record: the records of cells 0xff were skipped
+    const int total = S.off[P2GTile<T, CA>::NC - 1] + S.cnt[P2GTile<T, CA>::NC - 1];
+    const int k0 = (int)(((long long)total * warp) / nwarps), k1 = (int)(((long long)total * (warp + 1)) / nwarps);
+    const T* recs = reinterpret_cast<const T*>(S.rec);
+    int cur = -1;
+    T am[2] = {T(0), T(0)}, aq[2][3] = {{T(0), T(0), T(0)}, {T(0), T(0), T(0)}};
+    for (int k = k0; k < k1; ++k) {
+        const int j = S.order[k];
+        const int c = S.cellof[j];
+        if (c != cur) {
+            if (cur >= 0) p2g_flush_lane<T, CA>(S, cur, ox, oy, oz0, am, aq, MOM);
+            cur = c;
+            am[0] = am[1] = T(0);
+            aq[0][0] = aq[0][1] = aq[0][2] = aq[1][0] = aq[1][1] = aq[1][2] = T(0);
         }
+        const T* rs = recs + j * (4 * kRecV4);
+        const T wxy = rs[ox] * rs[4 + oy];
+        const T w0 = wxy * rs[8 + oz0], w1 = wxy * rs[10 + oz0];
+        const vec4<T>* r = &S.rec[j * kRecV4];
+        const vec4<T> qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
+        // q' + h A o; h A columns x (a4.x, a4.y, a4.z), y (a4.w, b4.x, b4.y), z (b4.z, b4.w, c4.x)
+        const T q0x = qm.x + a4.x * fx + a4.w * fy + b4.z * fz;
+        const T q0y = qm.y + a4.y * fx + b4.x * fy + b4.w * fz;
+        const T q0z = qm.z + a4.z * fx + b4.y * fy + c4.x * fz;
+        const T q1x = q0x + T(2) * b4.z, q1y = q0y + T(2) * b4.w, q1z = q0z + T(2) * c4.x;
+        if (MOM) { am[0] += w0 * qm.w; am[1] += w1 * qm.w; }
+        aq[0][0] += w0 * q0x; aq[0][1] += w0 * q0y; aq[0][2] += w0 * q0z;
+        aq[1][0] += w1 * q1x; aq[1][1] += w1 * q1y; aq[1][2] += w1 * q1z;
+    }
+    if (cur >= 0) p2g_flush_lane<T, CA>(S, cur, ox, oy, oz0, am, aq, MOM);
+}
+
+// Adds the tile (origin org) to the grid: one vector reduction per node that
+// received anything.
+template <typename T, int CA>
+__device__ __forceinline__ void p2g_flush(const DevParams<T>& P, const P2GTile<T, CA>& S, const int org[3],
+                                          vec4<T>* __restrict__ grid) {
+    constexpr int TS = P2GTile<T, CA>::TS;
+    constexpr int TC = P2GTile<T, CA>::TC;
+    for (int c = threadIdx.x; c < TC; c += blockDim.x) {
+        const int ix = c / (TS * TS), iy = (c / TS) % TS, iz = c % TS;
+        const int gx = org[0] + ix, gy = org[1] + iy, gz = org[2] + iz;
+        if (gx < 0 || gy < 0 || gz < 0 || gx >= P.M[0] || gy >= P.M[1] || gz >= P.M[2]) continue;
+        const vec4<T> v = mk4<T>(S.tile[c], S.tile[TC + c], S.tile[2 * TC + c], S.tile[3 * TC + c]);
+        if (v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0))
+            red_add4(grid + ((size_t)gx * P.M[1] + gy) * P.M[2] + gz, v);
+    }
+}
+
+// Direct scatter of one record to the grid, for a particle outside its
+// block's cell space (moved more than one cell in a step).
+template <typename T>
+__device__ void p2g_direct(const DevParams<T>& P, const vec4<T>* r, const int b[3], vec4<T>* __restrict__ grid) {
+    const vec4<T> wx4 = r[0], wy4 = r[1], wz4 = r[2], qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
+    const T wx[4] = {wx4.x, wx4.y, wx4.z, wx4.w}, wy[4] = {wy4.x, wy4.y, wy4.z, wy4.w},
+            wz[4] = {wz4.x, wz4.y, wz4.z, wz4.w};
+    for (int ox = 0; ox < 4; ++ox)
+        for (int oy = 0; oy < 4; ++oy)
+            for (int oz = 0; oz < 4; ++oz) {
+                const int gx = b[0] - 1 + ox, gy = b[1] - 1 + oy, gz = b[2] - 1 + oz;
+                if (gx < 0 || gy < 0 || gz < 0 || gx >= P.M[0] || gy >= P.M[1] || gz >= P.M[2]) continue;
+                const T w = (wx[ox] * wy[oy]) * wz[oz];
+                const T fo[3] = {(T)ox, (T)oy, (T)oz};
+                const T q0 = qm.x + a4.x * fo[0] + a4.w * fo[1] + b4.z * fo[2];
+                const T q1 = qm.y + a4.y * fo[0] + b4.x * fo[1] + b4.w * fo[2];
+                const T q2 = qm.z + a4.z * fo[0] + b4.y * fo[1] + c4.x * fo[2];
+                red_add4(grid + ((size_t)gx * P.M[1] + gy) * P.M[2] + gz, mk4<T>(w * qm.w, w * q0, w * q1, w * q2));
+            }
 }
 
 template <typename T, bool MOM, bool FORCE>
 __global__ void __launch_bounds__(kThreads) k_p2g(DevParams<T> P, DevBufs D) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
-    P2GShared<T>& S = *reinterpret_cast<P2GShared<T>*>(smem_raw);
+    P2GTile<T, kBlk>& S = *reinterpret_cast<P2GTile<T, kBlk>*>(smem_raw);
     const vec4<T>* __restrict__ pl = static_cast<const vec4<T>*>(D.pin);
     vec4<T>* __restrict__ grid = static_cast<vec4<T>*>(MOM ? D.grid : D.gforce);
-    const uint32_t nw = *D.nwork;
+    const uint32_t nw = min(*D.nwork, D.work_cap);
     const size_t n = (size_t)P.n;
     for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
         const int4 it = D.work[wi];
-        for (int c = threadIdx.x; c < 4 * kTileCells; c += blockDim.x) S.tile[c] = T(0);
-        for (int c = threadIdx.x; c < kCells; c += blockDim.x) S.cnt[c] = 0;
+        for (int c = threadIdx.x; c < 4 * P2GTile<T, kBlk>::TC; c += blockDim.x) S.tile[c] = T(0);
+        for (int c = threadIdx.x; c < P2GTile<T, kBlk>::NC; c += blockDim.x) S.cnt[c] = 0;
         int org[3];
         tile_origin(P, it.x, org);
         const int count = min(it.z, min(WorkP<T>::value, P.n - it.y));
@@ -458,81 +663,117 @@ __global__ void __launch_bounds__(kThreads) k_p2g(DevParams<T> P, DevBufs D) {
 #pragma unroll
                 for (int e = 0; e < 9; ++e) A[e] -= sc * G[e];
             }
-            T e3[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) e3[a] = (T)(St.b[a] - 1) * P.h - p.x[a];
-            T qp[3];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) qp[r] = mv[r] + (A[3 * r] * e3[0] + A[3 * r + 1] * e3[1] + A[3 * r + 2] * e3[2]);
-            vec4<T>* r = &S.rec[j * kRecV4];
-            r[0] = mk4<T>(St.w[0][0], St.w[0][1], St.w[0][2], St.w[0][3]);
-            r[1] = mk4<T>(St.w[1][0], St.w[1][1], St.w[1][2], St.w[1][3]);
-            r[2] = mk4<T>(St.w[2][0], St.w[2][1], St.w[2][2], St.w[2][3]);
-            r[3] = mk4<T>(qp[0], qp[1], qp[2], MOM ? p.m : T(0));
-            r[4] = mk4<T>(P.h * A[0], P.h * A[3], P.h * A[6], P.h * A[1]);
-            r[5] = mk4<T>(P.h * A[4], P.h * A[7], P.h * A[2], P.h * A[5]);
-            r[6] = mk4<T>(P.h * A[8], T(0), T(0), T(0));
+            write_record<T, MOM>(&S.rec[j * kRecV4], St, p.x, A, mv, p.m, P.h);
             const int cell = (St.rel[0] * kBlk + St.rel[1]) * kBlk + St.rel[2];
             S.cellof[j] = (uint8_t)cell;
             atomicAdd(&S.cnt[cell], 1);
         }
+        sort_records<T, kBlk>(S, count);
+        p2g_tasks<T, MOM, kBlk>(S, count);
         __syncthreads();
-        if (threadIdx.x < 32) {  // exclusive scan of the 64 cell counts
-            const int l = threadIdx.x;
-            const int a = S.cnt[2 * l], b = S.cnt[2 * l + 1];
-            int x = a + b;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, x, o);
-                if (l >= o) x += y;
-            }
-            S.off[2 * l] = x - a - b;
-            S.off[2 * l + 1] = x - b;
-        }
-        __syncthreads();
-        for (int c = threadIdx.x; c < kCells; c += blockDim.x) S.cnt[c] = S.off[c];  // cursor
-        __syncthreads();
-        for (int j = threadIdx.x; j < count; j += blockDim.x) {
-            const int c = S.cellof[j];
-            if (c != 0xff) S.order[atomicAdd(&S.cnt[c], 1)] = (uint16_t)j;
-        }
-        __syncthreads();
-        for (int c = threadIdx.x; c < kCells; c += blockDim.x) S.cnt[c] -= S.off[c];  // counts again
-        __syncthreads();
-        // phase 2: (cell, x offset) tasks
-        for (int task = threadIdx.x; task < kCells * 4; task += blockDim.x)
-            p2g_cell_task<T, MOM>(S, task % kCells, task / kCells);
-        __syncthreads();
-        for (int c = threadIdx.x; c < kTileCells; c += blockDim.x) {
-            size_t lin;
-            if (!cell_of_tile(P, org, c, lin)) continue;
-            const vec4<T> v = mk4<T>(S.tile[c], S.tile[kTileCells + c], S.tile[2 * kTileCells + c],
-                                     S.tile[3 * kTileCells + c]);
-            if (v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0)) red_add4(grid + lin, v);
-        }
+        p2g_flush<T, kBlk>(P, S, org, grid);
         __syncthreads();
     }
 }
 
-// ---------------------------------------------------------------- fused G2P
-// gridVelocitiesUpdate + updateDeformationGradient + updateParticleVelocities +
-// updateParticlePositions (material_point_method.cpp:256-262,306-350) for one
-// work item per loop trip.  The grid tile arrives as (m, p = m v + dt f) and is
-// turned into v = p / m + dt g (zero where m = 0 and on sticky walls) while it
-// is staged in shared memory.  The particle is written at its sorted position
-// into the other plane buffer, and its next block key is counted.
+// ---------------------------------------------------------------- fused G2P2G
+// One step for one work item per loop trip: gridVelocitiesUpdate,
+// updateDeformationGradient, updateParticleVelocities and
+// updateParticlePositions of this step (material_point_method.cpp:256-262,
+// 306-350), then rasterizeParticlesToGrid + computeExplicitGridForces of the
+// next step (:94-129,235-254) into the other grid buffer.
+//   * The 7^3 tile of grid n arrives as (m, p = m v + dt f) and becomes
+//     v = p / m + dt g (zero where m = 0 and on sticky walls) in shared memory.
+//   * A thread per particle: G2P, the plastic split, advection; the particle
+//     is written at its sorted slot of the other plane buffer and its next
+//     block key is counted; then its P2G record at x_{n+1}, whose stress comes
+//     from the split just made (no second SVD).
+//   * The records are scattered into a 9^3 tile of grid n+1 around the block
+//     (base cells within one cell of the block, 6^3 cell space); a particle
+//     that moved further goes straight to the grid.
+// The force of the next step uses this step's dt: rd_step recomputes the grid
+// with k_p2g when dt changes.
+constexpr int kFusedThreads = 256;
+static_assert(WorkP<float>::value <= kFusedThreads && WorkP<double>::value <= kFusedThreads,
+              "k_g2p2g runs at most one particle per thread");
+template <typename T> struct FusedShared {
+    vec4<T> gv[kTileCells];  // grid velocity of this step, (vx, vy, vz, 0)
+    P2GTile<T, kBlk + 2> p;
+};
+
+// G2P of one particle from the velocity tile (updateParticleVelocities,
+// material_point_method.cpp:332-342): v_p = sum w v_i and
+// B_p = sum w v_i (x_i - x_p)^T, evaluated separably: with w = wx wy wz and
+// (x_i - x_p) = (dx[ox], dy[oy], dz[oz]), the z sums of each (ox, oy) column
+// are formed first (sum wz v and sum wz dz v), then weighted by wy, wy dy and
+// by wx, wx dx.
+template <typename T>
+__device__ __forceinline__ void g2p_gather(const vec4<T>* __restrict__ gv, const Stencil<T>& St, T vp[3], T Bp[9]) {
+    T wzd[4], wyd[4];
+#pragma unroll
+    for (int o = 0; o < 4; ++o) { wzd[o] = St.w[2][o] * St.d[2][o]; wyd[o] = St.w[1][o] * St.d[1][o]; }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) vp[r] = T(0);
+#pragma unroll
+    for (int e = 0; e < 9; ++e) Bp[e] = T(0);
+#pragma unroll
+    for (int ox = 0; ox < 4; ++ox) {
+        T sx[3] = {T(0), T(0), T(0)}, sy[3] = {T(0), T(0), T(0)}, sz[3] = {T(0), T(0), T(0)};
+#pragma unroll
+        for (int oy = 0; oy < 4; ++oy) {
+            T col[3] = {T(0), T(0), T(0)}, colz[3] = {T(0), T(0), T(0)};
+            const int rowc = ((St.rel[0] + ox) * kTile + (St.rel[1] + oy)) * kTile + St.rel[2];
+#pragma unroll
+            for (int oz = 0; oz < 4; ++oz) {
+                const vec4<T> v = gv[rowc + oz];
+                col[0] += St.w[2][oz] * v.x; col[1] += St.w[2][oz] * v.y; col[2] += St.w[2][oz] * v.z;
+                colz[0] += wzd[oz] * v.x; colz[1] += wzd[oz] * v.y; colz[2] += wzd[oz] * v.z;
+            }
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                sx[r] += St.w[1][oy] * col[r];
+                sy[r] += wyd[oy] * col[r];
+                sz[r] += St.w[1][oy] * colz[r];
+            }
+        }
+        const T wx = St.w[0][ox], wxd = St.w[0][ox] * St.d[0][ox];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            vp[r] += wx * sx[r];
+            Bp[3 * r + 0] += wxd * sx[r];
+            Bp[3 * r + 1] += wx * sy[r];
+            Bp[3 * r + 2] += wx * sz[r];
+        }
+    }
+}
+
 template <typename T, bool TRACK_FP>
-__global__ void __launch_bounds__(kThreads) k_g2p_fused(DevParams<T> P, DevBufs D) {
-    __shared__ T sv[3 * kTileCells];
+__global__ void __launch_bounds__(kFusedThreads) k_g2p2g(DevParams<T> P, DevBufs D) {
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    FusedShared<T>& S = *reinterpret_cast<FusedShared<T>*>(smem_raw);
+    constexpr int CA = kBlk + 2;
     const vec4<T>* __restrict__ pin = static_cast<const vec4<T>*>(D.pin);
     vec4<T>* __restrict__ pout = static_cast<vec4<T>*>(D.pout);
     const vec4<T>* __restrict__ grid = static_cast<const vec4<T>*>(D.grid);
-    const uint32_t nw = *D.nwork;
+    vec4<T>* __restrict__ gnext = static_cast<vec4<T>*>(D.grid_next);
+    const uint32_t nw = min(*D.nwork, D.work_cap);
     const size_t n = (size_t)P.n;
     for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
         const int4 it = D.work[wi];
         int org[3];
         tile_origin(P, it.x, org);
+        const int porg[3] = {org[0] - 1, org[1] - 1, org[2] - 1};
+        const int count = min(it.z, min(WorkP<T>::value, P.n - it.y));
+        // one particle per thread (WorkP == blockDim): start its loads before
+        // the tile is staged so the two latencies overlap
+        const int j = threadIdx.x;
+        Particle<T> p;
+        T FP[9];
+        if (j < count) {
+            const uint32_t src = D.perm[it.y + j];
+            load_particle(pin, n, src, p);
+            if (TRACK_FP) load_fp(pin, n, src, FP);
+        }
         for (int c = threadIdx.x; c < kTileCells; c += blockDim.x) {
             size_t lin;
             T v0 = T(0), v1 = T(0), v2 = T(0);
@@ -548,47 +789,24 @@ __global__ void __launch_bounds__(kThreads) k_g2p_fused(DevParams<T> P, DevBufs 
                     }
                 }
             }
-            sv[c] = v0; sv[kTileCells + c] = v1; sv[2 * kTileCells + c] = v2;
+            S.gv[c] = mk4<T>(v0, v1, v2, T(0));
         }
+        for (int c = threadIdx.x; c < 4 * P2GTile<T, CA>::TC; c += blockDim.x) S.p.tile[c] = T(0);
+        for (int c = threadIdx.x; c < P2GTile<T, CA>::NC; c += blockDim.x) S.p.cnt[c] = 0;
         __syncthreads();
-        const int send = min(it.y + it.z, P.n);
-        for (int s = it.y + threadIdx.x; s < send; s += blockDim.x) {
-            Particle<T> p;
-            const uint32_t src = D.perm[s];
-            load_particle(pin, n, src, p);
-            T FP[9];
-            if (TRACK_FP) load_fp(pin, n, src, FP);
-            Stencil<T> S;
-            const bool ok = make_stencil(P, p.x, org, S);
+        if (j < count) {
+            const int s = it.y + j;
+            Stencil<T> St;
+            const bool ok = make_stencil(P, p.x, org, St);
             if (!ok) raise_flag(D.flags, 4u);
-            if (P.lagged) update_F<T, TRACK_FP>(P, p.B, p.F, p.Jp, FP);
+            Split<T> sp;
+            if (P.lagged) update_F<T, TRACK_FP>(P, p.B, p.F, p.Jp, FP, sp);
             T vp[3] = {T(0), T(0), T(0)};
             T Bp[9];
 #pragma unroll
             for (int e = 0; e < 9; ++e) Bp[e] = T(0);
-            if (ok) {
-#pragma unroll
-                for (int ox = 0; ox < 4; ++ox)
-#pragma unroll
-                    for (int oy = 0; oy < 4; ++oy) {
-                        const T wxy = S.w[0][ox] * S.w[1][oy];
-                        const int rowc = ((S.rel[0] + ox) * kTile + (S.rel[1] + oy)) * kTile + S.rel[2];
-#pragma unroll
-                        for (int oz = 0; oz < 4; ++oz) {
-                            const T w = wxy * S.w[2][oz];
-                            const int cell = rowc + oz;
-                            const T vi[3] = {sv[cell], sv[kTileCells + cell], sv[2 * kTileCells + cell]};
-                            const T dd[3] = {S.d[0][ox], S.d[1][oy], S.d[2][oz]};
-#pragma unroll
-                            for (int r = 0; r < 3; ++r) {
-                                vp[r] += vi[r] * w;
-#pragma unroll
-                                for (int c = 0; c < 3; ++c) Bp[3 * r + c] += w * (vi[r] * dd[c]);
-                            }
-                        }
-                    }
-            }
-            if (!P.lagged) update_F<T, TRACK_FP>(P, Bp, p.F, p.Jp, FP);
+            if (ok) g2p_gather(S.gv, St, vp, Bp);
+            if (!P.lagged) update_F<T, TRACK_FP>(P, Bp, p.F, p.Jp, FP, sp);
 #pragma unroll
             for (int a = 0; a < 3; ++a) p.v[a] = vp[a];
 #pragma unroll
@@ -597,16 +815,40 @@ __global__ void __launch_bounds__(kThreads) k_g2p_fused(DevParams<T> P, DevBufs 
             for (int a = 0; a < 3; ++a) p.x[a] = clampx(p.x[a] + p.v[a] * P.dt, P.xlo, P.xhi[a]);
             store_particle(pout, n, s, p);
             if (TRACK_FP) store_fp(pout, n, s, FP);
-            const int b[3] = {base_of(p.x[0], P.h), base_of(p.x[1], P.h), base_of(p.x[2], P.h)};
-            const uint32_t key = block_key(P, b);
-            D.keys_out[s] = key;
-            count_key(D.counts, key);
             bool finite = isfinite(p.x[0]) && isfinite(p.x[1]) && isfinite(p.x[2]) && isfinite(p.v[0]) &&
                           isfinite(p.v[1]) && isfinite(p.v[2]) && isfinite(p.Jp);
 #pragma unroll
             for (int e = 0; e < 9; ++e) finite = finite && isfinite(p.F[e]) && isfinite(p.B[e]);
             if (!finite) raise_flag(D.flags, 2u);
+            // next step's P2G record
+            Stencil<T> S2;
+            const bool in_space = make_stencil(P, p.x, porg, S2, CA - 1);
+            const uint32_t key = sort_key(P, S2.b);
+            D.keys_out[s] = key;
+            count_key(D.counts, key);
+            if (!stencil_in_grid(P, S2.b)) raise_flag(D.flags, 1u);
+            T G[9], A[9], mv[3];
+            stress_from_split(P, sp, p.Jp, G);
+            const T sc = P.fscale * (p.vol * P.dinv);
+#pragma unroll
+            for (int e = 0; e < 9; ++e) A[e] = p.m * (p.B[e] * P.dinv) - sc * G[e];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) mv[a] = p.m * p.v[a];
+            vec4<T>* rec = &S.p.rec[j * kRecV4];
+            write_record<T, true>(rec, S2, p.x, A, mv, p.m, P.h);
+            if (in_space) {
+                const int cell = (S2.rel[0] * CA + S2.rel[1]) * CA + S2.rel[2];
+                S.p.cellof[j] = (uint8_t)cell;
+                atomicAdd(&S.p.cnt[cell], 1);
+            } else {
+                S.p.cellof[j] = 0xff;
+                p2g_direct(P, rec, S2.b, gnext);
+            }
         }
+        sort_records<T, CA>(S.p, count);
+        p2g_tasks<T, true, CA>(S.p, count);
+        __syncthreads();
+        p2g_flush<T, CA>(P, S.p, porg, gnext);
         __syncthreads();
     }
 }
@@ -650,7 +892,8 @@ __global__ void __launch_bounds__(kThreads) k_update_F(DevParams<T> P, vec4<T>* 
     load_particle(pl, n, i, p);
     T FP[9];
     if (TRACK_FP) load_fp(pl, n, i, FP);
-    update_F<T, TRACK_FP>(P, p.B, p.F, p.Jp, FP);
+    Split<T> sp;
+    update_F<T, TRACK_FP>(P, p.B, p.F, p.Jp, FP, sp);
     store_particle(pl, n, i, p);
     if (TRACK_FP) store_fp(pl, n, i, FP);
 }
@@ -661,7 +904,7 @@ __global__ void __launch_bounds__(kThreads) k_g2p_stage(DevParams<T> P, DevBufs 
     __shared__ T sv[3 * kTileCells];
     vec4<T>* __restrict__ pl = static_cast<vec4<T>*>(D.pout);
     const vec4<T>* __restrict__ grid = static_cast<const vec4<T>*>(D.grid);
-    const uint32_t nw = *D.nwork;
+    const uint32_t nw = min(*D.nwork, D.work_cap);
     const size_t n = (size_t)P.n;
     for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
         const int4 it = D.work[wi];
@@ -768,7 +1011,7 @@ __global__ void k_volumes(DevParams<T> P, vec4<T>* __restrict__ pl, const vec4<T
 }
 
 // Grid export: mass and velocity per cell as the reference holds them; in
-// fused mode (m, p) -> v = p / m + dt g (+ walls) as k_g2p_fused stages it.
+// fused mode (m, p) -> v = p / m + dt g (+ walls) as k_g2p2g stages it.
 template <typename T, bool FUSED>
 __global__ void k_grid_export(DevParams<T> P, const vec4<T>* __restrict__ grid, T* __restrict__ mass,
                               T* __restrict__ vel) {

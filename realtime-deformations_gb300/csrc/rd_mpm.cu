@@ -104,7 +104,8 @@ struct rd_handle {
     int n = 0;
     size_t ncells = 0;
     int NB[3] = {0, 0, 0};
-    int nkeys = 0;
+    int nblocks = 0;  // 4x4x4-cell blocks
+    int nkeys = 0;    // sort keys: blocks x 64 cells
     int planes = kPlanes;
     size_t esize = 4;
     void* pl[2] = {nullptr, nullptr};
@@ -114,9 +115,14 @@ struct rd_handle {
     uint32_t* counts = nullptr;
     uint32_t* cursor = nullptr;
     int4* work = nullptr;
-    uint32_t* nwork = nullptr;
+    uint32_t* nwork2 = nullptr;  // two item counters: the current sort's and the next's
+    int nb = 0;                  // nwork2[nb] belongs to the last sort
+    uint32_t* tile_sums = nullptr;
     size_t work_cap = 0;
-    void* grid = nullptr;
+    void* grid[2] = {nullptr, nullptr};  // (m, p) of this step / the next (fused); (m, v) in stage mode
+    int g = 0;                           // current grid buffer
+    bool fgrid_valid = false;            // grid[g] holds P2G(x) for rd_step with fgrid_dt
+    double fgrid_dt = 0.0;
     void* gforce = nullptr;
     uint32_t* flags = nullptr;
     float4* xyzs = nullptr;
@@ -218,8 +224,10 @@ template <typename T> DevBufs bufs(rd_handle* h) {
     D.keys_out = h->keys[h->cur ^ 1];
     D.counts = h->counts;
     D.work = h->work;
-    D.nwork = h->nwork;
-    D.grid = h->grid;
+    D.nwork = h->nwork2 + h->nb;
+    D.work_cap = (uint32_t)h->work_cap;
+    D.grid = h->grid[h->g];
+    D.grid_next = h->grid[h->g ^ 1];
     D.gforce = h->gforce;
     D.flags = h->flags;
     return D;
@@ -265,7 +273,7 @@ void tmark_end(rd_handle* h, long i) {
 // scan + work items, scatter into perm.
 template <typename T> rd_status sort_particles(rd_handle* h) {
     if (h->n == 0) {
-        RD_TRY(check_cuda(h, cudaMemsetAsync(h->nwork, 0, sizeof(uint32_t), h->stream), "memset nwork"));
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->nwork2, 0, 2 * sizeof(uint32_t), h->stream), "memset nwork"));
         h->sorted = true;
         return RD_OK;
     }
@@ -278,11 +286,19 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
         tmark_end(h, t);
         RD_TRY(launched(h, "k_keys"));
     }
+    const int ntiles = (h->nkeys + kScanTile - 1) / kScanTile;
+    // this sort fills nwork2[nb ^ 1] (cleared by the previous sort or at
+    // creation) and clears nwork2[nb] for the next one
+    uint32_t* nw = h->nwork2 + (h->nb ^ 1);
+    uint32_t* nw_next = h->nwork2 + h->nb;
     long t = tmark_begin(h, RD_KERNEL_SCAN);
-    k_scan<<<1, 1024, 0, h->stream>>>(h->counts, h->cursor, h->work, h->nwork, h->nkeys, (uint32_t)h->n,
-                                      (uint32_t)h->work_cap, (uint32_t)WorkP<T>::value, h->flags);
+    k_tile_sums<<<ntiles, 256, 0, h->stream>>>(h->counts, h->nkeys, h->tile_sums);
+    k_scan<<<ntiles, kScanThreads, 0, h->stream>>>(h->counts, h->cursor, h->tile_sums, h->nkeys, h->work, nw, nw_next,
+                                                (uint32_t)h->n, (uint32_t)h->work_cap, (uint32_t)WorkP<T>::value,
+                                                h->flags);
     tmark_end(h, t);
-    RD_TRY(launched(h, "k_scan"));
+    RD_TRY(launched(h, "k_scan", 2));
+    h->nb ^= 1;
     t = tmark_begin(h, RD_KERNEL_SCATTER);
     k_scatter<<<blocks_for(h->n, 256), 256, 0, h->stream>>>(h->n, h->keys[h->cur], h->cursor, h->perm);
     tmark_end(h, t);
@@ -293,33 +309,49 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
 }
 
 template <typename T> unsigned persistent_grid(const rd_handle* h, int occ) {
-    const size_t max_items = (size_t)h->n / WorkP<T>::value + (size_t)std::min<int64_t>(h->nkeys, h->n) + 1;
+    const size_t max_items = (size_t)h->n / WorkP<T>::value + (size_t)std::min<int64_t>(h->nblocks, h->n) + 1;
     return (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)h->sms * occ));
 }
 
 template <typename T> rd_status step_fused(rd_handle* h, double dt) {
+    const size_t gbytes = h->ncells * sizeof(vec4<T>);
+    if (h->n == 0) {
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid[h->g ^ 1], 0, gbytes, h->stream), "memset grid"));
+        h->g ^= 1;
+        h->grid_mode = GRID_FUSED;
+        h->last_dt = dt;
+        return RD_OK;
+    }
     if (!h->sorted) RD_TRY(sort_particles<T>(h));
-    long t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
-    RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid, 0, h->ncells * sizeof(vec4<T>), h->stream), "memset grid"));
-    tmark_end(h, t);
-    if (h->n > 0) {
-        DevParams<T> P = make_params<T>(h, dt, (T)dt);
+    DevParams<T> P = make_params<T>(h, dt, (T)dt);
+    long t;
+    if (!(h->fgrid_valid && h->fgrid_dt == dt)) {  // P2G of the current state
+        t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid[h->g], 0, gbytes, h->stream), "memset grid"));
+        tmark_end(h, t);
         DevBufs D = bufs<T>(h);
         t = tmark_begin(h, RD_KERNEL_P2G);
-        k_p2g<T, true, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+        k_p2g<T, true, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GTile<T, kBlk>), h->stream>>>(P, D);
         tmark_end(h, t);
         RD_TRY(launched(h, "k_p2g"));
-        t = tmark_begin(h, RD_KERNEL_G2P);
-        if (h->prm.track_fp)
-            k_g2p_fused<T, true><<<persistent_grid<T>(h, h->occ_g2p), kThreads, 0, h->stream>>>(P, D);
-        else
-            k_g2p_fused<T, false><<<persistent_grid<T>(h, h->occ_g2p), kThreads, 0, h->stream>>>(P, D);
-        tmark_end(h, t);
-        RD_TRY(launched(h, "k_g2p_fused"));
-        h->cur ^= 1;
-        h->keys_valid = true;  // k_g2p_fused wrote keys[cur] and counted them
-        h->sorted = false;
     }
+    t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
+    RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid[h->g ^ 1], 0, gbytes, h->stream), "memset grid"));
+    tmark_end(h, t);
+    DevBufs D = bufs<T>(h);
+    t = tmark_begin(h, RD_KERNEL_G2P2G);
+    if (h->prm.track_fp)
+        k_g2p2g<T, true><<<persistent_grid<T>(h, h->occ_g2p), kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
+    else
+        k_g2p2g<T, false><<<persistent_grid<T>(h, h->occ_g2p), kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
+    tmark_end(h, t);
+    RD_TRY(launched(h, "k_g2p2g"));
+    h->cur ^= 1;
+    h->g ^= 1;
+    h->keys_valid = true;  // k_g2p2g wrote keys[cur] and counted them
+    h->sorted = false;
+    h->fgrid_valid = true;
+    h->fgrid_dt = dt;
     h->grid_mode = GRID_FUSED;
     h->last_dt = dt;
     return RD_OK;
@@ -329,17 +361,18 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
     const size_t nc = h->ncells;
     const unsigned cb = blocks_for(nc, 256);
     DevParams<T> P = make_params<T>(h, dt, T(1));
+    h->fgrid_valid = false;
     switch (stage) {
         case RD_STAGE_RASTERIZE: {
             if (!h->sorted) RD_TRY(sort_particles<T>(h));
-            RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid, 0, nc * sizeof(vec4<T>), h->stream), "memset grid"));
+            RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid[h->g], 0, nc * sizeof(vec4<T>), h->stream), "memset grid"));
             RD_TRY(check_cuda(h, cudaMemsetAsync(h->gforce, 0, nc * sizeof(vec4<T>), h->stream), "memset force"));
             if (h->n > 0) {
                 DevBufs D = bufs<T>(h);
-                k_p2g<T, true, false><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+                k_p2g<T, true, false><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GTile<T, kBlk>), h->stream>>>(P, D);
                 RD_TRY(launched(h, "k_p2g<rasterize>"));
             }
-            k_grid_normalize<T><<<cb, 256, 0, h->stream>>>(static_cast<vec4<T>*>(h->grid), nc);
+            k_grid_normalize<T><<<cb, 256, 0, h->stream>>>(static_cast<vec4<T>*>(h->grid[h->g]), nc);
             RD_TRY(launched(h, "k_grid_normalize"));
             h->grid_mode = GRID_V;
             return RD_OK;
@@ -349,14 +382,14 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
             if (!h->sorted) RD_TRY(sort_particles<T>(h));
             if (h->n > 0) {
                 DevBufs D = bufs<T>(h);
-                k_p2g<T, false, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+                k_p2g<T, false, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GTile<T, kBlk>), h->stream>>>(P, D);
                 RD_TRY(launched(h, "k_p2g<forces>"));
             }
             return RD_OK;
         }
         case RD_STAGE_GRID_VELOCITIES:
             if (h->grid_mode != GRID_V) return fail(h, RD_INVALID_ARG, "grid velocity stage needs a rasterized grid");
-            k_grid_velocities<T><<<cb, 256, 0, h->stream>>>(P, static_cast<vec4<T>*>(h->grid),
+            k_grid_velocities<T><<<cb, 256, 0, h->stream>>>(P, static_cast<vec4<T>*>(h->grid[h->g]),
                                                              static_cast<const vec4<T>*>(h->gforce));
             return launched(h, "k_grid_velocities");
         case RD_STAGE_COLLISIONS:
@@ -390,7 +423,7 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
                 return fail(h, RD_INVALID_ARG, "volume stage needs a rasterized grid");
             if (h->n == 0) return RD_OK;
             k_volumes<T><<<blocks_for(h->n, 256), 256, 0, h->stream>>>(P, static_cast<vec4<T>*>(h->pl[h->cur]),
-                                                                        static_cast<const vec4<T>*>(h->grid),
+                                                                        static_cast<const vec4<T>*>(h->grid[h->g]),
                                                                         h->flags);
             return launched(h, "k_volumes");
         default:
@@ -425,6 +458,7 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, const rd_partic
     }
     h->keys_valid = false;
     h->sorted = false;
+    h->fgrid_valid = false;
     h->grid_mode = GRID_NONE;
     return RD_OK;
 }
@@ -464,11 +498,11 @@ template <typename T> rd_status get_grid_impl(rd_handle* h, void* mass, void* ve
     T* v_d = host ? scratch + nc : static_cast<T*>(vel);
     DevParams<T> P = make_params<T>(h, h->last_dt, T(1));
     const unsigned cb = blocks_for(nc, 256);
-    if (h->grid_mode == GRID_FUSED)
-        k_grid_export<T, true><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid), mass ? m_d : nullptr,
-                                                          vel ? v_d : nullptr);
+    if (h->grid_mode == GRID_FUSED)  // the grid the last step's G2P read
+        k_grid_export<T, true><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g ^ 1]),
+                                                          mass ? m_d : nullptr, vel ? v_d : nullptr);
     else
-        k_grid_export<T, false><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid),
+        k_grid_export<T, false><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g]),
                                                            mass ? m_d : nullptr, vel ? v_d : nullptr);
     RD_TRY(launched(h, "k_grid_export"));
     T* f_d = nullptr;
@@ -525,16 +559,19 @@ template <typename T> rd_status init_volumes_impl(rd_handle* h) {
 
 template <typename T> rd_status occupancy(rd_handle* h) {
     int o = 0;
-    const int sm = (int)sizeof(P2GShared<T>);
+    const int sm = (int)sizeof(P2GTile<T, kBlk>);
     RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_p2g<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
     RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_p2g<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
     RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_p2g<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
     RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true>, kThreads, sm), "occ"));
     h->occ_p2g = std::max(1, o);
+    const int fsm = (int)sizeof(FusedShared<T>);
+    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_g2p2g<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm), "smem attr"));
+    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_g2p2g<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm), "smem attr"));
     if (h->prm.track_fp)
-        RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_g2p_fused<T, true>, kThreads, 0), "occ"));
+        RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_g2p2g<T, true>, kFusedThreads, fsm), "occ"));
     else
-        RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_g2p_fused<T, false>, kThreads, 0), "occ"));
+        RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_g2p2g<T, false>, kFusedThreads, fsm), "occ"));
     h->occ_g2p = std::max(1, o);
     return RD_OK;
 }
@@ -544,7 +581,7 @@ void release(rd_handle* h) {
         if (e) cudaEventDestroy(e);
     h->ev.clear();
     void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->cursor, h->work,
-                    h->nwork, h->grid, h->gforce, h->flags, h->xyzs, h->io, h->grid_io};
+                    h->nwork2, h->tile_sums, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -592,7 +629,8 @@ rd_status rd_create(const rd_params* params, rd_handle** out) {
     h->NB[0] = (p.max_i + kBlk - 1) / kBlk;
     h->NB[1] = (p.max_j + kBlk - 1) / kBlk;
     h->NB[2] = (p.max_k + kBlk - 1) / kBlk;
-    h->nkeys = h->NB[0] * h->NB[1] * h->NB[2];
+    h->nblocks = h->NB[0] * h->NB[1] * h->NB[2];
+    h->nkeys = h->nblocks * kCellsPerBlock;
     auto bail = [&](rd_status s) { release(h); delete h; return s; };
     if (cudaSetDevice(p.device) != cudaSuccess) return bail(RD_CUDA_ERROR);
     cudaDeviceProp prop;
@@ -602,7 +640,7 @@ rd_status rd_create(const rd_params* params, rd_handle** out) {
     const size_t n = std::max<size_t>(1, (size_t)h->n);
     const size_t v4 = 4 * h->esize;
     const size_t wp = p.precision == RD_FP64 ? WorkP<double>::value : WorkP<float>::value;
-    h->work_cap = n / wp + std::min<size_t>((size_t)h->nkeys, n) + 2;
+    h->work_cap = n / wp + std::min<size_t>((size_t)h->nblocks, n) + 2;
     struct { void** ptr; size_t bytes; } allocs[] = {
         {&h->pl[0], (size_t)h->planes * n * v4},
         {&h->pl[1], (size_t)h->planes * n * v4},
@@ -612,8 +650,10 @@ rd_status rd_create(const rd_params* params, rd_handle** out) {
         {(void**)&h->counts, (size_t)h->nkeys * 4},
         {(void**)&h->cursor, (size_t)h->nkeys * 4},
         {(void**)&h->work, h->work_cap * sizeof(int4)},
-        {(void**)&h->nwork, 4},
-        {&h->grid, h->ncells * v4},
+        {(void**)&h->nwork2, 8},
+        {(void**)&h->tile_sums, (size_t)((h->nkeys + kScanTile - 1) / kScanTile) * 4},
+        {&h->grid[0], h->ncells * v4},
+        {&h->grid[1], h->ncells * v4},
         {&h->gforce, h->ncells * v4},
         {(void**)&h->flags, 4},
         {(void**)&h->xyzs, n * sizeof(float4)},
@@ -629,7 +669,7 @@ rd_status rd_create(const rd_params* params, rd_handle** out) {
     cudaMemsetAsync(h->counts, 0, (size_t)h->nkeys * 4, h->stream);
     cudaMemsetAsync(h->perm, 0, n * 4, h->stream);  // every entry is a valid index from the start
     cudaMemsetAsync(h->flags, 0, 4, h->stream);
-    cudaMemsetAsync(h->nwork, 0, 4, h->stream);
+    cudaMemsetAsync(h->nwork2, 0, 8, h->stream);
     rd_status s = p.precision == RD_FP64 ? occupancy<double>(h) : occupancy<float>(h);
     if (s != RD_OK) return bail(s);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(RD_CUDA_ERROR);
