@@ -1,0 +1,254 @@
+// rd_lagrange_euler_view.hpp - C++ drop-in for the simulation class of
+// brocbyte/realtime-deformations, MaterialPointMethod::LagrangeEulerView
+// (realtime-deformations/material_point_method.hpp:174-233), implemented over
+// the C ABI of rd_mpm.h.  Header only; link against librd_mpm.so.
+//
+// A main.cpp-style driver keeps its calls (main.cpp:48-54,192-218):
+//
+//     MaterialPointMethod::WeightCalculator::h = 0.05f;      // before construction
+//     MaterialPointMethod::LagrangeEulerView MPM{20, 20, 20, 2147};
+//     MPM.initializeParticles({0.5f, 0.6f, 0.5f}, {0.0f, -200.0f, 0.0f});
+//     MPM.rasterizeParticlesToGrid();
+//     MPM.computeParticleVolumesAndDensities();
+//     for (;;) { MPM.rasterizeParticlesToGrid(); ...; MPM.updateParticlePositions(dt); }
+//
+// or replaces the seven stage calls by MPM.step(dt), the fused path.
+// getParticles() returns a host array of Particle synchronised from the device
+// on each call; writes through it reach the device only through
+// syncParticlesToDevice().  Errors throw rd::Error (a std::runtime_error).
+//
+// With glm on the include path the vector and matrix members are glm::vec3 and
+// glm::mat3 as in the reference (material_point_method.hpp:96-110); otherwise
+// small stand-ins with the same member access (x/y/z, m[col][row]) are used.
+#pragma once
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "rd_mpm.h"
+
+#if defined(RD_WITH_GLM) || __has_include(<glm/glm.hpp>)
+#include <glm/glm.hpp>
+namespace rd_facade {
+using vec3 = glm::vec3;
+using mat3 = glm::mat3;
+}  // namespace rd_facade
+#else
+namespace rd_facade {
+struct vec3 {
+    float x = 0, y = 0, z = 0;
+    vec3() = default;
+    vec3(float a, float b, float c) : x(a), y(b), z(c) {}
+    float& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+    float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+struct mat3 {  // column-major like glm: m[col][row]
+    vec3 c[3];
+    explicit mat3(float d = 1.0f) { c[0] = {d, 0, 0}; c[1] = {0, d, 0}; c[2] = {0, 0, d}; }
+    vec3& operator[](int i) { return c[i]; }
+    const vec3& operator[](int i) const { return c[i]; }
+};
+}  // namespace rd_facade
+#endif
+
+namespace rd {
+struct Error : std::runtime_error {
+    rd_status status;
+    Error(rd_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+}  // namespace rd
+
+namespace MaterialPointMethod {
+
+namespace WeightCalculator {
+// The reference's global cell size (material_point_method.cpp:17); read when a
+// LagrangeEulerView is constructed.
+inline float h = 0.05f;
+}  // namespace WeightCalculator
+
+// material_point_method.hpp:96-110 without the per-step neighbour list.
+struct Particle {
+    float mass = 0;
+    rd_facade::vec3 velocity;
+    float volume = 0;
+    rd_facade::vec3 pos;
+    rd_facade::mat3 FElastic{1.0f};
+    rd_facade::mat3 FPlastic{1.0f};
+    rd_facade::mat3 B{0.0f};
+    unsigned char r = 255, g = 255, b = 255, a = 255;  // colour (viewer only)
+    float size = 0.02f;
+};
+
+// material_point_method.cpp:18-63 with utils.h:110-127: 8 quarter-offset
+// points per cell of a cube around the origin, each jittered inside a ball of
+// a quarter cell drawn with the C library's rand(), kept within 0.2 of the
+// origin, mass 6e-5, filled from the last particle down; accepted points also
+// draw three colour values.  The types follow the reference's (randFloat
+// returns float, cos theta is double) so the same rand() sequence gives the
+// same positions.  Returns how many accepted points did not fit.
+inline int reference_initial_particles(float h, const rd_facade::vec3& origin, const rd_facade::vec3& velocity,
+                                       std::vector<Particle>& particles) {
+    const float width = 0.2f;
+    const int cx = static_cast<int>(origin.x / h), cy = static_cast<int>(origin.y / h),
+              cz = static_cast<int>(origin.z / h);
+    const int wic = static_cast<int>(width / h);
+    static const float ds[8][3] = {{1, 1, 1}, {1, 1, 3}, {1, 3, 1}, {1, 3, 3},
+                                   {3, 1, 1}, {3, 1, 3}, {3, 3, 1}, {3, 3, 3}};
+    int left = static_cast<int>(particles.size()), need_more = 0;
+    auto rand_float = [](float lo, float hi) -> float { return lo + (std::rand() % 2000) / 2000.0 * (hi - lo); };
+    for (int i = cx - wic; i < cx + wic; ++i)
+        for (int j = cy - wic; j < cy + wic; ++j)
+            for (int k = cz - wic; k < cz + wic; ++k)
+                for (int d = 0; d < 8; ++d) {
+                    const float phi = rand_float(0.0f, 2.0 * 3.1415);
+                    const double costheta = rand_float(0.0, 2.0) - 1.0;
+                    const float u = rand_float(0.0, 1.0);
+                    const double theta = std::acos(costheta);
+                    const float r = 0.25f * std::cbrt(u);
+                    const float jx = r * std::sin(theta) * std::cos((double)phi);
+                    const float jy = r * std::sin(theta) * std::sin((double)phi);
+                    const float jz = r * std::cos(theta);
+                    const float px = (i + ds[d][0] * (1 / 4.0f) + jx) * h;
+                    const float py = (j + ds[d][1] * (1 / 4.0f) + jy) * h;
+                    const float pz = (k + ds[d][2] * (1 / 4.0f) + jz) * h;
+                    const float dx = px - origin.x, dy = py - origin.y, dz = pz - origin.z;
+                    if (std::sqrt(dx * dx + dy * dy + dz * dz) > width) continue;
+                    if (!left) { ++need_more; continue; }
+                    Particle& p = particles[--left];
+                    p.pos = rd_facade::vec3(px, py, pz);
+                    p.velocity = velocity;
+                    for (int c = 0; c < 3; ++c) (void)std::rand();  // colour draws, overwritten with white
+                    p.mass = 0.00006f;
+                }
+    return need_more;
+}
+
+class LagrangeEulerView {
+public:
+    const int MAX_I, MAX_J, MAX_K;
+
+    // material_point_method.cpp:144-154.  Extra parameters are optional and
+    // default to the reference's constants.
+    LagrangeEulerView(int max_i, int max_j, int max_k, int particlesNum, const rd_params* extra = nullptr)
+        : MAX_I(max_i), MAX_J(max_j), MAX_K(max_k), n_(particlesNum), particles_(particlesNum) {
+        rd_params p;
+        if (extra) p = *extra; else rd_default_params(&p);
+        p.max_i = max_i; p.max_j = max_j; p.max_k = max_k; p.num_particles = particlesNum;
+        p.h = WeightCalculator::h;
+        p.track_fp = 1;
+        h_ = p.h;
+        check(rd_create(&p, &sim_), "rd_create");
+        host_.resize(static_cast<size_t>(n_) * 36);
+    }
+    ~LagrangeEulerView() { if (sim_) rd_destroy(sim_); }
+    LagrangeEulerView(const LagrangeEulerView&) = delete;
+    LagrangeEulerView& operator=(const LagrangeEulerView&) = delete;
+
+    int getNumParticles() const { return n_; }
+
+    // The reference's initialiser (see reference_initial_particles), then upload.
+    void initializeParticles(const rd_facade::vec3& origin, const rd_facade::vec3& velocity) {
+        reference_initial_particles(h_, origin, velocity, particles_);
+        syncParticlesToDevice();
+    }
+
+    // Returns the host copy, synchronised from the device (material_point_method.hpp:181-183).
+    Particle* getParticles() {
+        if (dirty_host_) download();
+        return particles_.data();
+    }
+    // Uploads the host copy after the caller changed particles through getParticles().
+    void syncParticlesToDevice() { upload(); }
+
+    void rasterizeParticlesToGrid() { stage(RD_STAGE_RASTERIZE, 0.0); }
+    void computeParticleVolumesAndDensities() { stage(RD_STAGE_VOLUMES, 0.0); }
+    void computeExplicitGridForces() { stage(RD_STAGE_FORCES, 0.0); }
+    void gridVelocitiesUpdate(float timeDelta) { stage(RD_STAGE_GRID_VELOCITIES, timeDelta); }
+    template <typename Colliders>
+    void gridBasedCollisions(float timeDelta, const Colliders& objects) {
+        if (!objects.empty()) throw rd::Error(RD_NOT_SUPPORTED, "SDF colliders are not part of this path");
+        stage(RD_STAGE_COLLISIONS, timeDelta);
+    }
+    void updateDeformationGradient(float timeDelta) { stage(RD_STAGE_DEFORMATION, timeDelta); }
+    void updateParticleVelocities() { stage(RD_STAGE_PARTICLE_VELOCITIES, 0.0); }
+    void updateParticlePositions(float timeDelta) { stage(RD_STAGE_POSITIONS, timeDelta); }
+
+    // The seven stage calls of main.cpp:192-218, fused (rd_step).
+    void step(float timeDelta, int nsteps = 1) {
+        check(rd_step(sim_, timeDelta, nsteps), "rd_step");
+        dirty_host_ = true;
+    }
+
+    rd_handle* handle() { return sim_; }
+
+private:
+    void check(rd_status s, const char* what) {
+        if (s == RD_OK) return;
+        char buf[256] = {0};
+        if (sim_) rd_last_error(sim_, buf, sizeof buf);
+        throw rd::Error(s, std::string(what) + ": " + buf);
+    }
+    void stage(int id, double dt) {
+        check(rd_stage(sim_, id, dt), "rd_stage");
+        dirty_host_ = true;
+    }
+    // host_ holds the SoA exchange arrays: x 3n | v 3n | B 9n | FE 9n | FP 9n | mass n | vol n | Jp n
+    float* soa(int k) {
+        static const size_t off[] = {0, 3, 6, 15, 24, 33, 34, 35};
+        return host_.data() + off[k] * static_cast<size_t>(n_);
+    }
+    rd_particles views() {
+        rd_particles v;
+        v.x = soa(0); v.v = soa(1); v.B = soa(2); v.FE = soa(3); v.FP = soa(4); v.mass = soa(5);
+        v.volume = soa(6); v.Jp = soa(7);
+        return v;
+    }
+    void upload() {
+        for (int i = 0; i < n_; ++i) {
+            const Particle& p = particles_[i];
+            for (int a = 0; a < 3; ++a) { soa(0)[3 * i + a] = p.pos[a]; soa(1)[3 * i + a] = p.velocity[a]; }
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) {
+                    soa(2)[9 * i + 3 * r + c] = p.B[c][r];
+                    soa(3)[9 * i + 3 * r + c] = p.FElastic[c][r];
+                    soa(4)[9 * i + 3 * r + c] = p.FPlastic[c][r];
+                }
+            soa(5)[i] = p.mass;
+            soa(6)[i] = p.volume;
+        }
+        rd_particles v = views();
+        v.Jp = nullptr;  // det F_P from FP
+        check(rd_set_particles(sim_, &v, RD_HOST), "rd_set_particles");
+        dirty_host_ = false;
+    }
+    void download() {
+        rd_particles v = views();
+        check(rd_get_particles(sim_, &v, RD_HOST), "rd_get_particles");
+        for (int i = 0; i < n_; ++i) {
+            Particle& p = particles_[i];
+            for (int a = 0; a < 3; ++a) { p.pos[a] = soa(0)[3 * i + a]; p.velocity[a] = soa(1)[3 * i + a]; }
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) {
+                    p.B[c][r] = soa(2)[9 * i + 3 * r + c];
+                    p.FElastic[c][r] = soa(3)[9 * i + 3 * r + c];
+                    p.FPlastic[c][r] = soa(4)[9 * i + 3 * r + c];
+                }
+            p.mass = soa(5)[i];
+            p.volume = soa(6)[i];
+        }
+        dirty_host_ = false;
+    }
+
+    int n_;
+    float h_ = 0.05f;
+    rd_handle* sim_ = nullptr;
+    std::vector<Particle> particles_;
+    std::vector<float> host_;
+    bool dirty_host_ = false;
+};
+
+}  // namespace MaterialPointMethod

@@ -1,0 +1,45 @@
+"""The C++ drop-in header (include/rd_lagrange_euler_view.hpp): the
+reference's initialiser restated in it (CPU) and a main.cpp-style driver
+linked against the CUDA library (GPU)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import REPO, b_scale, golden, rel, rel_floor
+
+INC = os.path.join(REPO, "include")
+CPP = os.path.join(REPO, "tests", "cpp")
+
+
+def test_reference_initialiser_is_bit_exact(tmp_path):
+    exe = tmp_path / "init_positions"
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", INC, os.path.join(CPP, "init_positions.cpp"), "-o",
+                           str(exe)])
+    out = tmp_path / "x.bin"
+    more = subprocess.check_output([str(exe), str(out)], text=True)
+    assert int(more) == 3  # the reference prints "3 more!!!" for its own scene
+    rec = np.fromfile(out, np.float32).reshape(-1, 4)
+    g = golden("ref_scene_20.npz")
+    assert np.array_equal(rec[:, :3], g["x0"])
+    assert np.array_equal(rec[:, 3], g["m0"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["stages", "fused"])
+def test_cpp_driver_matches_reference_scene(built_pkg, tmp_path, mode):
+    exe = tmp_path / "drive"
+    libdir = os.path.dirname(built_pkg.LIB_PATH)
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", INC, os.path.join(CPP, "main_reference_scene.cpp"),
+                           "-L", libdir, "-l:librd_mpm.so", f"-Wl,-rpath,{libdir}", "-o", str(exe)])
+    out = tmp_path / "state.bin"
+    subprocess.check_call([str(exe), str(out), mode])
+    rec = np.fromfile(out, np.float32).reshape(-1, 34)
+    g = golden("ref_scene_20.npz")
+    assert rel(rec[:, 0:3], g["s1_x"]) < 1e-5
+    assert rel(rec[:, 3:6], g["s1_v"]) < 1e-5
+    assert rel_floor(rec[:, 6:15], g["s1_B"], b_scale(g["s1_v"], 0.05)) < 1e-5
+    assert rel(rec[:, 15:24], g["s1_FE"]) < 1e-5
+    assert rel(rec[:, 24:33], g["s1_FP"]) < 1e-5
+    assert rel(rec[:, 33], g["vol0"]) < 1e-6
