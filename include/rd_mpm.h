@@ -35,7 +35,8 @@ typedef enum rd_status {
     RD_CUDA_ERROR = 3,       /* a CUDA runtime call failed; see rd_last_error */
     RD_DEVICE_FAULT_FLAG = 4,/* a kernel raised a status flag; see rd_get_flags */
     RD_TIMEOUT = 5,          /* a bounded device wait gave up */
-    RD_NOT_SUPPORTED = 6
+    RD_NOT_SUPPORTED = 6,
+    RD_TOO_LARGE = 7         /* beyond the fixed capacity of rd_rasterize_noalloc */
 } rd_status;
 
 enum { RD_FP32 = 0, RD_FP64 = 1 };
@@ -172,6 +173,36 @@ rd_status rd_set_kernel_timing(rd_handle* h, int enable);
 rd_status rd_kernel_timing(rd_handle* h, int kernel, uint64_t* launches, double* total_ms);
 /* Number of kernel launches issued by this handle so far. */
 rd_status rd_launch_count(rd_handle* h, uint64_t* count);
+
+/* Rasterize without allocating.  No counterpart in the reference: it exists for
+ * callers that cannot allocate GPU memory - an engine that has handed the whole
+ * device to its own pool allocator, or a real-time frame loop where
+ * cudaMalloc's device-wide synchronisation and unbounded latency (or an
+ * out-of-memory failure halfway through a frame) cannot be afforded - and
+ * therefore cannot create an rd_handle, which owns its buffers.
+ *
+ * Computes what rasterizeParticlesToGrid (material_point_method.cpp:94-129)
+ * accumulates before its velocity division: per grid node the mass sum of
+ * w m_p and the momentum sum of w m_p (v_p + B_p D^-1 (x_i - x_p)), written as
+ * float4 (m, p_x, p_y, p_z) to grid_out (max_i*max_j*max_k float4, device
+ * memory, overwritten; index i*max_j*max_k + j*max_k + k).  in holds device
+ * arrays of n = params->num_particles particles: x (n x 3), v (n x 3), mass (n)
+ * required, B (n x 9) optional (NULL = 0); other fields are ignored.  FP32 only
+ * (RD_NOT_SUPPORTED otherwise).  Work is queued on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream); the call returns without waiting.
+ *
+ * Limits: at most 65,536 particles and 262,144 grid nodes (and 4x4x4-cell
+ * blocks x 64 <= 262,144, e.g. a 64^3 grid); larger sizes return RD_TOO_LARGE
+ * before anything is queued.  The sort scratch is one fixed device array of
+ * about 2.6 MB inside this library, held by every GPU that loads it until the
+ * process exits; the call makes no device allocation of its own.  The first
+ * call on a device looks up that array's device address (once per device, with
+ * the device current); make that first call before any stream capture.  All
+ * calls share the array and it keeps the previous call's contents (the call
+ * clears what must start at zero), so calls whose work overlaps on the GPU -
+ * on different streams, or from different threads - race and must be
+ * serialised by the caller. */
+rd_status rd_rasterize_noalloc(const rd_params* params, const rd_particles* in, float* grid_out, void* stream);
 
 #ifdef __cplusplus
 }

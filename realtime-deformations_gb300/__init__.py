@@ -31,9 +31,9 @@ HEADER = os.path.join(REPO_DIR, "include", "rd_mpm.h")
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC,-ffp-contract=off", "-shared"]
 
-RD_OK, RD_INVALID_ARG, RD_OOM, RD_CUDA_ERROR, RD_DEVICE_FAULT_FLAG, RD_TIMEOUT, RD_NOT_SUPPORTED = range(7)
+RD_OK, RD_INVALID_ARG, RD_OOM, RD_CUDA_ERROR, RD_DEVICE_FAULT_FLAG, RD_TIMEOUT, RD_NOT_SUPPORTED, RD_TOO_LARGE = range(8)
 STATUS_NAMES = {0: "RD_OK", 1: "RD_INVALID_ARG", 2: "RD_OOM", 3: "RD_CUDA_ERROR",
-                4: "RD_DEVICE_FAULT_FLAG", 5: "RD_TIMEOUT", 6: "RD_NOT_SUPPORTED"}
+                4: "RD_DEVICE_FAULT_FLAG", 5: "RD_TIMEOUT", 6: "RD_NOT_SUPPORTED", 7: "RD_TOO_LARGE"}
 RD_FP32, RD_FP64 = 0, 1
 RD_HOST, RD_DEVICE = 0, 1
 RD_BC_NONE, RD_BC_STICKY = 0, 1
@@ -45,7 +45,7 @@ STAGES = {"rasterize": 0, "forces": 1, "grid_velocities": 2, "collisions": 3,
 EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "rd_get_particles",
            "rd_init_volumes", "rd_step", "rd_stage", "rd_get_grid", "rd_device_xyzs", "rd_get_flags",
            "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort",
-           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count")
+           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_rasterize_noalloc")
 KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g")
 
 
@@ -112,6 +112,7 @@ def lib():
             L.rd_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
             L.rd_debug_sort.argtypes = [vp, vp, vp, ctypes.c_int]
             L.rd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+            L.rd_rasterize_noalloc.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(_Particles), vp, vp]
             L.rd_set_kernel_timing.argtypes = [vp, ctypes.c_int]
             L.rd_kernel_timing.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64),
                                            ctypes.POINTER(ctypes.c_double)]

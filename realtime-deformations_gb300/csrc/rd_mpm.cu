@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -802,3 +803,165 @@ rd_status rd_launch_count(rd_handle* h, uint64_t* count) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free rasterize (rd_rasterize_noalloc).  The sort scratch lives in
+// one file-scope device array sized for the limits below; every GPU that loads
+// this library holds it until the process exits.
+namespace {
+
+constexpr int kNaMaxParticles = 1 << 16;  // 65,536 particles
+constexpr int kNaMaxKeys = 1 << 18;       // 262,144 cell keys (4x4x4 blocks x 64), e.g. a 64^3 grid
+constexpr int kNaMaxTiles = kNaMaxKeys / kScanTile;
+constexpr int kNaMaxWork = kNaMaxParticles / WorkP<float>::value + kNaMaxKeys / kCellsPerBlock + 2;
+
+struct NaScratch {
+    int4 work[kNaMaxWork];
+    uint32_t keys[kNaMaxParticles];
+    uint32_t perm[kNaMaxParticles];
+    uint32_t counts[kNaMaxKeys];
+    uint32_t cursor[kNaMaxKeys];
+    uint32_t tile_sums[kNaMaxTiles];
+    uint32_t nwork[2];
+    uint32_t flags;
+};
+
+// Block key and histogram of particles given as device arrays (x: n x 3).
+__global__ void __launch_bounds__(256) k_na_keys(DevParams<float> P, const float* __restrict__ x,
+                                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ counts,
+                                                 uint32_t* flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.n) return;
+    const int b[3] = {base_of(x[3 * i], P.h), base_of(x[3 * i + 1], P.h), base_of(x[3 * i + 2], P.h)};
+    if (!stencil_in_grid(P, b)) raise_flag(flags, 1u);
+    const uint32_t key = sort_key(P, b);
+    keys[i] = key;
+    count_key(counts, key);
+}
+
+// The rasterize P2G of k_p2g<float, true, false>, reading x, v, B and mass from
+// the caller's structure-of-arrays device buffers instead of particle planes.
+__global__ void __launch_bounds__(kThreads) k_na_p2g(DevParams<float> P, const float* __restrict__ x,
+                                                     const float* __restrict__ v, const float* __restrict__ B,
+                                                     const float* __restrict__ mass, const uint32_t* __restrict__ perm,
+                                                     const int4* __restrict__ work, const uint32_t* nwork,
+                                                     uint32_t work_cap, float4* __restrict__ grid, uint32_t* flags) {
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    P2GTile<float, kBlk>& S = *reinterpret_cast<P2GTile<float, kBlk>*>(smem_raw);
+    const uint32_t nw = min(*nwork, work_cap);
+    for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
+        const int4 it = work[wi];
+        for (int c = threadIdx.x; c < 4 * P2GTile<float, kBlk>::TC; c += blockDim.x) S.tile[c] = 0.f;
+        for (int c = threadIdx.x; c < P2GTile<float, kBlk>::NC; c += blockDim.x) S.cnt[c] = 0;
+        int org[3];
+        tile_origin(P, it.x, org);
+        const int count = min(it.z, min(WorkP<float>::value, P.n - it.y));
+        __syncthreads();
+        for (int j = threadIdx.x; j < count; j += blockDim.x) {
+            const uint32_t i = perm[it.y + j];
+            const float px[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+            Stencil<float> St;
+            if (!make_stencil(P, px, org, St)) {
+                raise_flag(flags, 4u);
+                S.cellof[j] = 0xff;
+                continue;
+            }
+            const float m = mass[i];
+            float A[9], mv[3];
+#pragma unroll
+            for (int e = 0; e < 9; ++e) A[e] = B ? m * (B[9 * i + e] * P.dinv) : 0.f;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) mv[a] = m * v[3 * i + a];
+            write_record<float, true>(&S.rec[j * kRecV4], St, px, A, mv, m, P.h);
+            const int cell = (St.rel[0] * kBlk + St.rel[1]) * kBlk + St.rel[2];
+            S.cellof[j] = (uint8_t)cell;
+            atomicAdd(&S.cnt[cell], 1);
+        }
+        sort_records<float, kBlk>(S, count);
+        p2g_tasks<float, true, kBlk>(S, count);
+        __syncthreads();
+        p2g_flush<float, kBlk>(P, S, org, grid);
+        __syncthreads();
+    }
+}
+
+struct NaDevice {
+    NaScratch* scratch = nullptr;
+    int sms = 0;
+    int occ = 1;
+};
+std::mutex g_na_mutex;
+NaDevice g_na[64];
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char rd_noalloc_scratch[sizeof(NaScratch)];
+
+extern "C" rd_status rd_rasterize_noalloc(const rd_params* params, const rd_particles* in, float* grid_out,
+                                          void* stream) {
+    if (!params || !in || !in->x || !in->v || !in->mass || !grid_out) return RD_INVALID_ARG;
+    const rd_params& p = *params;
+    if (p.precision != RD_FP32) return RD_NOT_SUPPORTED;
+    if (p.max_i < 8 || p.max_j < 8 || p.max_k < 8 || p.num_particles < 0 || !(p.h > 0)) return RD_INVALID_ARG;
+    const int64_t cells = (int64_t)p.max_i * p.max_j * p.max_k;
+    const int64_t nblocks = (int64_t)((p.max_i + kBlk - 1) / kBlk) * ((p.max_j + kBlk - 1) / kBlk) *
+                            ((p.max_k + kBlk - 1) / kBlk);
+    if (p.num_particles > kNaMaxParticles || cells > kNaMaxKeys || nblocks * kCellsPerBlock > kNaMaxKeys)
+        return RD_TOO_LARGE;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return RD_CUDA_ERROR;
+    NaDevice nd;
+    {
+        // once per device, with that device current: the scratch array's device
+        // address (the host-side name is only a stand-in) and the launch shape
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        if (!g_na[dev].scratch) {
+            void* ptr = nullptr;
+            if (cudaGetSymbolAddress(&ptr, rd_noalloc_scratch) != cudaSuccess || !ptr) return RD_CUDA_ERROR;
+            int sms = 0, occ = 0;
+            if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return RD_CUDA_ERROR;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_na_p2g, kThreads, sizeof(P2GTile<float, kBlk>)) !=
+                cudaSuccess)
+                return RD_CUDA_ERROR;
+            g_na[dev].sms = sms;
+            g_na[dev].occ = std::max(1, occ);
+            g_na[dev].scratch = static_cast<NaScratch*>(ptr);
+        }
+        nd = g_na[dev];
+    }
+    NaScratch* sc = nd.scratch;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    rd_handle hp;  // parameters only; owns no device memory
+    hp.prm = p;
+    hp.n = p.num_particles;
+    hp.NB[0] = (p.max_i + kBlk - 1) / kBlk;
+    hp.NB[1] = (p.max_j + kBlk - 1) / kBlk;
+    hp.NB[2] = (p.max_k + kBlk - 1) / kBlk;
+    hp.nblocks = (int)nblocks;
+    hp.nkeys = (int)nblocks * kCellsPerBlock;
+    DevParams<float> P = make_params<float>(&hp, 0.0, 0.0f);
+    const int n = p.num_particles;
+    // the scratch keeps the previous call's contents: clear what must start at zero
+    if (cudaMemsetAsync(grid_out, 0, (size_t)cells * sizeof(float4), st) != cudaSuccess ||
+        cudaMemsetAsync(sc->counts, 0, (size_t)hp.nkeys * sizeof(uint32_t), st) != cudaSuccess ||
+        cudaMemsetAsync(sc->nwork, 0, 2 * sizeof(uint32_t) + sizeof(uint32_t), st) != cudaSuccess)
+        return RD_CUDA_ERROR;
+    if (n > 0) {
+        const int ntiles = (hp.nkeys + kScanTile - 1) / kScanTile;
+        const uint32_t work_cap = (uint32_t)kNaMaxWork;
+        k_na_keys<<<blocks_for(n, 256), 256, 0, st>>>(P, static_cast<const float*>(in->x), sc->keys, sc->counts,
+                                                      &sc->flags);
+        k_tile_sums<<<ntiles, 256, 0, st>>>(sc->counts, hp.nkeys, sc->tile_sums);
+        k_scan<<<ntiles, kScanThreads, 0, st>>>(sc->counts, sc->cursor, sc->tile_sums, hp.nkeys, sc->work, &sc->nwork[0],
+                                                &sc->nwork[1], (uint32_t)n, work_cap, (uint32_t)WorkP<float>::value,
+                                                &sc->flags);
+        k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(n, sc->keys, sc->cursor, sc->perm);
+        const size_t max_items = (size_t)n / WorkP<float>::value + (size_t)std::min<int64_t>(nblocks, n) + 1;
+        const unsigned grid = (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)nd.sms * nd.occ));
+        k_na_p2g<<<grid, kThreads, sizeof(P2GTile<float, kBlk>), st>>>(
+            P, static_cast<const float*>(in->x), static_cast<const float*>(in->v), static_cast<const float*>(in->B),
+            static_cast<const float*>(in->mass), sc->perm, sc->work, &sc->nwork[0], work_cap,
+            reinterpret_cast<float4*>(grid_out), &sc->flags);
+    }
+    return cudaGetLastError() == cudaSuccess ? RD_OK : RD_CUDA_ERROR;
+}
