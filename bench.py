@@ -158,8 +158,23 @@ def measured_peak_hbm():
 
 
 def make_scene(name, seed):
+    graft.load_package()  # also in spawned worker processes
     from rd_gb300 import scenes
     return scenes.SCENES[name](seed=seed)
+
+
+def captured_traffic(kernel, workload, particles):
+    """DRAM bytes per launch of `kernel` from the ncu record in profiles/traffic.txt,
+    scaled by particle count to this workload, or None."""
+    path = os.path.join(REPO, "profiles", "traffic.txt")
+    try:
+        for line in open(path):
+            f = line.split()
+            if len(f) >= 5 and not line.startswith("#") and f[0] == kernel and f[1] == workload:
+                return (int(f[3]) + int(f[4])) * particles / int(f[2])
+    except OSError:
+        pass
+    return None
 
 
 def cpu_baseline_single_core(sc, seconds_hint=20.0):
@@ -283,7 +298,8 @@ def run_ours(args):
                 "path": "rd_set_particles(host) + rd_step + rd_get_particles(host), pinned buffers"},
         "roofline": {"bound": "hbm", "kernel": {"p2g": "k_p2g", "g2p2g": "k_g2p2g"}[dom],
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "traffic": None,
+                     "peak_source": peak_src,
+                     "traffic": captured_traffic({"p2g": "k_p2g", "g2p2g": "k_g2p2g"}[dom], sc.name, sc.n),
                      "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": avg_s * 1e6},
         "step_roofline": {"achieved": step_bytes / (step_ms / 1e3) / 1e9, "unit": "GB/s",
                           "frac": step_bytes / (step_ms / 1e3) / 1e9 / peak,
