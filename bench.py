@@ -62,6 +62,8 @@ def parse_args():
     ap.add_argument("--workload", default="two_balls_1m")
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-baseline", type=int, default=1, help="time the single-core CPU baseline (rank 0, N=1)")
+    ap.add_argument("--batch-steps", type=int, default=300,
+                    help="timed steps of the batched-forward workload (64 uneven scenes); 0 skips it")
     return ap.parse_args()
 
 
@@ -197,6 +199,49 @@ def cpu_baseline_single_core(sc, seconds_hint=20.0):
     return sc.n / dt, kind, f"1 step of all {sc.n} particles after init, single thread ({dt:.1f} s)"
 
 
+def measure_batched(pkg, local, steps, warmup, plain_value):
+    """Batched forward: the 64 uneven snowballs in one handle (one sort and one
+    fused kernel per step for all scenes), autotuned, CUDA-graph replay; CUDA
+    events on the handle's stream around `steps` steps after `warmup`."""
+    import torch
+    graft.load_package()
+    from rd_gb300 import scenes
+    batch = scenes.uneven_snowballs(seed=0)
+    b = pkg.Batch([pkg.make_params(*s.grid, s.n, s.h, device=local, **s.params()) for s in batch])
+    dt = batch[0].dt
+
+    def reset():
+        for i, s in enumerate(batch):
+            b.set_particles(i, s.x, s.v, s.mass)
+        b.init_volumes()
+
+    reset()
+    tune = b.autotune(dt, steps=5)
+    reset()
+    b.step(dt, warmup)
+    stream = torch.cuda.ExternalStream(b.stream(), device=local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b.synchronize()
+    l0 = b.launch_count()
+    e0.record(stream)
+    b.step(dt, steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = b.launch_count() - l0
+    flags = b.flags()
+    b.close()
+    value = b.n * steps / (ms / 1e3)
+    return {"value": value, "unit": "particle-steps/s", "vs_plain_forward": value / plain_value,
+            "steps": steps, "warmup": warmup, "ms_per_step": ms / steps, "gpu_launches": launches,
+            "scenes": len(batch), "particles": b.n, "grid_nodes": int(sum(np.prod(s.grid) for s in batch)),
+            "particles_range": [min(s.n for s in batch), max(s.n for s in batch)],
+            "grid_range": [min(s.grid[0] for s in batch), max(s.grid[0] for s in batch)],
+            "tuning": tune, "graphs": True, "flags": flags,
+            "workload": "uneven_snowballs (seed 0): log-uniform 4k-262k particles, 32^3-128^3 grids, "
+                        "E ~ U[5e4,3e5], nu ~ U[0.15,0.3], v0 ~ N(0,1)^3"}
+
+
 def run_ours(args):
     import torch
 
@@ -308,6 +353,8 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
+    if args.batch_steps > 0:
+        out["batched_forward"] = measure_batched(pkg, local, args.batch_steps, max(args.warmup, 3), value)
     if rank == 0 and ws == 1 and args.cpu_baseline:
         v, kind, sample = cpu_baseline_single_core(sc)
         out["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": kind, "sample": sample}

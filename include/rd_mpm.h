@@ -36,7 +36,7 @@ typedef enum rd_status {
     RD_DEVICE_FAULT_FLAG = 4,/* a kernel raised a status flag; see rd_get_flags */
     RD_TIMEOUT = 5,          /* a bounded device wait gave up */
     RD_NOT_SUPPORTED = 6,
-    RD_TOO_LARGE = 7         /* beyond the fixed capacity of rd_rasterize_noalloc */
+    RD_TOO_LARGE = 7         /* beyond a fixed capacity (rd_rasterize_noalloc; index ranges) */
 } rd_status;
 
 enum { RD_FP32 = 0, RD_FP64 = 1 };
@@ -173,6 +173,52 @@ rd_status rd_set_kernel_timing(rd_handle* h, int enable);
 rd_status rd_kernel_timing(rd_handle* h, int kernel, uint64_t* launches, double* total_ms);
 /* Number of kernel launches issued by this handle so far. */
 rd_status rd_launch_count(rd_handle* h, uint64_t* count);
+
+/* ---- Batches: many independent scenes stepped together ----
+ * No counterpart in the reference, which simulates one LagrangeEulerView per
+ * process.  scenes[s] describes scene s exactly as rd_create's params do (its
+ * own grid size, cell size, material, gravity, walls and particle count);
+ * precision, device, lagged_b and track_fp must agree across scenes and
+ * track_fp must be 0 (RD_NOT_SUPPORTED otherwise).  Each step sorts all
+ * scenes' particles once and runs one fused kernel over a work list of
+ * (scene, block) items; each item reads its scene's parameters.  rd_step,
+ * rd_init_volumes, rd_autotune, rd_get_flags, rd_synchronize and
+ * rd_device_xyzs act on the whole batch (the xyzs of scene s's particle i
+ * are entry first_s + i, first_s = the particle counts of scenes 0..s-1
+ * summed); rd_stage, rd_set_particles, rd_get_particles and rd_get_grid are
+ * single-scene calls and return RD_NOT_SUPPORTED / RD_INVALID_ARG on a batch.
+ * Every scene needs its particles set before rd_init_volumes and rd_step. */
+rd_status rd_batch_create(const rd_params* scenes, int32_t nscenes, rd_handle** out);
+rd_status rd_batch_num_scenes(rd_handle* h, int32_t* nscenes);
+/* rd_set_particles / rd_get_particles / rd_get_grid (mass and velocity) of one scene. */
+rd_status rd_batch_set_particles(rd_handle* h, int32_t scene, const rd_particles* in, int where);
+rd_status rd_batch_get_particles(rd_handle* h, int32_t scene, rd_particles* out, int where);
+rd_status rd_batch_get_grid(rd_handle* h, int32_t scene, void* mass, void* velocity, int where);
+/* Same as rd_step. */
+rd_status rd_batch_step(rd_handle* h, double dt, int32_t nsteps);
+
+/* CUDA graphs, on by default: within one rd_step call, once the step is steady
+ * (positions counted, grid built for this dt), each pair of steps is replayed
+ * as one captured graph (scan, scatter, grid clear and the fused kernel, twice)
+ * instead of individual launches.  Results are those of the launches. */
+rd_status rd_set_graphs(rd_handle* h, int enable);
+
+/* Autotuner: times `steps` steps of the current state (from the same saved
+ * state each time) for each work-item size (FP32: 128, 192, 256 particles;
+ * FP64: 64, 96, 128) and each persistent grid of 1 .. max resident CTAs per
+ * SM of the fused kernel, keeps the fastest and restores the state (the next
+ * step re-sorts and rebuilds the grid).  Allocates a copy of the particle
+ * state for its duration. */
+typedef struct rd_tune_result {
+    int32_t particles_per_item; /* chosen work-item size */
+    int32_t ctas_per_sm;        /* chosen persistent CTAs per SM */
+    double ms_per_step;         /* measured for the chosen pair */
+    int32_t trials;             /* pairs timed */
+} rd_tune_result;
+rd_status rd_autotune(rd_handle* h, double dt, int32_t steps, rd_tune_result* result);
+/* Sets the pair by hand (0 = default: the largest item, max resident CTAs). */
+rd_status rd_set_tuning(rd_handle* h, int32_t particles_per_item, int32_t ctas_per_sm);
+rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas_per_sm);
 
 /* Rasterize without allocating.  No counterpart in the reference: it exists for
  * callers that cannot allocate GPU memory - an engine that has handed the whole

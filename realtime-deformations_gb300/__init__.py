@@ -45,7 +45,10 @@ STAGES = {"rasterize": 0, "forces": 1, "grid_velocities": 2, "collisions": 3,
 EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "rd_get_particles",
            "rd_init_volumes", "rd_step", "rd_stage", "rd_get_grid", "rd_device_xyzs", "rd_get_flags",
            "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort",
-           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_rasterize_noalloc")
+           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_batch_create",
+           "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
+           "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
+           "rd_rasterize_noalloc")
 KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g")
 
 
@@ -85,6 +88,11 @@ _LIB = None
 _LIB_LOCK = threading.Lock()
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("particles_per_item", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+                ("ms_per_step", ctypes.c_double), ("trials", ctypes.c_int32)]
+
+
 def lib():
     """The loaded CUDA library; raises if it has not been built."""
     global _LIB
@@ -113,6 +121,16 @@ def lib():
             L.rd_debug_sort.argtypes = [vp, vp, vp, ctypes.c_int]
             L.rd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
             L.rd_rasterize_noalloc.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(_Particles), vp, vp]
+            L.rd_batch_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int32, ctypes.POINTER(vp)]
+            L.rd_batch_num_scenes.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
+            L.rd_batch_set_particles.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(_Particles), ctypes.c_int]
+            L.rd_batch_get_particles.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(_Particles), ctypes.c_int]
+            L.rd_batch_get_grid.argtypes = [vp, ctypes.c_int32, vp, vp, ctypes.c_int]
+            L.rd_batch_step.argtypes = [vp, ctypes.c_double, ctypes.c_int32]
+            L.rd_set_graphs.argtypes = [vp, ctypes.c_int]
+            L.rd_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(TuneResult)]
+            L.rd_set_tuning.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
+            L.rd_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
             L.rd_set_kernel_timing.argtypes = [vp, ctypes.c_int]
             L.rd_kernel_timing.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64),
                                            ctypes.POINTER(ctypes.c_double)]
@@ -192,23 +210,14 @@ class Simulation:
             return None
         return np.ascontiguousarray(np.asarray(a, self.dtype).reshape(shape))
 
-    def set_particles(self, x, v, mass, B=None, FE=None, FP=None, Jp=None, volume=None, sync=True):
-        """Copies host arrays in (rd_set_particles).  With sync=False the call
-        returns once the copies are queued; the arrays must stay alive and
-        unchanged until the handle's stream reaches them."""
-        n = self.n
+    def _particles_in(self, n, x, v, mass, B, FE, FP, Jp, volume):
         arrs = {"x": self._arr(x, (n, 3)), "v": self._arr(v, (n, 3)), "B": self._arr(B, (n, 9)),
                 "FE": self._arr(FE, (n, 9)), "FP": self._arr(FP, (n, 9)), "Jp": self._arr(Jp, (n,)),
                 "mass": self._arr(mass, (n,)), "volume": self._arr(volume, (n,))}
         ps = _Particles(**{k: (a.ctypes.data if a is not None else None) for k, a in arrs.items()})
-        self._check(lib().rd_set_particles(self._h, ctypes.byref(ps), RD_HOST), "rd_set_particles")
-        if sync:
-            self._check(lib().rd_synchronize(self._h), "rd_synchronize")
+        return ps, arrs
 
-    def get_particles(self, fields=("x", "v", "B", "FE", "FP", "Jp", "mass", "volume"), out=None):
-        """Copies the particle state out in the original particle order
-        (rd_get_particles).  ``out`` may supply the destination arrays."""
-        n = self.n
+    def _particles_out(self, n, fields, out):
         shapes = {"x": (n, 3), "v": (n, 3), "B": (n, 9), "FE": (n, 9), "FP": (n, 9), "Jp": (n,),
                   "mass": (n,), "volume": (n,)}
         if out is None:
@@ -218,6 +227,21 @@ class Simulation:
             if a.shape != shapes[k] or a.dtype != self.dtype or not a.flags.c_contiguous:
                 raise ValueError(f"out[{k!r}] must be a contiguous {self.dtype.__name__} array of shape {shapes[k]}")
         ps = _Particles(**{k: (out[k].ctypes.data if k in fields else None) for k in shapes})
+        return ps, out
+
+    def set_particles(self, x, v, mass, B=None, FE=None, FP=None, Jp=None, volume=None, sync=True):
+        """Copies host arrays in (rd_set_particles).  With sync=False the call
+        returns once the copies are queued; the arrays must stay alive and
+        unchanged until the handle's stream reaches them."""
+        ps, self._pending = self._particles_in(self.n, x, v, mass, B, FE, FP, Jp, volume)
+        self._check(lib().rd_set_particles(self._h, ctypes.byref(ps), RD_HOST), "rd_set_particles")
+        if sync:
+            self._check(lib().rd_synchronize(self._h), "rd_synchronize")
+
+    def get_particles(self, fields=("x", "v", "B", "FE", "FP", "Jp", "mass", "volume"), out=None):
+        """Copies the particle state out in the original particle order
+        (rd_get_particles).  ``out`` may supply the destination arrays."""
+        ps, out = self._particles_out(self.n, fields, out)
         self._check(lib().rd_get_particles(self._h, ctypes.byref(ps), RD_HOST), "rd_get_particles")
         return out
 
@@ -287,6 +311,72 @@ class Simulation:
         c = ctypes.c_uint64()
         self._check(lib().rd_launch_count(self._h, ctypes.byref(c)), "rd_launch_count")
         return c.value
+
+    def set_graphs(self, enable: bool):
+        self._check(lib().rd_set_graphs(self._h, int(enable)), "rd_set_graphs")
+
+    def autotune(self, dt: float, steps: int = 10) -> dict:
+        """rd_autotune: picks the work-item size and CTAs per SM by timing."""
+        r = TuneResult()
+        self._check(lib().rd_autotune(self._h, float(dt), int(steps), ctypes.byref(r)), "rd_autotune")
+        return {"particles_per_item": r.particles_per_item, "ctas_per_sm": r.ctas_per_sm,
+                "ms_per_step": r.ms_per_step, "trials": r.trials}
+
+    def set_tuning(self, particles_per_item: int = 0, ctas_per_sm: int = 0):
+        self._check(lib().rd_set_tuning(self._h, int(particles_per_item), int(ctas_per_sm)), "rd_set_tuning")
+
+    def tuning(self):
+        a, b = ctypes.c_int32(), ctypes.c_int32()
+        self._check(lib().rd_get_tuning(self._h, ctypes.byref(a), ctypes.byref(b)), "rd_get_tuning")
+        return a.value, b.value
+
+
+class Batch(Simulation):
+    """Several independent scenes in one handle (rd_batch_create): one sort and
+    one fused kernel per step for all of them.  Scene s is described by its own
+    ``Params``; its particles are set and read per scene."""
+
+    def __init__(self, scenes):
+        scenes = list(scenes)
+        if not scenes:
+            raise ValueError("a batch needs at least one scene")
+        self.scene_params = scenes
+        self.params = scenes[0]
+        self.counts = [p.num_particles for p in scenes]
+        self.offsets = [int(o) for o in np.cumsum([0] + self.counts)[:-1]]
+        self.n = int(sum(self.counts))
+        self.dtype = np.float64 if scenes[0].precision == RD_FP64 else np.float32
+        self._h = ctypes.c_void_p()
+        arr = (Params * len(scenes))(*scenes)
+        s = lib().rd_batch_create(arr, len(scenes), ctypes.byref(self._h))
+        if s != RD_OK:
+            raise RDError(s, "rd_batch_create failed")
+
+    @property
+    def nscenes(self) -> int:
+        return len(self.scene_params)
+
+    def set_particles(self, scene, x, v, mass, B=None, FE=None, FP=None, Jp=None, volume=None, sync=True):
+        ps, self._pending = self._particles_in(self.counts[scene], x, v, mass, B, FE, FP, Jp, volume)
+        self._check(lib().rd_batch_set_particles(self._h, int(scene), ctypes.byref(ps), RD_HOST),
+                    "rd_batch_set_particles")
+        if sync:
+            self._check(lib().rd_synchronize(self._h), "rd_synchronize")
+
+    def get_particles(self, scene, fields=("x", "v", "B", "FE", "FP", "Jp", "mass", "volume"), out=None):
+        ps, out = self._particles_out(self.counts[scene], fields, out)
+        self._check(lib().rd_batch_get_particles(self._h, int(scene), ctypes.byref(ps), RD_HOST),
+                    "rd_batch_get_particles")
+        return out
+
+    def get_grid(self, scene):
+        p = self.scene_params[scene]
+        nc = p.max_i * p.max_j * p.max_k
+        m = np.zeros(nc, self.dtype)
+        v = np.zeros((nc, 3), self.dtype)
+        self._check(lib().rd_batch_get_grid(self._h, int(scene), m.ctypes.data, v.ctypes.data, RD_HOST),
+                    "rd_batch_get_grid")
+        return {"mass": m, "vel": v}
 
 
 class LagrangeEulerView:

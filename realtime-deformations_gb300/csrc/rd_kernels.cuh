@@ -30,6 +30,10 @@ template <typename T> struct DevParams {
     T fscale;      // force scale in P2G: dt when fused with the momentum, 1 alone
     int bc, bc_width;
     int lagged;
+    // Place of this scene in a batch (zero for a single scene): its first
+    // 4x4x4 block among all scenes' blocks, and its first grid node.
+    uint32_t block_base;
+    unsigned long long goff;
 };
 
 struct DevBufs {
@@ -45,7 +49,33 @@ struct DevBufs {
     void* grid_next;   // vec4 per cell: P2G of the next step (fused kernel)
     void* gforce;      // vec4 per cell (stage mode forces)
     uint32_t* flags;
+    // batches: DevParams<T> per scene, first block and first particle of each
+    // scene (nscenes + 1 entries, ascending)
+    const void* scenes;
+    const uint32_t* sblock;
+    const uint32_t* spoff;
+    int nscenes;
 };
+
+// The scene holding item v of a batch: the last s with starts[s] <= v.
+__device__ __forceinline__ int scene_of(const uint32_t* __restrict__ starts, int nscenes, uint32_t v) {
+    int lo = 0, hi = nscenes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(starts + mid) <= v) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Copies scene s's parameters into shared memory (all threads; the caller
+// synchronises before use).
+template <typename T>
+__device__ __forceinline__ void copy_scene(DevParams<T>& dst, const void* table, int s) {
+    static_assert(sizeof(DevParams<T>) % 4 == 0, "DevParams is copied as words");
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(static_cast<const DevParams<T>*>(table) + s);
+    uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(DevParams<T>) / 4); k += blockDim.x) d[k] = __ldg(src + k);
+}
 
 __device__ __forceinline__ void raise_flag(uint32_t* flags, uint32_t f) {
     if ((__ldcg(flags) & f) == 0) atomicOr(flags, f);
@@ -65,7 +95,7 @@ __device__ __forceinline__ uint32_t sort_key(const DevParams<T>& P, const int b[
         k[a] = v / kBlk;
         c[a] = v - k[a] * kBlk;
     }
-    const uint32_t blk = ((uint32_t)k[0] * P.NB[1] + k[1]) * P.NB[2] + k[2];
+    const uint32_t blk = P.block_base + ((uint32_t)k[0] * P.NB[1] + k[1]) * P.NB[2] + k[2];
     return blk * kCellsPerBlock + (uint32_t)((c[0] * kBlk + c[1]) * kBlk + c[2]);
 }
 
@@ -82,12 +112,16 @@ __device__ __forceinline__ void count_key(uint32_t* counts, uint32_t key) {
 }
 
 // ---------------------------------------------------------------- sorting
-template <typename T>
-__global__ void __launch_bounds__(256) k_keys(DevParams<T> P, const vec4<T>* __restrict__ pl,
-                                              uint32_t* __restrict__ keys, uint32_t* __restrict__ counts,
-                                              uint32_t* flags) {
+template <typename T, bool BATCH>
+__global__ void __launch_bounds__(256) k_keys(DevParams<T> P0, DevBufs D, const vec4<T>* __restrict__ pl,
+                                              uint32_t* __restrict__ keys) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    if (i >= P0.n) return;
+    uint32_t* counts = D.counts;
+    uint32_t* flags = D.flags;
+    DevParams<T> P;
+    if (BATCH) P = static_cast<const DevParams<T>*>(D.scenes)[scene_of(D.spoff, D.nscenes, (uint32_t)i)];
+    else P = P0;
     const vec4<T> x = ld_stream(pl + i);
     const int b[3] = {base_of(x.x, P.h), base_of(x.y, P.h), base_of(x.z, P.h)};
     if (!stencil_in_grid(P, b)) raise_flag(flags, 1u);
@@ -149,7 +183,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
                                                        const uint32_t* __restrict__ tile_sums, int nkeys,
                                                        int4* __restrict__ work, uint32_t* __restrict__ nwork,
                                                        uint32_t* __restrict__ nwork_next_sort, uint32_t n_expected,
-                                                       uint32_t work_cap, uint32_t wp, uint32_t* flags) {
+                                                       uint32_t work_cap, uint32_t wp, uint32_t* flags,
+                                                       const uint32_t* __restrict__ sblock, int nscenes) {
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_blk[kBlocksPerTile];  // particles per block of this tile
     __shared__ uint32_t s_off;
@@ -205,11 +240,13 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
         const uint32_t bc = s_blk[b];
         const uint32_t ni = (bc + wp - 1) / wp;
         if (ni) {
+            const uint32_t blk = (uint32_t)(t * kBlocksPerTile + b);
+            const int scene = nscenes > 1 ? scene_of(sblock, nscenes, blk) : 0;
             uint32_t oi = atomicAdd(nwork, ni);
             uint32_t st = st0;
             for (uint32_t j = 0; j < ni; ++j, ++oi) {
                 const uint32_t cnt = bc / ni + (j < bc % ni ? 1u : 0u);
-                if (oi < work_cap) work[oi] = make_int4(t * kBlocksPerTile + b, (int)st, (int)cnt, 0);
+                if (oi < work_cap) work[oi] = make_int4((int)blk, (int)st, (int)cnt, scene);
                 else atomicOr(flags, 4u);
                 st += cnt;
             }
@@ -401,7 +438,8 @@ __device__ __forceinline__ bool wall_node(const DevParams<T>& P, int i, int j, i
 }
 
 template <typename T>
-__device__ __forceinline__ void tile_origin(const DevParams<T>& P, int key, int org[3]) {
+__device__ __forceinline__ void tile_origin(const DevParams<T>& P, int gkey, int org[3]) {
+    const int key = gkey - (int)P.block_base;
     const int bz = key % P.NB[2];
     const int by = (key / P.NB[2]) % P.NB[1];
     const int bx = key / (P.NB[1] * P.NB[2]);
@@ -619,60 +657,80 @@ __device__ void p2g_direct(const DevParams<T>& P, const vec4<T>* r, const int b[
             }
 }
 
+// One work item of k_p2g; P is the item's scene.
 template <typename T, bool MOM, bool FORCE>
-__global__ void __launch_bounds__(kThreads) k_p2g(DevParams<T> P, DevBufs D) {
-    extern __shared__ __align__(32) unsigned char smem_raw[];
-    P2GTile<T, kBlk>& S = *reinterpret_cast<P2GTile<T, kBlk>*>(smem_raw);
+__device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D, P2GTile<T, kBlk>& S,
+                                         const int4 it) {
     const vec4<T>* __restrict__ pl = static_cast<const vec4<T>*>(D.pin);
-    vec4<T>* __restrict__ grid = static_cast<vec4<T>*>(MOM ? D.grid : D.gforce);
-    const uint32_t nw = min(*D.nwork, D.work_cap);
+    vec4<T>* __restrict__ grid = static_cast<vec4<T>*>(MOM ? D.grid : D.gforce) + P.goff;
     const size_t n = (size_t)P.n;
+    for (int c = threadIdx.x; c < 4 * P2GTile<T, kBlk>::TC; c += blockDim.x) S.tile[c] = T(0);
+    for (int c = threadIdx.x; c < P2GTile<T, kBlk>::NC; c += blockDim.x) S.cnt[c] = 0;
+    int org[3];
+    tile_origin(P, it.x, org);
+    const int count = min(it.z, min(WorkP<T>::value, P.n - it.y));
+    __syncthreads();
+    // phase 1: a record per particle
+    for (int j = threadIdx.x; j < count; j += blockDim.x) {
+        Particle<T> p;
+        load_particle(pl, n, D.perm[it.y + j], p);
+        Stencil<T> St;
+        if (!make_stencil(P, p.x, org, St)) {
+            raise_flag(D.flags, 4u);
+            S.cellof[j] = 0xff;
+            continue;
+        }
+        if (!stencil_in_grid(P, St.b)) raise_flag(D.flags, 1u);
+        T A[9];
+        T mv[3] = {T(0), T(0), T(0)};
+#pragma unroll
+        for (int e = 0; e < 9; ++e) A[e] = T(0);
+        if (MOM) {
+#pragma unroll
+            for (int e = 0; e < 9; ++e) A[e] = p.m * (p.B[e] * P.dinv);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) mv[a] = p.m * p.v[a];
+        }
+        if (FORCE) {
+            T G[9];
+            stress_PFt(P, p.F, p.Jp, G);
+            const T sc = P.fscale * (p.vol * P.dinv);
+#pragma unroll
+            for (int e = 0; e < 9; ++e) A[e] -= sc * G[e];
+        }
+        write_record<T, MOM>(&S.rec[j * kRecV4], St, p.x, A, mv, p.m, P.h);
+        const int cell = (St.rel[0] * kBlk + St.rel[1]) * kBlk + St.rel[2];
+        S.cellof[j] = (uint8_t)cell;
+        atomicAdd(&S.cnt[cell], 1);
+    }
+    sort_records<T, kBlk>(S, count);
+    p2g_tasks<T, MOM, kBlk>(S, count);
+    __syncthreads();
+    p2g_flush<T, kBlk>(P, S, org, grid);
+    __syncthreads();
+}
+
+template <typename T> struct P2GShared {
+    P2GTile<T, kBlk> t;
+    DevParams<T> par;  // the item's scene (batches)
+};
+
+// BATCH: the work items belong to different scenes (D.scenes); otherwise all
+// to the scene P0.
+template <typename T, bool MOM, bool FORCE, bool BATCH>
+__global__ void __launch_bounds__(kThreads) k_p2g(DevParams<T> P0, DevBufs D) {
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    P2GShared<T>& S = *reinterpret_cast<P2GShared<T>*>(smem_raw);
+    const uint32_t nw = min(*D.nwork, D.work_cap);
     for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
         const int4 it = D.work[wi];
-        for (int c = threadIdx.x; c < 4 * P2GTile<T, kBlk>::TC; c += blockDim.x) S.tile[c] = T(0);
-        for (int c = threadIdx.x; c < P2GTile<T, kBlk>::NC; c += blockDim.x) S.cnt[c] = 0;
-        int org[3];
-        tile_origin(P, it.x, org);
-        const int count = min(it.z, min(WorkP<T>::value, P.n - it.y));
-        __syncthreads();
-        // phase 1: a record per particle
-        for (int j = threadIdx.x; j < count; j += blockDim.x) {
-            Particle<T> p;
-            load_particle(pl, n, D.perm[it.y + j], p);
-            Stencil<T> St;
-            if (!make_stencil(P, p.x, org, St)) {
-                raise_flag(D.flags, 4u);
-                S.cellof[j] = 0xff;
-                continue;
-            }
-            if (!stencil_in_grid(P, St.b)) raise_flag(D.flags, 1u);
-            T A[9];
-            T mv[3] = {T(0), T(0), T(0)};
-#pragma unroll
-            for (int e = 0; e < 9; ++e) A[e] = T(0);
-            if (MOM) {
-#pragma unroll
-                for (int e = 0; e < 9; ++e) A[e] = p.m * (p.B[e] * P.dinv);
-#pragma unroll
-                for (int a = 0; a < 3; ++a) mv[a] = p.m * p.v[a];
-            }
-            if (FORCE) {
-                T G[9];
-                stress_PFt(P, p.F, p.Jp, G);
-                const T sc = P.fscale * (p.vol * P.dinv);
-#pragma unroll
-                for (int e = 0; e < 9; ++e) A[e] -= sc * G[e];
-            }
-            write_record<T, MOM>(&S.rec[j * kRecV4], St, p.x, A, mv, p.m, P.h);
-            const int cell = (St.rel[0] * kBlk + St.rel[1]) * kBlk + St.rel[2];
-            S.cellof[j] = (uint8_t)cell;
-            atomicAdd(&S.cnt[cell], 1);
+        if constexpr (BATCH) {
+            copy_scene(S.par, D.scenes, it.w);
+            __syncthreads();
+            p2g_item<T, MOM, FORCE>(S.par, D, S.t, it);
+        } else {
+            p2g_item<T, MOM, FORCE>(P0, D, S.t, it);
         }
-        sort_records<T, kBlk>(S, count);
-        p2g_tasks<T, MOM, kBlk>(S, count);
-        __syncthreads();
-        p2g_flush<T, kBlk>(P, S, org, grid);
-        __syncthreads();
     }
 }
 
@@ -703,6 +761,7 @@ static_assert(WorkP<float>::value <= kFusedThreads && WorkP<double>::value <= kF
 template <typename T> struct FusedShared {
     vec4<T> gv[kTileCells];  // grid velocity of this step, (vx, vy, vz, 0)
     P2GTile<T, kBlk + 2> p;
+    DevParams<T> par;        // the item's scene (batches)
 };
 
 // G2P of one particle from the velocity tile (updateParticleVelocities,
@@ -751,19 +810,17 @@ __device__ __forceinline__ void g2p_gather(const vec4<T>* __restrict__ gv, const
     }
 }
 
+// One work item of k_g2p2g; P is the item's scene.
 template <typename T, bool TRACK_FP>
-__global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlocks : 1) k_g2p2g(DevParams<T> P, DevBufs D) {
-    extern __shared__ __align__(32) unsigned char smem_raw[];
-    FusedShared<T>& S = *reinterpret_cast<FusedShared<T>*>(smem_raw);
+__device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
+                                           const int4 it) {
     constexpr int CA = kBlk + 2;
     const vec4<T>* __restrict__ pin = static_cast<const vec4<T>*>(D.pin);
     vec4<T>* __restrict__ pout = static_cast<vec4<T>*>(D.pout);
-    const vec4<T>* __restrict__ grid = static_cast<const vec4<T>*>(D.grid);
-    vec4<T>* __restrict__ gnext = static_cast<vec4<T>*>(D.grid_next);
-    const uint32_t nw = min(*D.nwork, D.work_cap);
+    const vec4<T>* __restrict__ grid = static_cast<const vec4<T>*>(D.grid) + P.goff;
+    vec4<T>* __restrict__ gnext = static_cast<vec4<T>*>(D.grid_next) + P.goff;
     const size_t n = (size_t)P.n;
-    for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
-        const int4 it = D.work[wi];
+    {
         int org[3];
         tile_origin(P, it.x, org);
         const int porg[3] = {org[0] - 1, org[1] - 1, org[2] - 1};
@@ -854,6 +911,26 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
         __syncthreads();
         p2g_flush<T, CA>(P, S.p, porg, gnext);
         __syncthreads();
+    }
+}
+
+// BATCH: the work items belong to different scenes (D.scenes); otherwise all
+// to the scene P0.
+template <typename T, bool TRACK_FP, bool BATCH>
+__global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlocks : 1)
+    k_g2p2g(DevParams<T> P0, DevBufs D) {
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    FusedShared<T>& S = *reinterpret_cast<FusedShared<T>*>(smem_raw);
+    const uint32_t nw = min(*D.nwork, D.work_cap);
+    for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
+        const int4 it = D.work[wi];
+        if constexpr (BATCH) {
+            copy_scene(S.par, D.scenes, it.w);
+            __syncthreads();
+            g2p2g_item<T, TRACK_FP>(S.par, D, S, it);
+        } else {
+            g2p2g_item<T, TRACK_FP>(P0, D, S, it);
+        }
     }
 }
 
@@ -983,11 +1060,15 @@ __global__ void k_advect(DevParams<T> P, vec4<T>* __restrict__ pl) {
 
 // computeParticleVolumesAndDensities (material_point_method.cpp:131-142):
 // rho_p = sum m_i w_ip / h^3, V_p = m_p / rho_p (0 where rho_p = 0).
-template <typename T>
-__global__ void k_volumes(DevParams<T> P, vec4<T>* __restrict__ pl, const vec4<T>* __restrict__ grid,
-                          uint32_t* flags) {
+template <typename T, bool BATCH>
+__global__ void k_volumes(DevParams<T> P0, DevBufs D, vec4<T>* __restrict__ pl, const vec4<T>* __restrict__ grid0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    if (i >= P0.n) return;
+    uint32_t* flags = D.flags;
+    DevParams<T> P;
+    if (BATCH) P = static_cast<const DevParams<T>*>(D.scenes)[scene_of(D.spoff, D.nscenes, (uint32_t)i)];
+    else P = P0;
+    const vec4<T>* __restrict__ grid = grid0 + P.goff;
     const vec4<T> x4 = pl[i];
     const T x[3] = {x4.x, x4.y, x4.z};
     int b[3];

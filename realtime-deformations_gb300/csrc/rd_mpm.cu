@@ -21,8 +21,10 @@ namespace {
 
 enum GridMode { GRID_NONE = 0, GRID_FUSED = 1, GRID_MV = 2, GRID_V = 3 };
 
+// Particles off .. off + n - 1 of planes holding ntot particles (one scene of
+// a batch, or all of a single scene), from structure-of-arrays input.
 template <typename T>
-__global__ void k_pack(int n, const T* __restrict__ x, const T* __restrict__ v, const T* __restrict__ B,
+__global__ void k_pack(int n, int off, int ntot, const T* __restrict__ x, const T* __restrict__ v, const T* __restrict__ B,
                        const T* __restrict__ FE, const T* __restrict__ FP, const T* __restrict__ Jp,
                        const T* __restrict__ mass, const T* __restrict__ vol, vec4<T>* __restrict__ pl,
                        int track_fp) {
@@ -41,20 +43,20 @@ __global__ void k_pack(int n, const T* __restrict__ x, const T* __restrict__ v, 
         P[e] = FP ? FP[9 * i + e] : ((e % 4 == 0) ? T(1) : T(0));
     }
     p.Jp = Jp ? Jp[i] : (FP ? det3(P) : T(1));
-    p.id = (uint32_t)i;
-    store_particle(pl, (size_t)n, (size_t)i, p);
-    if (track_fp) store_fp(pl, (size_t)n, (size_t)i, P);
+    p.id = (uint32_t)(off + i);
+    store_particle(pl, (size_t)ntot, (size_t)(off + i), p);
+    if (track_fp) store_fp(pl, (size_t)ntot, (size_t)(off + i), P);
 }
 
 template <typename T>
-__global__ void k_unpack(int n, const vec4<T>* __restrict__ pl, T* __restrict__ x, T* __restrict__ v,
+__global__ void k_unpack(int n, int off, int ntot, const vec4<T>* __restrict__ pl, T* __restrict__ x, T* __restrict__ v,
                          T* __restrict__ B, T* __restrict__ FE, T* __restrict__ FP, T* __restrict__ Jp,
                          T* __restrict__ mass, T* __restrict__ vol, int track_fp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Particle<T> p;
-    load_particle(pl, (size_t)n, (size_t)i, p);
-    const uint32_t o = p.id;
+    load_particle(pl, (size_t)ntot, (size_t)(off + i), p);
+    const uint32_t o = p.id - (uint32_t)off;
     if (o >= (uint32_t)n) return;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -69,7 +71,7 @@ __global__ void k_unpack(int n, const vec4<T>* __restrict__ pl, T* __restrict__ 
     if (FP) {
         T P[9];
         if (track_fp) {
-            load_fp(pl, (size_t)n, (size_t)i, P);
+            load_fp(pl, (size_t)ntot, (size_t)(off + i), P);
         } else {  // only det F_P is carried: report the isotropic F_P with that det
             const T c = cbrt(p.Jp);
 #pragma unroll
@@ -98,8 +100,43 @@ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 }  // namespace
 
-struct rd_handle {
+// One scene of a handle: its parameters and where its particles, grid nodes
+// and 4x4x4 blocks start in the handle's shared arrays.
+struct rd_scene_info {
     rd_params prm{};
+    int n = 0;
+    uint32_t poff = 0;
+    size_t ncells = 0;
+    size_t goff = 0;
+    int NB[3] = {0, 0, 0};
+    int nblocks = 0;
+    uint32_t block_base = 0;
+    bool set = false;  // particles uploaded
+};
+
+// Two steady steps captured as one CUDA graph, for one assignment of the
+// ping-pong buffers and one dt.
+struct rd_graph {
+    int key = 0;
+    double dt = 0.0;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t launches = 0;
+};
+
+struct rd_handle {
+    rd_params prm{};                    // scene 0's (precision, device, flags for all)
+    std::vector<rd_scene_info> scenes;  // one, or a batch
+    void* d_scenes = nullptr;           // DevParams<T> per scene (batches)
+    uint32_t* d_sblock = nullptr;       // first block of each scene, then the total
+    uint32_t* d_spoff = nullptr;        // first particle of each scene, then the total
+    void* h_scenes = nullptr;           // pinned staging of the table
+    bool table_valid = false;
+    double table_dt = 0.0, table_fs = 0.0;
+    size_t max_scene_cells = 0;
+    std::vector<rd_graph> graphs;
+    bool use_graphs = true;
+    int wp = 0;         // particles per work item (<= WorkP)
+    int grid_mult = 0;  // persistent CTAs per SM of the step kernels (0: occupancy)
     cudaStream_t stream = nullptr;
     int sms = 0;
     int n = 0;
@@ -180,13 +217,13 @@ template <typename T> T reference_dinv(T h) {
     return r;
 }
 
-template <typename T> DevParams<T> make_params(const rd_handle* h, double dt, T fscale) {
-    const rd_params& p = h->prm;
+template <typename T>
+DevParams<T> params_of(const rd_params& p, const int NB[3], int nkeys, int n, double dt, T fscale) {
     DevParams<T> P{};
     P.M[0] = p.max_i; P.M[1] = p.max_j; P.M[2] = p.max_k;
-    P.NB[0] = h->NB[0]; P.NB[1] = h->NB[1]; P.NB[2] = h->NB[2];
-    P.nkeys = h->nkeys;
-    P.n = h->n;
+    P.NB[0] = NB[0]; P.NB[1] = NB[1]; P.NB[2] = NB[2];
+    P.nkeys = nkeys;
+    P.n = n;
     const T hh = (T)p.h;
     P.h = hh;
     P.dinv = reference_dinv<T>(hh);
@@ -214,8 +251,26 @@ template <typename T> DevParams<T> make_params(const rd_handle* h, double dt, T 
     P.bc = p.bc;
     P.bc_width = p.bc_width;
     P.lagged = p.lagged_b;
+    P.block_base = 0;
+    P.goff = 0;
     return P;
 }
+
+// Parameters of scene 0 (the whole handle for a single scene); n is the
+// particle count of all scenes, the stride of the particle planes.
+template <typename T> DevParams<T> make_params(const rd_handle* h, double dt, T fscale) {
+    return params_of<T>(h->prm, h->NB, h->nkeys, h->n, dt, fscale);
+}
+
+template <typename T> DevParams<T> scene_params(const rd_handle* h, int s, double dt, T fscale) {
+    const rd_scene_info& sc = h->scenes[s];
+    DevParams<T> P = params_of<T>(sc.prm, sc.NB, sc.nblocks * kCellsPerBlock, h->n, dt, fscale);
+    P.block_base = sc.block_base;
+    P.goff = sc.goff;
+    return P;
+}
+
+inline bool batched(const rd_handle* h) { return h->scenes.size() > 1; }
 
 template <typename T> DevBufs bufs(rd_handle* h) {
     DevBufs D{};
@@ -231,6 +286,10 @@ template <typename T> DevBufs bufs(rd_handle* h) {
     D.grid_next = h->grid[h->g ^ 1];
     D.gforce = h->gforce;
     D.flags = h->flags;
+    D.scenes = h->d_scenes;
+    D.sblock = h->d_sblock;
+    D.spoff = h->d_spoff;
+    D.nscenes = (int)h->scenes.size();
     return D;
 }
 
@@ -242,6 +301,24 @@ rd_status launched(rd_handle* h, const char* what, int count = 1) {
 }
 
 constexpr size_t kEventPairs = 4096;
+
+// Uploads the per-scene parameter table of a batch for (dt, fscale) unless it
+// holds them already.
+template <typename T> rd_status ensure_table(rd_handle* h, double dt, T fscale) {
+    if (!batched(h)) return RD_OK;
+    if (h->table_valid && h->table_dt == dt && h->table_fs == (double)fscale) return RD_OK;
+    // the pinned staging may still be the source of the previous upload
+    RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "sync"));
+    DevParams<T>* hp = static_cast<DevParams<T>*>(h->h_scenes);
+    for (size_t s = 0; s < h->scenes.size(); ++s) hp[s] = scene_params<T>(h, (int)s, dt, fscale);
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(h->d_scenes, hp, h->scenes.size() * sizeof(DevParams<T>),
+                                         cudaMemcpyHostToDevice, h->stream),
+                      "scene table"));
+    h->table_valid = true;
+    h->table_dt = dt;
+    h->table_fs = (double)fscale;
+    return RD_OK;
+}
 
 // Adds the elapsed time of every recorded pair to the per-kernel totals.
 rd_status harvest_timing(rd_handle* h) {
@@ -270,6 +347,10 @@ void tmark_end(rd_handle* h, long i) {
     if (i >= 0) cudaEventRecord(h->ev[2 * i + 1], h->stream);
 }
 
+template <typename T> int work_size(const rd_handle* h) {
+    return h->wp > 0 ? std::min(h->wp, WorkP<T>::value) : WorkP<T>::value;
+}
+
 // Sort by block key: histogram (unless the last fused G2P already counted),
 // scan + work items, scatter into perm.
 template <typename T> rd_status sort_particles(rd_handle* h) {
@@ -282,8 +363,14 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     if (!h->keys_valid) {
         RD_TRY(check_cuda(h, cudaMemsetAsync(h->counts, 0, sizeof(uint32_t) * h->nkeys, h->stream), "memset counts"));
         long t = tmark_begin(h, RD_KERNEL_KEYS);
-        k_keys<T><<<blocks_for(h->n, 256), 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->pl[h->cur]),
-                                                                  h->keys[h->cur], h->counts, h->flags);
+        const DevBufs D = bufs<T>(h);
+        const vec4<T>* pl = static_cast<const vec4<T>*>(h->pl[h->cur]);
+        if (batched(h)) {
+            RD_TRY(ensure_table<T>(h, h->table_valid ? h->table_dt : 0.0, T(h->table_valid ? h->table_fs : 0.0)));
+            k_keys<T, true><<<blocks_for(h->n, 256), 256, 0, h->stream>>>(P, D, pl, h->keys[h->cur]);
+        } else {
+            k_keys<T, false><<<blocks_for(h->n, 256), 256, 0, h->stream>>>(P, D, pl, h->keys[h->cur]);
+        }
         tmark_end(h, t);
         RD_TRY(launched(h, "k_keys"));
     }
@@ -295,8 +382,8 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     long t = tmark_begin(h, RD_KERNEL_SCAN);
     k_tile_sums<<<ntiles, 256, 0, h->stream>>>(h->counts, h->nkeys, h->tile_sums);
     k_scan<<<ntiles, kScanThreads, 0, h->stream>>>(h->counts, h->cursor, h->tile_sums, h->nkeys, h->work, nw, nw_next,
-                                                (uint32_t)h->n, (uint32_t)h->work_cap, (uint32_t)WorkP<T>::value,
-                                                h->flags);
+                                                (uint32_t)h->n, (uint32_t)h->work_cap, (uint32_t)work_size<T>(h),
+                                                h->flags, h->d_sblock, (int)h->scenes.size());
     tmark_end(h, t);
     RD_TRY(launched(h, "k_scan", 2));
     h->nb ^= 1;
@@ -310,8 +397,9 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
 }
 
 template <typename T> unsigned persistent_grid(const rd_handle* h, int occ) {
-    const size_t max_items = (size_t)h->n / WorkP<T>::value + (size_t)std::min<int64_t>(h->nblocks, h->n) + 1;
-    return (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)h->sms * occ));
+    const size_t max_items = (size_t)h->n / work_size<T>(h) + (size_t)std::min<int64_t>(h->nblocks, h->n) + 1;
+    const int per_sm = h->grid_mult > 0 ? std::min(h->grid_mult, occ) : occ;
+    return (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)h->sms * per_sm));
 }
 
 template <typename T> rd_status step_fused(rd_handle* h, double dt) {
@@ -323,6 +411,8 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
         h->last_dt = dt;
         return RD_OK;
     }
+    const bool batch = batched(h);
+    if (batch) RD_TRY(ensure_table<T>(h, dt, (T)dt));
     if (!h->sorted) RD_TRY(sort_particles<T>(h));
     DevParams<T> P = make_params<T>(h, dt, (T)dt);
     long t;
@@ -332,7 +422,11 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
         tmark_end(h, t);
         DevBufs D = bufs<T>(h);
         t = tmark_begin(h, RD_KERNEL_P2G);
-        k_p2g<T, true, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GTile<T, kBlk>), h->stream>>>(P, D);
+        const unsigned pg = persistent_grid<T>(h, h->occ_p2g);
+        if (batch)
+            k_p2g<T, true, true, true><<<pg, kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+        else
+            k_p2g<T, true, true, false><<<pg, kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
         tmark_end(h, t);
         RD_TRY(launched(h, "k_p2g"));
     }
@@ -341,10 +435,13 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
     tmark_end(h, t);
     DevBufs D = bufs<T>(h);
     t = tmark_begin(h, RD_KERNEL_G2P2G);
-    if (h->prm.track_fp)
-        k_g2p2g<T, true><<<persistent_grid<T>(h, h->occ_g2p), kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
+    const unsigned fg = persistent_grid<T>(h, h->occ_g2p);
+    if (batch)
+        k_g2p2g<T, false, true><<<fg, kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
+    else if (h->prm.track_fp)
+        k_g2p2g<T, true, false><<<fg, kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
     else
-        k_g2p2g<T, false><<<persistent_grid<T>(h, h->occ_g2p), kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
+        k_g2p2g<T, false, false><<<fg, kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
     tmark_end(h, t);
     RD_TRY(launched(h, "k_g2p2g"));
     h->cur ^= 1;
@@ -359,6 +456,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
 }
 
 template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
+    if (batched(h)) return fail(h, RD_NOT_SUPPORTED, "the stage calls drive a single scene; batches step with rd_step");
     const size_t nc = h->ncells;
     const unsigned cb = blocks_for(nc, 256);
     DevParams<T> P = make_params<T>(h, dt, T(1));
@@ -370,7 +468,7 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
             RD_TRY(check_cuda(h, cudaMemsetAsync(h->gforce, 0, nc * sizeof(vec4<T>), h->stream), "memset force"));
             if (h->n > 0) {
                 DevBufs D = bufs<T>(h);
-                k_p2g<T, true, false><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GTile<T, kBlk>), h->stream>>>(P, D);
+                k_p2g<T, true, false, false><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
                 RD_TRY(launched(h, "k_p2g<rasterize>"));
             }
             k_grid_normalize<T><<<cb, 256, 0, h->stream>>>(static_cast<vec4<T>*>(h->grid[h->g]), nc);
@@ -383,7 +481,7 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
             if (!h->sorted) RD_TRY(sort_particles<T>(h));
             if (h->n > 0) {
                 DevBufs D = bufs<T>(h);
-                k_p2g<T, false, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GTile<T, kBlk>), h->stream>>>(P, D);
+                k_p2g<T, false, true, false><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
                 RD_TRY(launched(h, "k_p2g<forces>"));
             }
             return RD_OK;
@@ -423,17 +521,17 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
             if (h->grid_mode != GRID_V && h->grid_mode != GRID_MV)
                 return fail(h, RD_INVALID_ARG, "volume stage needs a rasterized grid");
             if (h->n == 0) return RD_OK;
-            k_volumes<T><<<blocks_for(h->n, 256), 256, 0, h->stream>>>(P, static_cast<vec4<T>*>(h->pl[h->cur]),
-                                                                        static_cast<const vec4<T>*>(h->grid[h->g]),
-                                                                        h->flags);
+            k_volumes<T, false><<<blocks_for(h->n, 256), 256, 0, h->stream>>>(
+                P, bufs<T>(h), static_cast<vec4<T>*>(h->pl[h->cur]), static_cast<const vec4<T>*>(h->grid[h->g]));
             return launched(h, "k_volumes");
         default:
             return fail(h, RD_INVALID_ARG, "unknown stage id");
     }
 }
 
-template <typename T> rd_status set_particles_impl(rd_handle* h, const rd_particles* in, int where) {
-    const size_t n = (size_t)h->n;
+template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, const rd_particles* in, int where) {
+    rd_scene_info& sc = h->scenes[scene];
+    const size_t n = (size_t)sc.n;
     if (!in->x || !in->v || !in->mass) return fail(h, RD_INVALID_ARG, "x, v and mass are required");
     T* io = static_cast<T*>(h->io);
     // io layout: x 3n | v 3n | B 9n | FE 9n | FP 9n | Jp n | mass n | vol n
@@ -452,11 +550,12 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, const rd_partic
         }
     }
     if (n > 0) {
-        k_pack<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, ptr[0], ptr[1], ptr[2], ptr[3], ptr[4], ptr[5],
-                                                             ptr[6], ptr[7], static_cast<vec4<T>*>(h->pl[h->cur]),
-                                                             h->prm.track_fp);
+        k_pack<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, (int)sc.poff, h->n, ptr[0], ptr[1], ptr[2], ptr[3],
+                                                             ptr[4], ptr[5], ptr[6], ptr[7],
+                                                             static_cast<vec4<T>*>(h->pl[h->cur]), h->prm.track_fp);
         RD_TRY(launched(h, "k_pack"));
     }
+    sc.set = true;
     h->keys_valid = false;
     h->sorted = false;
     h->fgrid_valid = false;
@@ -464,8 +563,9 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, const rd_partic
     return RD_OK;
 }
 
-template <typename T> rd_status get_particles_impl(rd_handle* h, rd_particles* out, int where) {
-    const size_t n = (size_t)h->n;
+template <typename T> rd_status get_particles_impl(rd_handle* h, int scene, rd_particles* out, int where) {
+    const rd_scene_info& sc = h->scenes[scene];
+    const size_t n = (size_t)sc.n;
     if (n == 0) return RD_OK;
     T* io = static_cast<T*>(h->io);
     T* d[8] = {io, io + 3 * n, io + 6 * n, io + 15 * n, io + 24 * n, io + 33 * n, io + 34 * n, io + 35 * n};
@@ -473,8 +573,9 @@ template <typename T> rd_status get_particles_impl(rd_handle* h, rd_particles* o
     const size_t cnt[8] = {3 * n, 3 * n, 9 * n, 9 * n, 9 * n, n, n, n};
     T* tgt[8];
     for (int k = 0; k < 8; ++k) tgt[k] = dst[k] ? (where == RD_HOST ? d[k] : static_cast<T*>(dst[k])) : nullptr;
-    k_unpack<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, static_cast<const vec4<T>*>(h->pl[h->cur]), tgt[0],
-                                                           tgt[1], tgt[2], tgt[3], tgt[4], tgt[5], tgt[6], tgt[7],
+    k_unpack<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, (int)sc.poff, h->n,
+                                                           static_cast<const vec4<T>*>(h->pl[h->cur]), tgt[0], tgt[1],
+                                                           tgt[2], tgt[3], tgt[4], tgt[5], tgt[6], tgt[7],
                                                            h->prm.track_fp);
     RD_TRY(launched(h, "k_unpack"));
     if (where == RD_HOST) {
@@ -487,23 +588,26 @@ template <typename T> rd_status get_particles_impl(rd_handle* h, rd_particles* o
     return RD_OK;
 }
 
-template <typename T> rd_status get_grid_impl(rd_handle* h, void* mass, void* vel, void* force, int where) {
-    const size_t nc = h->ncells;
+template <typename T>
+rd_status get_grid_impl(rd_handle* h, int scene, void* mass, void* vel, void* force, int where) {
+    const rd_scene_info& sc = h->scenes[scene];
+    const size_t nc = sc.ncells;
     if (h->grid_mode == GRID_NONE) return fail(h, RD_INVALID_ARG, "no grid computed yet");
+    if (force && batched(h)) return fail(h, RD_NOT_SUPPORTED, "grid forces exist in stage mode only");
     const bool host = where == RD_HOST;
     if (host && !h->grid_io) {  // allocated on first use only: a debugging / parity path
-        RD_TRY(check_cuda(h, cudaMalloc(&h->grid_io, 7 * nc * sizeof(T)), "grid export buffer"));
+        RD_TRY(check_cuda(h, cudaMalloc(&h->grid_io, 7 * h->max_scene_cells * sizeof(T)), "grid export buffer"));
     }
     T* scratch = static_cast<T*>(h->grid_io);
     T* m_d = host ? scratch : static_cast<T*>(mass);
     T* v_d = host ? scratch + nc : static_cast<T*>(vel);
-    DevParams<T> P = make_params<T>(h, h->last_dt, T(1));
+    DevParams<T> P = scene_params<T>(h, scene, h->last_dt, T(1));
     const unsigned cb = blocks_for(nc, 256);
     if (h->grid_mode == GRID_FUSED)  // the grid the last step's G2P read
-        k_grid_export<T, true><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g ^ 1]),
+        k_grid_export<T, true><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g ^ 1]) + sc.goff,
                                                           mass ? m_d : nullptr, vel ? v_d : nullptr);
     else
-        k_grid_export<T, false><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g]),
+        k_grid_export<T, false><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g]) + sc.goff,
                                                            mass ? m_d : nullptr, vel ? v_d : nullptr);
     RD_TRY(launched(h, "k_grid_export"));
     T* f_d = nullptr;
@@ -554,37 +658,64 @@ template <typename T> rd_status debug_sort_impl(rd_handle* h, uint32_t* keys, ui
 }
 
 template <typename T> rd_status init_volumes_impl(rd_handle* h) {
-    RD_TRY(stage_impl<T>(h, RD_STAGE_RASTERIZE, 0.0));
-    return stage_impl<T>(h, RD_STAGE_VOLUMES, 0.0);
+    if (!batched(h)) {
+        RD_TRY(stage_impl<T>(h, RD_STAGE_RASTERIZE, 0.0));
+        return stage_impl<T>(h, RD_STAGE_VOLUMES, 0.0);
+    }
+    // a batch: the rasterized mass of every scene, then V_p = m_p / rho_p
+    RD_TRY(ensure_table<T>(h, h->table_valid ? h->table_dt : 0.0, T(h->table_valid ? h->table_fs : 0.0)));
+    if (!h->sorted) RD_TRY(sort_particles<T>(h));
+    h->fgrid_valid = false;
+    RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid[h->g], 0, h->ncells * sizeof(vec4<T>), h->stream), "memset grid"));
+    const DevParams<T> P = make_params<T>(h, 0.0, T(1));
+    const DevBufs D = bufs<T>(h);
+    k_p2g<T, true, false, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+    RD_TRY(launched(h, "k_p2g<rasterize>"));
+    k_volumes<T, true><<<blocks_for(h->n, 256), 256, 0, h->stream>>>(P, D, static_cast<vec4<T>*>(h->pl[h->cur]),
+                                                                      static_cast<const vec4<T>*>(h->grid[h->g]));
+    RD_TRY(launched(h, "k_volumes"));
+    h->grid_mode = GRID_MV;
+    return RD_OK;
 }
 
 template <typename T> rd_status occupancy(rd_handle* h) {
     int o = 0;
-    const int sm = (int)sizeof(P2GTile<T, kBlk>);
-    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_p2g<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
-    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_p2g<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
-    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_p2g<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
-    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true>, kThreads, sm), "occ"));
+    const int sm = (int)sizeof(P2GShared<T>);
+    const void* p2g[] = {(const void*)k_p2g<T, true, true, false>, (const void*)k_p2g<T, true, false, false>,
+                         (const void*)k_p2g<T, false, true, false>, (const void*)k_p2g<T, true, true, true>,
+                         (const void*)k_p2g<T, true, false, true>};
+    for (const void* f : p2g)
+        RD_TRY(check_cuda(h, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
+    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true, false>, kThreads, sm), "occ"));
     h->occ_p2g = std::max(1, o);
     const int fsm = (int)sizeof(FusedShared<T>);
-    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_g2p2g<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm), "smem attr"));
-    RD_TRY(check_cuda(h, cudaFuncSetAttribute(k_g2p2g<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm), "smem attr"));
-    if (h->prm.track_fp)
-        RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_g2p2g<T, true>, kFusedThreads, fsm), "occ"));
-    else
-        RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_g2p2g<T, false>, kFusedThreads, fsm), "occ"));
+    const void* fused[] = {(const void*)k_g2p2g<T, true, false>, (const void*)k_g2p2g<T, false, false>,
+                           (const void*)k_g2p2g<T, false, true>};
+    for (const void* f : fused)
+        RD_TRY(check_cuda(h, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm), "smem attr"));
+    const void* used = batched(h) ? fused[2] : (h->prm.track_fp ? fused[0] : fused[1]);
+    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, used, kFusedThreads, fsm), "occ"));
     h->occ_g2p = std::max(1, o);
     return RD_OK;
+}
+
+void drop_graphs(rd_handle* h) {
+    for (rd_graph& g : h->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    h->graphs.clear();
 }
 
 void release(rd_handle* h) {
     for (cudaEvent_t e : h->ev)
         if (e) cudaEventDestroy(e);
     h->ev.clear();
+    drop_graphs(h);
     void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->cursor, h->work,
-                    h->nwork2, h->tile_sums, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io};
+                    h->nwork2, h->tile_sums, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
+                    h->d_scenes, h->d_sblock, h->d_spoff};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (h->h_scenes) cudaFreeHost(h->h_scenes);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -612,27 +743,69 @@ void rd_default_params(rd_params* p) {
     p->device = 0;
 }
 
-rd_status rd_create(const rd_params* params, rd_handle** out) {
-    if (!params || !out) return RD_INVALID_ARG;
+}  // extern "C"
+
+namespace {
+
+bool valid_scene(const rd_params& p) {
+    return p.max_i >= 8 && p.max_j >= 8 && p.max_k >= 8 && p.num_particles >= 0 && p.h > 0 &&
+           (p.precision == RD_FP32 || p.precision == RD_FP64) && p.bc_width >= 0 &&
+           (int64_t)p.max_i * p.max_j * p.max_k <= (int64_t)1 << 30;
+}
+
+// Creates a handle over nscenes scenes: the particles of scene s occupy
+// [poff_s, poff_s + n_s) of the shared particle planes (in every step's
+// sorted order too, since the block keys of scene s precede those of s + 1),
+// its grid nodes [goff_s, goff_s + cells_s) of each grid buffer.
+rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
+    if (!params || !out || nscenes < 1) return RD_INVALID_ARG;
     *out = nullptr;
-    const rd_params& p = *params;
-    if (p.max_i < 8 || p.max_j < 8 || p.max_k < 8 || p.num_particles < 0 || !(p.h > 0) ||
-        (p.precision != RD_FP32 && p.precision != RD_FP64) || p.bc_width < 0 ||
-        (int64_t)p.max_i * p.max_j * p.max_k > (int64_t)1 << 30)
-        return RD_INVALID_ARG;
+    const rd_params& p = params[0];
+    int64_t ntot = 0, cells = 0, blocks = 0;
+    for (int s = 0; s < nscenes; ++s) {
+        const rd_params& q = params[s];
+        if (!valid_scene(q)) return RD_INVALID_ARG;
+        if (q.precision != p.precision || q.device != p.device || q.lagged_b != p.lagged_b || q.track_fp != p.track_fp)
+            return RD_INVALID_ARG;
+        ntot += q.num_particles;
+        cells += (int64_t)q.max_i * q.max_j * q.max_k;
+        blocks += (int64_t)((q.max_i + kBlk - 1) / kBlk) * ((q.max_j + kBlk - 1) / kBlk) * ((q.max_k + kBlk - 1) / kBlk);
+    }
+    if (nscenes > 1 && p.track_fp) return RD_NOT_SUPPORTED;
+    if (ntot >= ((int64_t)1 << 30) || blocks * kCellsPerBlock >= ((int64_t)1 << 31)) return RD_TOO_LARGE;
     rd_handle* h = new (std::nothrow) rd_handle;
     if (!h) return RD_OOM;
     h->prm = p;
-    h->n = p.num_particles;
+    h->scenes.resize(nscenes);
+    {
+        uint32_t poff = 0, bbase = 0;
+        size_t goff = 0;
+        for (int s = 0; s < nscenes; ++s) {
+            rd_scene_info& sc = h->scenes[s];
+            sc.prm = params[s];
+            sc.n = params[s].num_particles;
+            sc.poff = poff;
+            sc.ncells = (size_t)sc.prm.max_i * sc.prm.max_j * sc.prm.max_k;
+            sc.goff = goff;
+            sc.NB[0] = (sc.prm.max_i + kBlk - 1) / kBlk;
+            sc.NB[1] = (sc.prm.max_j + kBlk - 1) / kBlk;
+            sc.NB[2] = (sc.prm.max_k + kBlk - 1) / kBlk;
+            sc.nblocks = sc.NB[0] * sc.NB[1] * sc.NB[2];
+            sc.block_base = bbase;
+            poff += (uint32_t)sc.n;
+            goff += sc.ncells;
+            bbase += (uint32_t)sc.nblocks;
+            h->max_scene_cells = std::max(h->max_scene_cells, sc.ncells);
+        }
+    }
+    h->n = (int)ntot;
     h->esize = p.precision == RD_FP64 ? 8 : 4;
     h->planes = p.track_fp ? kPlanesFP : kPlanes;
-    h->ncells = (size_t)p.max_i * p.max_j * p.max_k;
-    h->NB[0] = (p.max_i + kBlk - 1) / kBlk;
-    h->NB[1] = (p.max_j + kBlk - 1) / kBlk;
-    h->NB[2] = (p.max_k + kBlk - 1) / kBlk;
-    h->nblocks = h->NB[0] * h->NB[1] * h->NB[2];
-    h->nkeys = h->nblocks * kCellsPerBlock;
-    auto bail = [&](rd_status s) { release(h); delete h; return s; };
+    h->ncells = (size_t)cells;
+    for (int a = 0; a < 3; ++a) h->NB[a] = h->scenes[0].NB[a];
+    h->nblocks = (int)blocks;
+    h->nkeys = (int)blocks * kCellsPerBlock;
+    auto bail = [&](rd_status st) { release(h); delete h; return st; };
     if (cudaSetDevice(p.device) != cudaSuccess) return bail(RD_CUDA_ERROR);
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, p.device) != cudaSuccess) return bail(RD_CUDA_ERROR);
@@ -641,40 +814,207 @@ rd_status rd_create(const rd_params* params, rd_handle** out) {
     const size_t n = std::max<size_t>(1, (size_t)h->n);
     const size_t v4 = 4 * h->esize;
     const size_t wp = p.precision == RD_FP64 ? WorkP<double>::value : WorkP<float>::value;
-    h->work_cap = n / wp + std::min<size_t>((size_t)h->nblocks, n) + 2;
-    struct { void** ptr; size_t bytes; } allocs[] = {
-        {&h->pl[0], (size_t)h->planes * n * v4},
-        {&h->pl[1], (size_t)h->planes * n * v4},
-        {(void**)&h->keys[0], n * 4},
-        {(void**)&h->keys[1], n * 4},
-        {(void**)&h->perm, n * 4},
-        {(void**)&h->counts, (size_t)h->nkeys * 4},
-        {(void**)&h->cursor, (size_t)h->nkeys * 4},
-        {(void**)&h->work, h->work_cap * sizeof(int4)},
-        {(void**)&h->nwork2, 8},
-        {(void**)&h->tile_sums, (size_t)((h->nkeys + kScanTile - 1) / kScanTile) * 4},
-        {&h->grid[0], h->ncells * v4},
-        {&h->grid[1], h->ncells * v4},
-        {&h->gforce, h->ncells * v4},
-        {(void**)&h->flags, 4},
-        {(void**)&h->xyzs, n * sizeof(float4)},
-        {&h->io, align_up(36 * n * h->esize, 256)},
+    // items: at most n / wp + one partial item per occupied block; autotuned
+    // item sizes go down to wp / 4
+    h->work_cap = 4 * (n / wp) + std::min<size_t>((size_t)h->nblocks, n) + 2;
+    const size_t psize = p.precision == RD_FP64 ? sizeof(DevParams<double>) : sizeof(DevParams<float>);
+    const bool batch = nscenes > 1;
+    struct { void** ptr; size_t bytes; bool need; } allocs[] = {
+        {&h->pl[0], (size_t)h->planes * n * v4, true},
+        {&h->pl[1], (size_t)h->planes * n * v4, true},
+        {(void**)&h->keys[0], n * 4, true},
+        {(void**)&h->keys[1], n * 4, true},
+        {(void**)&h->perm, n * 4, true},
+        {(void**)&h->counts, (size_t)h->nkeys * 4, true},
+        {(void**)&h->cursor, (size_t)h->nkeys * 4, true},
+        {(void**)&h->work, h->work_cap * sizeof(int4), true},
+        {(void**)&h->nwork2, 8, true},
+        {(void**)&h->tile_sums, (size_t)((h->nkeys + kScanTile - 1) / kScanTile) * 4, true},
+        {&h->grid[0], h->ncells * v4, true},
+        {&h->grid[1], h->ncells * v4, true},
+        {&h->gforce, h->ncells * v4, !batch},  // stage mode only
+        {(void**)&h->flags, 4, true},
+        {(void**)&h->xyzs, n * sizeof(float4), true},
+        {&h->io, align_up(36 * n * h->esize, 256), true},
+        {&h->d_scenes, nscenes * psize, batch},
+        {(void**)&h->d_sblock, (nscenes + 1) * sizeof(uint32_t), batch},
+        {(void**)&h->d_spoff, (nscenes + 1) * sizeof(uint32_t), batch},
     };
     for (auto& a : allocs) {
+        if (!a.need) continue;
         cudaError_t e = cudaMalloc(a.ptr, a.bytes);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return bail(e == cudaErrorMemoryAllocation ? RD_OOM : RD_CUDA_ERROR);
         }
     }
+    if (batch) {
+        if (cudaMallocHost(&h->h_scenes, nscenes * psize) != cudaSuccess) return bail(RD_OOM);
+        std::vector<uint32_t> sb(nscenes + 1), sp(nscenes + 1);
+        for (int s = 0; s < nscenes; ++s) { sb[s] = h->scenes[s].block_base; sp[s] = h->scenes[s].poff; }
+        sb[nscenes] = (uint32_t)blocks;
+        sp[nscenes] = (uint32_t)ntot;
+        if (cudaMemcpy(h->d_sblock, sb.data(), sb.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(h->d_spoff, sp.data(), sp.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(RD_CUDA_ERROR);
+    }
     cudaMemsetAsync(h->counts, 0, (size_t)h->nkeys * 4, h->stream);
     cudaMemsetAsync(h->perm, 0, n * 4, h->stream);  // every entry is a valid index from the start
     cudaMemsetAsync(h->flags, 0, 4, h->stream);
     cudaMemsetAsync(h->nwork2, 0, 8, h->stream);
-    rd_status s = p.precision == RD_FP64 ? occupancy<double>(h) : occupancy<float>(h);
-    if (s != RD_OK) return bail(s);
+    rd_status st = p.precision == RD_FP64 ? occupancy<double>(h) : occupancy<float>(h);
+    if (st != RD_OK) return bail(st);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(RD_CUDA_ERROR);
     *out = h;
+    return RD_OK;
+}
+
+// Replays (capturing first if needed) two steady steps as one CUDA graph.
+// Steady: the keys of the current positions are counted, the grid holds
+// their P2G for this dt, and the scene table (batches) is current, so the two
+// steps are exactly scan, scatter, grid clear and k_g2p2g twice, and leave the
+// host-side state as they found it.
+template <typename T> rd_status graph_two_steps(rd_handle* h, double dt) {
+    const int key = h->cur | (h->g << 1) | (h->nb << 2);
+    for (rd_graph& g : h->graphs)
+        if (g.key == key && g.dt == dt) {
+            RD_TRY(check_cuda(h, cudaGraphLaunch(g.exec, h->stream), "graph launch"));
+            h->launches += g.launches;
+            return RD_OK;
+        }
+    if (h->graphs.size() >= 8) drop_graphs(h);
+    const uint64_t l0 = h->launches;
+    RD_TRY(check_cuda(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture"));
+    rd_status s1 = step_fused<T>(h, dt);
+    rd_status s2 = s1 == RD_OK ? step_fused<T>(h, dt) : s1;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    if (s2 != RD_OK || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        h->use_graphs = false;  // eager steps from here on
+        return s2 != RD_OK ? s2 : check_cuda(h, e, "end capture");
+    }
+    rd_graph g;
+    g.key = key;
+    g.dt = dt;
+    g.launches = h->launches - l0;
+    const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    RD_TRY(check_cuda(h, ie, "graph instantiate"));
+    h->graphs.push_back(g);
+    return check_cuda(h, cudaGraphLaunch(g.exec, h->stream), "graph launch");
+}
+
+bool steady(const rd_handle* h, double dt) {
+    return h->use_graphs && !h->timing && h->n > 0 && h->keys_valid && !h->sorted && h->fgrid_valid &&
+           h->fgrid_dt == dt && h->grid_mode == GRID_FUSED &&
+           (!batched(h) || (h->table_valid && h->table_dt == dt && h->table_fs == dt));
+}
+
+template <typename T> rd_status steps_impl(rd_handle* h, double dt, int nsteps) {
+    for (int s = 0; s < nsteps;) {
+        if (nsteps - s >= 2 && steady(h, dt)) {
+            RD_TRY(graph_two_steps<T>(h, dt));
+            s += 2;
+        } else {
+            RD_TRY(step_fused<T>(h, dt));
+            s += 1;
+        }
+    }
+    return RD_OK;
+}
+
+// Times the step under each candidate work-item size and persistent grid
+// (CTAs per SM) from the same saved state, keeps the fastest and puts the
+// state back as it was (the next step re-sorts and rebuilds the grid).
+template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps, rd_tune_result* res) {
+    const int wps_f[] = {128, 192, 256}, wps_d[] = {64, 96, 128};
+    const int* wps = sizeof(T) == 4 ? wps_f : wps_d;
+    rd_tune_result best{WorkP<T>::value, 0, 0.0, 0};
+    if (h->n == 0) { *res = best; return RD_OK; }
+    const size_t bytes = (size_t)h->planes * h->n * 4 * h->esize;
+    void* saved = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&](rd_status st) {
+        cudaStreamSynchronize(h->stream);
+        if (saved) cudaFree(saved);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return st;
+    };
+    auto restore = [&]() {
+        h->keys_valid = false;
+        h->sorted = false;
+        h->fgrid_valid = false;
+        h->grid_mode = GRID_NONE;
+        return check_cuda(h, cudaMemcpyAsync(h->pl[h->cur], saved, bytes, cudaMemcpyDeviceToDevice, h->stream),
+                          "restore state");
+    };
+    rd_status st = check_cuda(h, cudaMalloc(&saved, bytes), "autotune state");
+    if (st == RD_OK) st = check_cuda(h, cudaEventCreate(&e0), "event");
+    if (st == RD_OK) st = check_cuda(h, cudaEventCreate(&e1), "event");
+    if (st == RD_OK)
+        st = check_cuda(h, cudaMemcpyAsync(saved, h->pl[h->cur], bytes, cudaMemcpyDeviceToDevice, h->stream), "save");
+    const int old_wp = h->wp, old_mult = h->grid_mult;
+    float best_ms = 0.f;
+    for (int a = 0; a < 3 && st == RD_OK; ++a)
+        for (int c = 1; c <= h->occ_g2p && st == RD_OK; ++c) {
+            h->wp = wps[a];
+            h->grid_mult = c;
+            drop_graphs(h);
+            if ((st = restore()) != RD_OK) break;
+            // two eager steps (sort, P2G), then one captured pair, untimed
+            if ((st = steps_impl<T>(h, dt, 2)) != RD_OK) break;
+            if ((st = steps_impl<T>(h, dt, 2)) != RD_OK) break;
+            if ((st = check_cuda(h, cudaEventRecord(e0, h->stream), "event")) != RD_OK) break;
+            if ((st = steps_impl<T>(h, dt, steps)) != RD_OK) break;
+            if ((st = check_cuda(h, cudaEventRecord(e1, h->stream), "event")) != RD_OK) break;
+            if ((st = check_cuda(h, cudaEventSynchronize(e1), "event sync")) != RD_OK) break;
+            float ms = 0.f;
+            if ((st = check_cuda(h, cudaEventElapsedTime(&ms, e0, e1), "event time")) != RD_OK) break;
+            ++best.trials;
+            if (best.trials == 1 || ms < best_ms) {
+                best_ms = ms;
+                best.particles_per_item = wps[a];
+                best.ctas_per_sm = c;
+            }
+        }
+    if (st != RD_OK) {
+        h->wp = old_wp;
+        h->grid_mult = old_mult;
+        drop_graphs(h);
+        if (saved) restore();
+        return cleanup(st);
+    }
+    h->wp = best.particles_per_item;
+    h->grid_mult = best.ctas_per_sm;
+    best.ms_per_step = steps > 0 ? best_ms / steps : 0.0;
+    drop_graphs(h);
+    st = restore();
+    *res = best;
+    return cleanup(st);
+}
+
+bool all_set(const rd_handle* h) {
+    for (const rd_scene_info& sc : h->scenes)
+        if (!sc.set && sc.n > 0) return false;
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+rd_status rd_create(const rd_params* params, rd_handle** out) { return create_impl(params, 1, out); }
+
+rd_status rd_batch_create(const rd_params* scenes, int32_t nscenes, rd_handle** out) {
+    return create_impl(scenes, nscenes, out);
+}
+
+rd_status rd_batch_num_scenes(rd_handle* h, int32_t* nscenes) {
+    if (!h || !nscenes) return RD_INVALID_ARG;
+    *nscenes = (int32_t)h->scenes.size();
     return RD_OK;
 }
 
@@ -689,31 +1029,89 @@ rd_status rd_destroy(rd_handle* h) {
 
 #define RD_DISPATCH(h, fn, ...) ((h)->prm.precision == RD_FP64 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
 
+rd_status rd_batch_set_particles(rd_handle* h, int32_t scene, const rd_particles* in, int where) {
+    if (!h || !in || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
+    if (scene < 0 || scene >= (int32_t)h->scenes.size()) return fail(h, RD_INVALID_ARG, "no such scene");
+    cudaSetDevice(h->prm.device);
+    return RD_DISPATCH(h, set_particles_impl, h, scene, in, where);
+}
+
+rd_status rd_batch_get_particles(rd_handle* h, int32_t scene, rd_particles* out, int where) {
+    if (!h || !out || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
+    if (scene < 0 || scene >= (int32_t)h->scenes.size()) return fail(h, RD_INVALID_ARG, "no such scene");
+    cudaSetDevice(h->prm.device);
+    return RD_DISPATCH(h, get_particles_impl, h, scene, out, where);
+}
+
+rd_status rd_batch_get_grid(rd_handle* h, int32_t scene, void* mass, void* velocity, int where) {
+    if (!h || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
+    if (scene < 0 || scene >= (int32_t)h->scenes.size()) return fail(h, RD_INVALID_ARG, "no such scene");
+    cudaSetDevice(h->prm.device);
+    return RD_DISPATCH(h, get_grid_impl, h, scene, mass, velocity, nullptr, where);
+}
+
+rd_status rd_batch_step(rd_handle* h, double dt, int32_t nsteps) { return rd_step(h, dt, nsteps); }
+
 rd_status rd_set_particles(rd_handle* h, const rd_particles* in, int where) {
     if (!h || !in || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
+    if (batched(h)) return fail(h, RD_INVALID_ARG, "a batch takes its particles per scene (rd_batch_set_particles)");
     cudaSetDevice(h->prm.device);
-    return RD_DISPATCH(h, set_particles_impl, h, in, where);
+    return RD_DISPATCH(h, set_particles_impl, h, 0, in, where);
 }
 
 rd_status rd_get_particles(rd_handle* h, rd_particles* out, int where) {
     if (!h || !out || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
+    if (batched(h)) return fail(h, RD_INVALID_ARG, "a batch returns its particles per scene (rd_batch_get_particles)");
     cudaSetDevice(h->prm.device);
-    return RD_DISPATCH(h, get_particles_impl, h, out, where);
+    return RD_DISPATCH(h, get_particles_impl, h, 0, out, where);
 }
 
 rd_status rd_init_volumes(rd_handle* h) {
     if (!h) return RD_INVALID_ARG;
+    if (!all_set(h)) return fail(h, RD_INVALID_ARG, "every scene needs its particles first");
     cudaSetDevice(h->prm.device);
     return RD_DISPATCH(h, init_volumes_impl, h);
 }
 
 rd_status rd_step(rd_handle* h, double dt, int32_t nsteps) {
     if (!h || nsteps < 0 || !std::isfinite(dt)) return RD_INVALID_ARG;
+    if (!all_set(h)) return fail(h, RD_INVALID_ARG, "every scene needs its particles first");
     cudaSetDevice(h->prm.device);
-    for (int s = 0; s < nsteps; ++s) {
-        rd_status st = RD_DISPATCH(h, step_fused, h, dt);
-        if (st != RD_OK) return st;
-    }
+    return RD_DISPATCH(h, steps_impl, h, dt, nsteps);
+}
+
+rd_status rd_autotune(rd_handle* h, double dt, int32_t steps, rd_tune_result* result) {
+    if (!h || !result || steps < 1 || !std::isfinite(dt)) return RD_INVALID_ARG;
+    if (!all_set(h)) return fail(h, RD_INVALID_ARG, "every scene needs its particles first");
+    cudaSetDevice(h->prm.device);
+    return RD_DISPATCH(h, autotune_impl, h, dt, steps, result);
+}
+
+rd_status rd_set_tuning(rd_handle* h, int32_t particles_per_item, int32_t ctas_per_sm) {
+    if (!h || particles_per_item < 0 || ctas_per_sm < 0) return RD_INVALID_ARG;
+    const int wmax = h->prm.precision == RD_FP64 ? WorkP<double>::value : WorkP<float>::value;
+    if (particles_per_item != 0 && (particles_per_item < wmax / 4 || particles_per_item > wmax))
+        return fail(h, RD_INVALID_ARG, "particles per item out of range");
+    cudaSetDevice(h->prm.device);
+    h->wp = particles_per_item;
+    h->grid_mult = ctas_per_sm;
+    drop_graphs(h);
+    return RD_OK;
+}
+
+rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas_per_sm) {
+    if (!h || !particles_per_item || !ctas_per_sm) return RD_INVALID_ARG;
+    const int wmax = h->prm.precision == RD_FP64 ? WorkP<double>::value : WorkP<float>::value;
+    *particles_per_item = h->wp > 0 ? std::min(h->wp, wmax) : wmax;
+    *ctas_per_sm = h->grid_mult > 0 ? std::min(h->grid_mult, h->occ_g2p) : h->occ_g2p;
+    return RD_OK;
+}
+
+rd_status rd_set_graphs(rd_handle* h, int enable) {
+    if (!h) return RD_INVALID_ARG;
+    cudaSetDevice(h->prm.device);
+    h->use_graphs = enable != 0;
+    if (!enable) drop_graphs(h);
     return RD_OK;
 }
 
@@ -725,8 +1123,9 @@ rd_status rd_stage(rd_handle* h, int32_t stage, double dt) {
 
 rd_status rd_get_grid(rd_handle* h, void* mass, void* velocity, void* force, int where) {
     if (!h || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
+    if (batched(h)) return fail(h, RD_INVALID_ARG, "a batch exports its grids per scene (rd_batch_get_grid)");
     cudaSetDevice(h->prm.device);
-    return RD_DISPATCH(h, get_grid_impl, h, mass, velocity, force, where);
+    return RD_DISPATCH(h, get_grid_impl, h, 0, mass, velocity, force, where);
 }
 
 rd_status rd_device_xyzs(rd_handle* h, float** xyzs) {
@@ -954,7 +1353,7 @@ extern "C" rd_status rd_rasterize_noalloc(const rd_params* params, const rd_part
         k_tile_sums<<<ntiles, 256, 0, st>>>(sc->counts, hp.nkeys, sc->tile_sums);
         k_scan<<<ntiles, kScanThreads, 0, st>>>(sc->counts, sc->cursor, sc->tile_sums, hp.nkeys, sc->work, &sc->nwork[0],
                                                 &sc->nwork[1], (uint32_t)n, work_cap, (uint32_t)WorkP<float>::value,
-                                                &sc->flags);
+                                                &sc->flags, nullptr, 1);
         k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(n, sc->keys, sc->cursor, sc->perm);
         const size_t max_items = (size_t)n / WorkP<float>::value + (size_t)std::min<int64_t>(nblocks, n) + 1;
         const unsigned grid = (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)nd.sms * nd.occ));

@@ -19,6 +19,16 @@ same particles:
                     workload is quoted at.
 * ``cube``          65,536 particles uniform in a 0.2-side cube at
                     (0.5, 0.6, 0.5), 64^3 grid, 50 steps.
+
+Batches (lists of scenes stepped together):
+
+* ``uneven_snowballs``  64 snowballs, each with a log-uniform 4,096-262,144
+                    particles on a 32^3-128^3 grid (drawn from the seed), per
+                    scene E ~ U[5e4, 3e5], nu ~ U[0.15, 0.3], v0 ~ N(0, 1)^3,
+                    300 steps.  The radius is set by the particle count at 8
+                    particles per cell, r = (3 N / (32 pi))^(1/3) cells, and a
+                    grid drawn too small for the ball is raised to
+                    2 r + 24 cells.
 """
 from __future__ import annotations
 
@@ -138,5 +148,28 @@ def perturbed_state(rng, n, scale_B=1.0, scale_F=1e-3, dinv=1.0):
     FP = np.eye(3).reshape(1, 9) + rng.normal(0.0, scale_F, size=(n, 9))
     return B.astype(np.float32), FE.astype(np.float32), FP.astype(np.float32)
 
+
+def uneven_snowballs(seed: int = 0, nscenes: int = 64, n_lo: int = 4096, n_hi: int = 262144, g_lo: int = 32,
+                     g_hi: int = 128, steps: int = 300, ppc: float = 8.0) -> list:
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(nscenes):
+        n = int(round(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi)))))
+        g = int(rng.integers(g_lo, g_hi + 1))
+        r_cells = (3.0 * n / (4.0 * np.pi * ppc)) ** (1.0 / 3.0)
+        g = max(g, int(np.ceil(2.0 * r_cells + 24.0)))
+        h = 1.0 / g
+        r = r_cells * h
+        mat = dict(SNOW, E=float(rng.uniform(5e4, 3e5)), nu=float(rng.uniform(0.15, 0.3)))
+        v0 = rng.normal(0.0, 1.0, size=3)
+        x = uniform_ball(rng, n, (0.5, 0.55, 0.5), r)
+        v = np.tile(v0, (n, 1))
+        m = np.full(n, 400.0 * 4.0 / 3.0 * np.pi * r ** 3 / n)
+        out.append(Scene(f"uneven_snowballs[{s}]", (g,) * 3, h, x.astype(np.float32), v.astype(np.float32),
+                         m.astype(np.float32), 1e-4, steps, mat))
+    return out
+
+
+BATCHES = {"uneven_snowballs": uneven_snowballs}
 
 SCENES = {"snowball": snowball, "two_balls": two_balls, "two_balls_1m": two_balls_1m, "cube": cube}

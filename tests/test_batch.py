@@ -1,0 +1,154 @@
+"""Batches of uneven scenes in one handle (rd_batch_*), CUDA-graph replay and
+the autotuner.  Every scene of a batch must step exactly as it does alone:
+against the oracle for the physics, against a single-scene handle for the
+batching itself."""
+import numpy as np
+import pytest
+
+from conftest import b_scale, rel, rel_floor
+
+pytestmark = pytest.mark.gpu
+
+
+def small_batch(seed=5, nscenes=5):
+    """Uneven scenes: particle counts, grid sizes, materials and velocities all differ."""
+    from rd_gb300 import scenes
+    return scenes.uneven_snowballs(seed=seed, nscenes=nscenes, n_lo=1500, n_hi=12000, g_lo=24, g_hi=48)
+
+
+def scene_params(pkg, sc, **over):
+    return pkg.make_params(*sc.grid, sc.n, sc.h, **sc.params(**over))
+
+
+def oracle_of(orc, sc):
+    kw = sc.params()
+    o = orc.OracleSim(orc.Params(*sc.grid, float(sc.h), **kw), sc.x, sc.v, sc.mass)
+    o.init()
+    return o
+
+
+def make_batch(pkg, batch, **over):
+    b = pkg.Batch([scene_params(pkg, sc, **over) for sc in batch])
+    for s, sc in enumerate(batch):
+        b.set_particles(s, sc.x, sc.v, sc.mass)
+    b.init_volumes()
+    return b
+
+
+def compare(got, o, h, tol):
+    errs = {"x": rel(got["x"], o.x), "v": rel(got["v"], o.v),
+            "B": rel_floor(got["B"], o.B, b_scale(o.v, h)), "FE": rel(got["FE"], o.FE), "Jp": rel(got["Jp"], o.Jp)}
+    assert all(e < tol for e in errs.values()), errs
+    return errs
+
+
+def test_batch_one_step_matches_oracle_per_scene(built_pkg, orc):
+    batch = small_batch()
+    b = make_batch(built_pkg, batch)
+    assert b.nscenes == len(batch)
+    orcs = [oracle_of(orc, sc) for sc in batch]
+    for s, o in enumerate(orcs):
+        assert rel(b.get_particles(s, ("volume",))["volume"], o.vol) < 1e-6
+    b.step(batch[0].dt, 1)
+    for s, (sc, o) in enumerate(zip(batch, orcs)):
+        o.step(sc.dt, 1)
+        compare(b.get_particles(s), o, sc.h, 1e-5)
+        g = b.get_grid(s)
+        assert rel(g["mass"], o.gmass) < 1e-6
+        assert rel(g["mass"][:, None] * g["vel"], o.gmass[:, None] * o.gvel) < 1e-5
+    assert b.flags() == 0
+
+
+def test_batch_rollout_matches_single_scene_handles(built_pkg):
+    """20 steps (graph replay included): each scene of the batch against the
+    same scene in its own handle; only the order of FP32 atomics differs."""
+    batch = small_batch(seed=6)
+    b = make_batch(built_pkg, batch)
+    singles = []
+    for sc in batch:
+        s = built_pkg.Simulation(scene_params(built_pkg, sc))
+        s.set_particles(sc.x, sc.v, sc.mass)
+        s.init_volumes()
+        s.step(sc.dt, 20)
+        singles.append(s)
+    b.step(batch[0].dt, 20)
+    for s, (sc, single) in enumerate(zip(batch, singles)):
+        got, ref = b.get_particles(s), single.get_particles()
+        for k in ("x", "v", "FE", "Jp"):
+            assert rel(got[k], ref[k]) < 2e-5, (s, k, rel(got[k], ref[k]))
+        assert rel_floor(got["B"], ref["B"], b_scale(ref["v"], sc.h)) < 2e-5
+        total = float(np.sum(sc.mass, dtype=np.float64))
+        gm = b.get_grid(s)["mass"]
+        assert abs(float(np.sum(gm, dtype=np.float64)) - total) / total < 1e-6
+    assert b.flags() == 0
+
+
+def test_graph_replay_matches_eager_launches(built_pkg):
+    from rd_gb300 import scenes
+    sc = scenes.snowball(seed=4, n=6000, grid=32)
+    out = []
+    for graphs in (True, False):
+        s = built_pkg.Simulation(scene_params(built_pkg, sc))
+        s.set_graphs(graphs)
+        s.set_particles(sc.x, sc.v, sc.mass)
+        s.init_volumes()
+        s.step(sc.dt, 3)
+        l0 = s.launch_count()
+        s.step(sc.dt, 10)
+        # steady steps: tile sums, scan, scatter and the fused kernel
+        assert s.launch_count() - l0 == 40
+        out.append(s.get_particles())
+    for k in ("x", "v", "FE", "Jp"):
+        assert rel(out[0][k], out[1][k]) < 1e-5
+
+
+def test_autotune_picks_a_valid_pair_and_restores_state(built_pkg):
+    batch = small_batch(seed=7, nscenes=4)
+    dt = batch[0].dt
+    tuned = make_batch(built_pkg, batch)
+    ref = make_batch(built_pkg, batch)
+    r = tuned.autotune(dt, steps=4)
+    assert r["particles_per_item"] in (128, 192, 256)
+    assert r["trials"] >= 3 and r["ms_per_step"] > 0
+    assert tuned.tuning() == (r["particles_per_item"], r["ctas_per_sm"])
+    tuned.step(dt, 5)
+    ref.step(dt, 5)
+    for s in range(len(batch)):
+        a, c = tuned.get_particles(s), ref.get_particles(s)
+        for k in ("x", "v", "Jp"):
+            assert rel(a[k], c[k]) < 1e-5, (s, k)
+
+
+@pytest.mark.parametrize("wp", [64, 128, 192])
+def test_item_size_does_not_change_results(built_pkg, orc, wp):
+    from rd_gb300 import scenes
+    sc = scenes.snowball(seed=8, n=5000, grid=32)
+    s = built_pkg.Simulation(scene_params(built_pkg, sc))
+    s.set_tuning(wp, 1)
+    s.set_particles(sc.x, sc.v, sc.mass)
+    s.init_volumes()
+    o = oracle_of(orc, sc)
+    s.step(sc.dt, 1)
+    o.step(sc.dt, 1)
+    compare(s.get_particles(), o, sc.h, 1e-5)
+
+
+def test_batch_rejects_single_scene_calls_and_unset_scenes(built_pkg):
+    pkg = built_pkg
+    batch = small_batch(seed=9, nscenes=3)
+    b = pkg.Batch([scene_params(pkg, sc) for sc in batch])
+    with pytest.raises(pkg.RDError):
+        b.step(1e-4, 1)  # scene particles not set
+    for s, sc in enumerate(batch):
+        b.set_particles(s, sc.x, sc.v, sc.mass)
+    with pytest.raises(pkg.RDError):
+        b.stage("rasterize")
+    with pytest.raises(pkg.RDError):
+        pkg.Simulation.set_particles(b, np.zeros((b.n, 3)), np.zeros((b.n, 3)), np.ones(b.n))
+    with pytest.raises(pkg.RDError):
+        pkg.Batch([scene_params(pkg, sc, track_fp=1) for sc in batch])
+    with pytest.raises(pkg.RDError):
+        b.set_particles(-1, batch[-1].x, batch[-1].v, batch[-1].mass)  # no scene -1
+    b.init_volumes()
+    b.step(1e-4, 2)
+    assert b.flags() == 0
