@@ -230,14 +230,40 @@ def measure_batched(pkg, local, steps, warmup, plain_value):
     ms = e0.elapsed_time(e1)
     launches = b.launch_count() - l0
     flags = b.flags()
+    # per-kernel split of the same steps (events around each launch, no graphs)
+    reset()
+    b.step(dt, warmup)
+    b.set_kernel_timing(True)
+    b.step(dt, steps)
+    kt = b.kernel_timing()
+    b.set_kernel_timing(False)
     b.close()
     value = b.n * steps / (ms / 1e3)
+    # the same scenes as plain forwards, one handle after the other
+    seq_steps = min(steps, 50)
+    seq_ms = 0.0
+    for s in batch:
+        one = pkg.Simulation(pkg.make_params(*s.grid, s.n, s.h, device=local, **s.params()))
+        one.set_particles(s.x, s.v, s.mass)
+        one.init_volumes()
+        one.step(dt, warmup)
+        st = torch.cuda.ExternalStream(one.stream(), device=local)
+        one.synchronize()
+        e0.record(st)
+        one.step(dt, seq_steps)
+        e1.record(st)
+        e1.synchronize()
+        seq_ms += e0.elapsed_time(e1)
+        one.close()
+    seq_value = b.n * seq_steps / (seq_ms / 1e3)
     return {"value": value, "unit": "particle-steps/s", "vs_plain_forward": value / plain_value,
+            "plain_forward_one_scene_at_a_time": seq_value, "vs_one_scene_at_a_time": value / seq_value,
             "steps": steps, "warmup": warmup, "ms_per_step": ms / steps, "gpu_launches": launches,
             "scenes": len(batch), "particles": b.n, "grid_nodes": int(sum(np.prod(s.grid) for s in batch)),
             "particles_range": [min(s.n for s in batch), max(s.n for s in batch)],
             "grid_range": [min(s.grid[0] for s in batch), max(s.grid[0] for s in batch)],
             "tuning": tune, "graphs": True, "flags": flags,
+            "kernels_ms_per_step": {k: v[1] / steps for k, v in kt.items() if v[0]},
             "workload": "uneven_snowballs (seed 0): log-uniform 4k-262k particles, 32^3-128^3 grids, "
                         "E ~ U[5e4,3e5], nu ~ U[0.15,0.3], v0 ~ N(0,1)^3"}
 

@@ -49,6 +49,9 @@ struct DevBufs {
     void* grid_next;   // vec4 per cell: P2G of the next step (fused kernel)
     void* gforce;      // vec4 per cell (stage mode forces)
     uint32_t* flags;
+    uint32_t* bcount;  // particles per 4x4x4 block (the block sums of counts)
+    uint8_t* gmark;       // blocks of grid that hold data (set by every writer)
+    uint8_t* gmark_next;  // the same for grid_next
     // batches: DevParams<T> per scene, first block and first particle of each
     // scene (nscenes + 1 entries, ascending)
     const void* scenes;
@@ -104,11 +107,15 @@ __device__ __forceinline__ bool stencil_in_grid(const DevParams<T>& P, const int
     return b[0] >= 1 && b[1] >= 1 && b[2] >= 1 && b[0] + 2 < P.M[0] && b[1] + 2 < P.M[1] && b[2] + 2 < P.M[2];
 }
 
-// One atomic per distinct key among the active lanes of the warp.
-__device__ __forceinline__ void count_key(uint32_t* counts, uint32_t key) {
-    const uint32_t peers = __match_any_sync(__activemask(), key);
-    const int leader = __ffs(peers) - 1;
-    if ((int)(threadIdx.x & 31) == leader) atomicAdd(counts + key, (uint32_t)__popc(peers));
+// One atomic per distinct key, and one per distinct block, among the active
+// lanes of the warp.
+__device__ __forceinline__ void count_key(uint32_t* counts, uint32_t* bcount, uint32_t key) {
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, key);
+    const int lane = (int)(threadIdx.x & 31);
+    if (lane == __ffs(peers) - 1) atomicAdd(counts + key, (uint32_t)__popc(peers));
+    const uint32_t bpeers = __match_any_sync(active, key / 64u);
+    if (lane == __ffs(bpeers) - 1) atomicAdd(bcount + key / 64u, (uint32_t)__popc(bpeers));
 }
 
 // ---------------------------------------------------------------- sorting
@@ -127,17 +134,19 @@ __global__ void __launch_bounds__(256) k_keys(DevParams<T> P0, DevBufs D, const 
     if (!stencil_in_grid(P, b)) raise_flag(flags, 1u);
     const uint32_t key = sort_key(P, b);
     keys[i] = key;
-    count_key(counts, key);
+    count_key(counts, D.bcount, key);
 }
 
 // Exclusive scan of the per-cell counts into the scatter cursor (the first
 // sorted slot of each cell), emission of the work items and reset of the
 // counts for the next histogram, over kScanTile-key tiles on all SMs:
-// k_tile_sums adds up each tile, k_scan scans one tile (16 whole blocks) per
-// CTA after summing the tiles before it.  A block of c particles becomes
-// ceil(c / wp) work items of nearly equal size; the items are appended to the
-// list through an atomic counter (their order does not matter) and the
-// counter of the next sort is cleared here.
+// k_tile_sums adds up each tile from the block counts, k_scan scans one tile
+// (64 whole blocks) per CTA after summing the tiles before it; only occupied
+// blocks read or write their cells, so empty grid space costs 4 bytes per
+// block.  A block of c particles becomes ceil(c / wp) work items of nearly
+// equal size; the items are appended to the list through an atomic counter
+// (their order does not matter) and the counter of the next sort is cleared
+// here.
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 4;                                 // consecutive keys per thread
 constexpr int kScanTile = kScanThreads * kScanPer;          // keys per CTA
@@ -159,27 +168,22 @@ __device__ __forceinline__ void st4(uint32_t* p, int k0, int nkeys, uint4 v) {
     if (k0 + 2 < nkeys) p[k0 + 2] = v.z;
 }
 
-__global__ void __launch_bounds__(256) k_tile_sums(const uint32_t* __restrict__ counts, int nkeys,
+// Particles per tile from the block counts: a warp per tile of 64 blocks.
+__global__ void __launch_bounds__(256) k_tile_sums(const uint32_t* __restrict__ bcount, int nblocks, int ntiles,
                                                    uint32_t* __restrict__ tile_sums) {
-    __shared__ uint32_t part[8];
-    const int t = blockIdx.x, tid = threadIdx.x;
+    const int t = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (t >= ntiles) return;
+    const int b0 = t * kBlocksPerTile + 2 * lane;
     uint32_t sum = 0;
-    for (int k = t * kScanTile + tid * kScanPer; k < min(nkeys, (t + 1) * kScanTile); k += blockDim.x * kScanPer) {
-        const uint4 v = ld4_or_zero(counts, k, nkeys);
-        sum += v.x + v.y + v.z + v.w;
-    }
+    if (b0 < nblocks) sum += bcount[b0];
+    if (b0 + 1 < nblocks) sum += bcount[b0 + 1];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    if ((tid & 31) == 0) part[tid >> 5] = sum;
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t tot = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += part[w];
-        tile_sums[t] = tot;
-    }
+    if (lane == 0) tile_sums[t] = sum;
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
+                                                       uint32_t* __restrict__ bcount,
                                                        const uint32_t* __restrict__ tile_sums, int nkeys,
                                                        int4* __restrict__ work, uint32_t* __restrict__ nwork,
                                                        uint32_t* __restrict__ nwork_next_sort, uint32_t n_expected,
@@ -205,12 +209,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
     }
     __syncthreads();
     const int k0 = t * kScanTile + tid * kScanPer;
-    const uint4 c = ld4_or_zero(counts, k0, nkeys);
+    // the cell counts of an empty block are zero and its cursor is never read:
+    // only occupied blocks touch their 64 cells
+    const int gblk = k0 / kCellsPerBlock;
+    const uint32_t bsum = gblk * kCellsPerBlock < nkeys ? bcount[gblk] : 0u;
+    const uint4 c = bsum ? ld4_or_zero(counts, k0, nkeys) : make_uint4(0u, 0u, 0u, 0u);
     const uint32_t tc = c.x + c.y + c.z + c.w;
-    // particles of this thread's block: the 16 threads of a block are 16 aligned lanes
-    uint32_t bsum = tc;
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) bsum += __shfl_xor_sync(0xffffffffu, bsum, o);
     if ((tid & (kThreadsPerBlockKeys - 1)) == 0) s_blk[tid / kThreadsPerBlockKeys] = bsum;
     uint32_t ic = tc;
 #pragma unroll
@@ -232,12 +236,16 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
     }
     __syncthreads();
     const uint32_t st0 = s_off + (wid ? s_w[wid - 1] : 0u) + ic - tc;
-    st4(cursor, k0, nkeys, make_uint4(st0, st0 + c.x, st0 + c.x + c.y, st0 + c.x + c.y + c.z));
-    st4(counts, k0, nkeys, make_uint4(0u, 0u, 0u, 0u));
-    // the first thread of each block emits the block's work items
+    if (bsum) {
+        st4(cursor, k0, nkeys, make_uint4(st0, st0 + c.x, st0 + c.x + c.y, st0 + c.x + c.y + c.z));
+        st4(counts, k0, nkeys, make_uint4(0u, 0u, 0u, 0u));
+    }
+    // the first thread of each block emits the block's work items and clears
+    // the block count for the next histogram
     if ((tid & (kThreadsPerBlockKeys - 1)) == 0) {
         const int b = tid / kThreadsPerBlockKeys;
         const uint32_t bc = s_blk[b];
+        if (bc) bcount[gblk] = 0u;
         const uint32_t ni = (bc + wp - 1) / wp;
         if (ni) {
             const uint32_t blk = (uint32_t)(t * kBlocksPerTile + b);
@@ -452,6 +460,72 @@ __device__ __forceinline__ bool cell_of_tile(const DevParams<T>& P, const int or
     const int gx = org[0] + ix, gy = org[1] + iy, gz = org[2] + iz;
     lin = ((size_t)gx * P.M[1] + gy) * P.M[2] + gz;
     return gx >= 0 && gy >= 0 && gz >= 0 && gx < P.M[0] && gy < P.M[1] && gz < P.M[2];
+}
+
+// ---------------------------------------------------------------- grid marks
+// Every kernel that adds to a grid buffer marks the 4x4x4 node blocks it may
+// have written (one byte per block, indexed like the sort blocks), so that
+// k_grid_clear zeroes only those blocks before the buffer is filled again.
+
+// Marks the blocks within one block of block key (a tile of P2G nodes
+// spans at most the neighbouring blocks).
+template <typename T>
+__device__ __forceinline__ void mark_around(const DevParams<T>& P, uint8_t* marks, int gkey) {
+    const int t = threadIdx.x;
+    if (t >= 27) return;
+    const int key = gkey - (int)P.block_base;
+    const int bz = key % P.NB[2], by = (key / P.NB[2]) % P.NB[1], bx = key / (P.NB[1] * P.NB[2]);
+    const int nx = bx + t / 9 - 1, ny = by + (t / 3) % 3 - 1, nz = bz + t % 3 - 1;
+    if (nx < 0 || ny < 0 || nz < 0 || nx >= P.NB[0] || ny >= P.NB[1] || nz >= P.NB[2]) return;
+    marks[P.block_base + (nx * P.NB[1] + ny) * P.NB[2] + nz] = 1;
+}
+
+// Marks the blocks holding nodes b - 1 .. b + 2 (one particle's stencil).
+template <typename T>
+__device__ __forceinline__ void mark_stencil(const DevParams<T>& P, uint8_t* marks, const int b[3]) {
+    int lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = max(b[a] - 1, 0) / kBlk;
+        hi[a] = min(b[a] + 2, P.M[a] - 1) / kBlk;
+    }
+    for (int x = lo[0]; x <= hi[0]; ++x)
+        for (int y = lo[1]; y <= hi[1]; ++y)
+            for (int z = lo[2]; z <= hi[2]; ++z) marks[P.block_base + (x * P.NB[1] + y) * P.NB[2] + z] = 1;
+}
+
+// Zeroes the node blocks marked in marks and clears the marks: a warp looks
+// at 32 blocks, then zeroes each marked one together (two nodes a lane).
+template <typename T, bool BATCH>
+__global__ void __launch_bounds__(256) k_grid_clear(DevParams<T> P0, DevBufs D, vec4<T>* __restrict__ grid0,
+                                                    uint8_t* __restrict__ marks, int nblocks) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int b0 = warp * 32; b0 < nblocks; b0 += nwarps * 32) {
+        const int mine = b0 + lane;
+        const bool m = mine < nblocks && marks[mine] != 0;
+        uint32_t todo = __ballot_sync(0xffffffffu, m);
+        while (todo) {
+            const int l = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int gblk = b0 + l;
+            const DevParams<T>* sp = &P0;
+            if (BATCH) sp = static_cast<const DevParams<T>*>(D.scenes) + scene_of(D.sblock, D.nscenes, (uint32_t)gblk);
+            const int key = gblk - (int)sp->block_base;
+            const int NB1 = sp->NB[1], NB2 = sp->NB[2];
+            const int bz = key % NB2, by = (key / NB2) % NB1, bx = key / (NB1 * NB2);
+            vec4<T>* grid = grid0 + sp->goff;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int node = lane + 32 * k;  // 0..63: x = node / 16, y = (node / 4) % 4, z = node % 4
+                const int gx = bx * kBlk + node / 16, gy = by * kBlk + (node / 4) % 4, gz = bz * kBlk + node % 4;
+                if (gx < sp->M[0] && gy < sp->M[1] && gz < sp->M[2])
+                    grid[((size_t)gx * sp->M[1] + gy) * sp->M[2] + gz] = mk4<T>(T(0), T(0), T(0), T(0));
+            }
+        }
+        if (m) marks[mine] = 0;
+    }
 }
 
 // ---------------------------------------------------------------- P2G
@@ -707,6 +781,7 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
     p2g_tasks<T, MOM, kBlk>(S, count);
     __syncthreads();
     p2g_flush<T, kBlk>(P, S, org, grid);
+    if (MOM) mark_around(P, D.gmark, it.x);
     __syncthreads();
 }
 
@@ -886,7 +961,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             const bool in_space = make_stencil(P, p.x, porg, S2, CA - 1);
             const uint32_t key = sort_key(P, S2.b);
             D.keys_out[s] = key;
-            count_key(D.counts, key);
+            count_key(D.counts, D.bcount, key);
             if (!stencil_in_grid(P, S2.b)) raise_flag(D.flags, 1u);
             T G[9], A[9], mv[3];
             stress_from_split(P, sp, p.Jp, G);
@@ -904,12 +979,14 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             } else {
                 S.p.cellof[j] = 0xff;
                 p2g_direct(P, rec, S2.b, gnext);
+                mark_stencil(P, D.gmark_next, S2.b);
             }
         }
         sort_records<T, CA>(S.p, count);
         p2g_tasks<T, true, CA>(S.p, count);
         __syncthreads();
         p2g_flush<T, CA>(P, S.p, porg, gnext);
+        mark_around(P, D.gmark_next, it.x);
         __syncthreads();
     }
 }

@@ -151,6 +151,8 @@ struct rd_handle {
     uint32_t* keys[2] = {nullptr, nullptr};
     uint32_t* perm = nullptr;
     uint32_t* counts = nullptr;
+    uint32_t* bcount = nullptr;   // particles per block
+    uint8_t* gmark[2] = {nullptr, nullptr};  // blocks of grid[0] / grid[1] holding data
     uint32_t* cursor = nullptr;
     int4* work = nullptr;
     uint32_t* nwork2 = nullptr;  // two item counters: the current sort's and the next's
@@ -286,6 +288,9 @@ template <typename T> DevBufs bufs(rd_handle* h) {
     D.grid_next = h->grid[h->g ^ 1];
     D.gforce = h->gforce;
     D.flags = h->flags;
+    D.bcount = h->bcount;
+    D.gmark = h->gmark[h->g];
+    D.gmark_next = h->gmark[h->g ^ 1];
     D.scenes = h->d_scenes;
     D.sblock = h->d_sblock;
     D.spoff = h->d_spoff;
@@ -362,6 +367,7 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     DevParams<T> P = make_params<T>(h, 0.0, T(0));
     if (!h->keys_valid) {
         RD_TRY(check_cuda(h, cudaMemsetAsync(h->counts, 0, sizeof(uint32_t) * h->nkeys, h->stream), "memset counts"));
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->bcount, 0, sizeof(uint32_t) * h->nblocks, h->stream), "memset counts"));
         long t = tmark_begin(h, RD_KERNEL_KEYS);
         const DevBufs D = bufs<T>(h);
         const vec4<T>* pl = static_cast<const vec4<T>*>(h->pl[h->cur]);
@@ -380,8 +386,10 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     uint32_t* nw = h->nwork2 + (h->nb ^ 1);
     uint32_t* nw_next = h->nwork2 + h->nb;
     long t = tmark_begin(h, RD_KERNEL_SCAN);
-    k_tile_sums<<<ntiles, 256, 0, h->stream>>>(h->counts, h->nkeys, h->tile_sums);
-    k_scan<<<ntiles, kScanThreads, 0, h->stream>>>(h->counts, h->cursor, h->tile_sums, h->nkeys, h->work, nw, nw_next,
+    k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, h->stream>>>(h->bcount, h->nblocks, ntiles,
+                                                                             h->tile_sums);
+    k_scan<<<ntiles, kScanThreads, 0, h->stream>>>(h->counts, h->cursor, h->bcount, h->tile_sums, h->nkeys, h->work,
+                                                nw, nw_next,
                                                 (uint32_t)h->n, (uint32_t)h->work_cap, (uint32_t)work_size<T>(h),
                                                 h->flags, h->d_sblock, (int)h->scenes.size());
     tmark_end(h, t);
@@ -402,6 +410,19 @@ template <typename T> unsigned persistent_grid(const rd_handle* h, int occ) {
     return (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)h->sms * per_sm));
 }
 
+// Zeroes the marked node blocks of grid buffer `which` (k_grid_clear).
+template <typename T> rd_status clear_grid(rd_handle* h, int which) {
+    const DevParams<T> P = make_params<T>(h, 0.0, T(0));
+    DevBufs D = bufs<T>(h);
+    const unsigned nb = (unsigned)std::min<size_t>(blocks_for((size_t)h->nblocks, 256), (size_t)h->sms * 16);
+    vec4<T>* grid = static_cast<vec4<T>*>(h->grid[which]);
+    if (batched(h))
+        k_grid_clear<T, true><<<nb, 256, 0, h->stream>>>(P, D, grid, h->gmark[which], h->nblocks);
+    else
+        k_grid_clear<T, false><<<nb, 256, 0, h->stream>>>(P, D, grid, h->gmark[which], h->nblocks);
+    return launched(h, "k_grid_clear");
+}
+
 template <typename T> rd_status step_fused(rd_handle* h, double dt) {
     const size_t gbytes = h->ncells * sizeof(vec4<T>);
     if (h->n == 0) {
@@ -418,7 +439,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
     long t;
     if (!(h->fgrid_valid && h->fgrid_dt == dt)) {  // P2G of the current state
         t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
-        RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid[h->g], 0, gbytes, h->stream), "memset grid"));
+        RD_TRY(clear_grid<T>(h, h->g));
         tmark_end(h, t);
         DevBufs D = bufs<T>(h);
         t = tmark_begin(h, RD_KERNEL_P2G);
@@ -431,7 +452,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
         RD_TRY(launched(h, "k_p2g"));
     }
     t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
-    RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid[h->g ^ 1], 0, gbytes, h->stream), "memset grid"));
+    RD_TRY(clear_grid<T>(h, h->g ^ 1));
     tmark_end(h, t);
     DevBufs D = bufs<T>(h);
     t = tmark_begin(h, RD_KERNEL_G2P2G);
@@ -666,7 +687,7 @@ template <typename T> rd_status init_volumes_impl(rd_handle* h) {
     RD_TRY(ensure_table<T>(h, h->table_valid ? h->table_dt : 0.0, T(h->table_valid ? h->table_fs : 0.0)));
     if (!h->sorted) RD_TRY(sort_particles<T>(h));
     h->fgrid_valid = false;
-    RD_TRY(check_cuda(h, cudaMemsetAsync(h->grid[h->g], 0, h->ncells * sizeof(vec4<T>), h->stream), "memset grid"));
+    RD_TRY(clear_grid<T>(h, h->g));
     const DevParams<T> P = make_params<T>(h, 0.0, T(1));
     const DevBufs D = bufs<T>(h);
     k_p2g<T, true, false, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
@@ -710,7 +731,8 @@ void release(rd_handle* h) {
         if (e) cudaEventDestroy(e);
     h->ev.clear();
     drop_graphs(h);
-    void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->cursor, h->work,
+    void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->bcount, h->gmark[0],
+                    h->gmark[1], h->cursor, h->work,
                     h->nwork2, h->tile_sums, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
                     h->d_scenes, h->d_sblock, h->d_spoff};
     for (void* p : ptrs)
@@ -826,6 +848,9 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
         {(void**)&h->keys[1], n * 4, true},
         {(void**)&h->perm, n * 4, true},
         {(void**)&h->counts, (size_t)h->nkeys * 4, true},
+        {(void**)&h->bcount, (size_t)h->nblocks * 4, true},
+        {(void**)&h->gmark[0], (size_t)h->nblocks, true},
+        {(void**)&h->gmark[1], (size_t)h->nblocks, true},
         {(void**)&h->cursor, (size_t)h->nkeys * 4, true},
         {(void**)&h->work, h->work_cap * sizeof(int4), true},
         {(void**)&h->nwork2, 8, true},
@@ -859,6 +884,13 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
             return bail(RD_CUDA_ERROR);
     }
     cudaMemsetAsync(h->counts, 0, (size_t)h->nkeys * 4, h->stream);
+    cudaMemsetAsync(h->bcount, 0, (size_t)h->nblocks * 4, h->stream);
+    // both grid buffers start zero and unmarked; from then on only marked
+    // blocks are written and cleared
+    cudaMemsetAsync(h->grid[0], 0, h->ncells * v4, h->stream);
+    cudaMemsetAsync(h->grid[1], 0, h->ncells * v4, h->stream);
+    cudaMemsetAsync(h->gmark[0], 0, (size_t)h->nblocks, h->stream);
+    cudaMemsetAsync(h->gmark[1], 0, (size_t)h->nblocks, h->stream);
     cudaMemsetAsync(h->perm, 0, n * 4, h->stream);  // every entry is a valid index from the start
     cudaMemsetAsync(h->flags, 0, 4, h->stream);
     cudaMemsetAsync(h->nwork2, 0, 8, h->stream);
@@ -1219,6 +1251,7 @@ struct NaScratch {
     uint32_t keys[kNaMaxParticles];
     uint32_t perm[kNaMaxParticles];
     uint32_t counts[kNaMaxKeys];
+    uint32_t bcount[kNaMaxKeys / kCellsPerBlock];
     uint32_t cursor[kNaMaxKeys];
     uint32_t tile_sums[kNaMaxTiles];
     uint32_t nwork[2];
@@ -1228,14 +1261,14 @@ struct NaScratch {
 // Block key and histogram of particles given as device arrays (x: n x 3).
 __global__ void __launch_bounds__(256) k_na_keys(DevParams<float> P, const float* __restrict__ x,
                                                  uint32_t* __restrict__ keys, uint32_t* __restrict__ counts,
-                                                 uint32_t* flags) {
+                                                 uint32_t* __restrict__ bcount, uint32_t* flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.n) return;
     const int b[3] = {base_of(x[3 * i], P.h), base_of(x[3 * i + 1], P.h), base_of(x[3 * i + 2], P.h)};
     if (!stencil_in_grid(P, b)) raise_flag(flags, 1u);
     const uint32_t key = sort_key(P, b);
     keys[i] = key;
-    count_key(counts, key);
+    count_key(counts, bcount, key);
 }
 
 // The rasterize P2G of k_p2g<float, true, false>, reading x, v, B and mass from
@@ -1343,15 +1376,17 @@ extern "C" rd_status rd_rasterize_noalloc(const rd_params* params, const rd_part
     // the scratch keeps the previous call's contents: clear what must start at zero
     if (cudaMemsetAsync(grid_out, 0, (size_t)cells * sizeof(float4), st) != cudaSuccess ||
         cudaMemsetAsync(sc->counts, 0, (size_t)hp.nkeys * sizeof(uint32_t), st) != cudaSuccess ||
+        cudaMemsetAsync(sc->bcount, 0, (size_t)hp.nblocks * sizeof(uint32_t), st) != cudaSuccess ||
         cudaMemsetAsync(sc->nwork, 0, 2 * sizeof(uint32_t) + sizeof(uint32_t), st) != cudaSuccess)
         return RD_CUDA_ERROR;
     if (n > 0) {
         const int ntiles = (hp.nkeys + kScanTile - 1) / kScanTile;
         const uint32_t work_cap = (uint32_t)kNaMaxWork;
         k_na_keys<<<blocks_for(n, 256), 256, 0, st>>>(P, static_cast<const float*>(in->x), sc->keys, sc->counts,
-                                                      &sc->flags);
-        k_tile_sums<<<ntiles, 256, 0, st>>>(sc->counts, hp.nkeys, sc->tile_sums);
-        k_scan<<<ntiles, kScanThreads, 0, st>>>(sc->counts, sc->cursor, sc->tile_sums, hp.nkeys, sc->work, &sc->nwork[0],
+                                                      sc->bcount, &sc->flags);
+        k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, st>>>(sc->bcount, hp.nblocks, ntiles, sc->tile_sums);
+        k_scan<<<ntiles, kScanThreads, 0, st>>>(sc->counts, sc->cursor, sc->bcount, sc->tile_sums, hp.nkeys, sc->work,
+                                                &sc->nwork[0],
                                                 &sc->nwork[1], (uint32_t)n, work_cap, (uint32_t)WorkP<float>::value,
                                                 &sc->flags, nullptr, 1);
         k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(n, sc->keys, sc->cursor, sc->perm);
