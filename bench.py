@@ -62,6 +62,7 @@ def parse_args():
     ap.add_argument("--workload", default="two_balls_1m")
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-baseline", type=int, default=1, help="time the single-core CPU baseline (rank 0, N=1)")
+    ap.add_argument("--adjoint", type=int, default=1, help="measure forward + adjoint on the 65,536-particle cube")
     ap.add_argument("--batch-steps", type=int, default=300,
                     help="timed steps of the batched-forward workload (64 uneven scenes); 0 skips it")
     return ap.parse_args()
@@ -268,6 +269,59 @@ def measure_batched(pkg, local, steps, warmup, plain_value):
                         "E ~ U[5e4,3e5], nu ~ U[0.15,0.3], v0 ~ N(0,1)^3"}
 
 
+def measure_adjoint(pkg, local, reps=3):
+    """Forward + adjoint: the 65,536-particle cube on 64^3 for 50 steps,
+    checkpoint every 10, loss ||centroid(x_T) - (0.55, 0.3, 0.5)||^2, gradients
+    with respect to v0 (per particle), E and nu; against the plain forward of
+    the same 50 steps, both timed on the host clock around synchronised calls
+    (best of `reps`)."""
+    graft.load_package()
+    from rd_gb300 import scenes
+    sc = scenes.cube(seed=0)
+    steps, every = 50, 10
+    target = np.array([0.55, 0.3, 0.5])
+    sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, device=local, **sc.params()))
+
+    def start():
+        sim.set_particles(sc.x, sc.v, sc.mass)
+        sim.init_volumes()
+        sim.synchronize()
+
+    t_fwd, t_fa, t_rec = [], [], []
+    for _ in range(reps + 1):  # the first round warms up
+        start()
+        t0 = time.perf_counter()
+        sim.step(sc.dt, steps)
+        sim.synchronize()
+        t_fwd.append(time.perf_counter() - t0)
+        start()
+        t0 = time.perf_counter()
+        sim.adjoint_record(sc.dt, steps, every)
+        xT = sim.get_particles(("x",))["x"].astype(np.float64)
+        t1 = time.perf_counter()
+        gx = np.tile(2.0 * (xT.mean(0) - target) / sc.n, (sc.n, 1)).astype(np.float32)
+        g = sim.adjoint_backward(gx)
+        t_fa.append(time.perf_counter() - t0)
+        t_rec.append(t1 - t0)
+    # per-kernel split of one forward + adjoint (events around each launch)
+    start()
+    sim.set_kernel_timing(True)
+    sim.adjoint_record(sc.dt, steps, every)
+    xT = sim.get_particles(("x",))["x"].astype(np.float64)
+    sim.adjoint_backward(np.tile(2.0 * (xT.mean(0) - target) / sc.n, (sc.n, 1)).astype(np.float32))
+    kt = sim.kernel_timing()
+    sim.set_kernel_timing(False)
+    sim.close()
+    fwd, fa, rec = min(t_fwd[1:]), min(t_fa[1:]), min(t_rec[1:])
+    return {"value": sc.n * steps / fa, "unit": "particle-steps/s (forward + adjoint)",
+            "ms_forward": fwd * 1e3, "ms_forward_adjoint": fa * 1e3, "ms_record": rec * 1e3,
+            "ratio_vs_forward": fa / fwd, "steps": steps, "checkpoint_every": every,
+            "kernels_ms": {k: v[1] for k, v in kt.items() if v[0]},
+            "grad_v0_norm": float(np.linalg.norm(g["v0"])), "grad_E": float(g["E"][0]), "grad_nu": float(g["nu"][0]),
+            "workload": "cube: 65,536 particles in a 0.2 cube at (0.5, 0.6, 0.5), 64^3, 50 steps, "
+                        "loss ||centroid(x_T) - (0.55, 0.3, 0.5)||^2, FP32"}
+
+
 def run_ours(args):
     import torch
 
@@ -381,6 +435,8 @@ def run_ours(args):
     }
     if args.batch_steps > 0:
         out["batched_forward"] = measure_batched(pkg, local, args.batch_steps, max(args.warmup, 3), value)
+    if args.adjoint:
+        out["forward_adjoint"] = measure_adjoint(pkg, local)
     if rank == 0 and ws == 1 and args.cpu_baseline:
         v, kind, sample = cpu_baseline_single_core(sc)
         out["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": kind, "sample": sample}

@@ -163,7 +163,9 @@ enum {
                                or after the step size changed) */
     RD_KERNEL_G2P2G = 5,    /* grid update + G2P + F update + advection of this step and
                                the P2G (with the MLS force) of the next, fused */
-    RD_KERNEL_COUNT = 6
+    RD_KERNEL_ADJ_G2P = 6,  /* reverse of G2P, advection and the plastic split */
+    RD_KERNEL_ADJ_P2G = 7,  /* reverse of the grid update and of P2G with the stress */
+    RD_KERNEL_COUNT = 8
 };
 /* Per-kernel timing with CUDA events recorded on the handle's stream around
  * each launch of rd_step (profiling runs; off by default).  rd_kernel_timing
@@ -219,6 +221,31 @@ rd_status rd_autotune(rd_handle* h, double dt, int32_t steps, rd_tune_result* re
 /* Sets the pair by hand (0 = default: the largest item, max resident CTAs). */
 rd_status rd_set_tuning(rd_handle* h, int32_t particles_per_item, int32_t ctas_per_sm);
 rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas_per_sm);
+
+/* ---- Reverse mode: gradients of a rollout ----
+ * No counterpart in the reference.  rd_adjoint_record runs `steps` steps of
+ * rd_step from the current state (of every scene of a batch) and keeps a copy
+ * of the state every `checkpoint_every` steps; the handle then holds the final
+ * state.  rd_adjoint_backward takes dL/dx (and optionally dL/dv) of the final
+ * state, n x 3 in original particle order (scene order for a batch), and
+ * returns dL/dv of the recorded start state and, per scene, dL/dE, dL/dnu,
+ * dL/dtheta_c, dL/dtheta_s.  It recomputes each segment from its checkpoint
+ * (memory: the checkpoints plus one segment of states and grids) and runs
+ * hand-written adjoint kernels of every stage per step: advection and the
+ * position clamp, G2P (as a scatter), the plastic SVD split (with the clamp's
+ * subgradient), the grid update and P2G with the fixed-corotated stress (as a
+ * gather).  Volumes and masses are constants; the lagged-B step only
+ * (RD_NOT_SUPPORTED otherwise).  The handle keeps the final state afterwards.
+ * Any call that changes the state in between invalidates the record. */
+typedef struct rd_grads {
+    void* v0;         /* n x 3 element type, or NULL; host or device per `where` */
+    double* E;        /* one per scene, host, or NULL */
+    double* nu;
+    double* theta_c;
+    double* theta_s;
+} rd_grads;
+rd_status rd_adjoint_record(rd_handle* h, double dt, int32_t steps, int32_t checkpoint_every);
+rd_status rd_adjoint_backward(rd_handle* h, const void* grad_x, const void* grad_v, int where, rd_grads* grads);
 
 /* Rasterize without allocating.  No counterpart in the reference: it exists for
  * callers that cannot allocate GPU memory - an engine that has handed the whole

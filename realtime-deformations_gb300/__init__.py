@@ -48,8 +48,8 @@ EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "
            "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_batch_create",
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
-           "rd_rasterize_noalloc")
-KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g")
+           "rd_adjoint_record", "rd_adjoint_backward", "rd_rasterize_noalloc")
+KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g", "adj_g2p", "adj_p2g")
 
 
 def _sources():
@@ -86,6 +86,12 @@ class _Particles(ctypes.Structure):
 
 _LIB = None
 _LIB_LOCK = threading.Lock()
+
+
+class Grads(ctypes.Structure):
+    _fields_ = [("v0", ctypes.c_void_p), ("E", ctypes.POINTER(ctypes.c_double)),
+                ("nu", ctypes.POINTER(ctypes.c_double)), ("theta_c", ctypes.POINTER(ctypes.c_double)),
+                ("theta_s", ctypes.POINTER(ctypes.c_double))]
 
 
 class TuneResult(ctypes.Structure):
@@ -131,6 +137,8 @@ def lib():
             L.rd_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(TuneResult)]
             L.rd_set_tuning.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
             L.rd_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+            L.rd_adjoint_record.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32]
+            L.rd_adjoint_backward.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.POINTER(Grads)]
             L.rd_set_kernel_timing.argtypes = [vp, ctypes.c_int]
             L.rd_kernel_timing.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64),
                                            ctypes.POINTER(ctypes.c_double)]
@@ -312,6 +320,32 @@ class Simulation:
         self._check(lib().rd_launch_count(self._h, ctypes.byref(c)), "rd_launch_count")
         return c.value
 
+    @property
+    def num_scenes(self) -> int:
+        return 1
+
+    def adjoint_record(self, dt: float, steps: int, checkpoint_every: int = 10):
+        """rd_adjoint_record: `steps` steps from the current state, keeping
+        checkpoints for the reverse pass; the handle then holds the final state."""
+        self._check(lib().rd_adjoint_record(self._h, float(dt), int(steps), int(checkpoint_every)),
+                    "rd_adjoint_record")
+
+    def adjoint_backward(self, grad_x, grad_v=None) -> dict:
+        """rd_adjoint_backward: dL/dx (and dL/dv) of the final state, n x 3 in
+        original order -> {"v0": dL/dv of the start state, "E", "nu",
+        "theta_c", "theta_s": one value per scene}."""
+        gx = self._arr(grad_x, (self.n, 3))
+        gv = self._arr(grad_v, (self.n, 3))
+        ns = self.num_scenes
+        out = {"v0": np.zeros((self.n, 3), self.dtype)}
+        for k in ("E", "nu", "theta_c", "theta_s"):
+            out[k] = np.zeros(ns, np.float64)
+        dp = ctypes.POINTER(ctypes.c_double)
+        g = Grads(out["v0"].ctypes.data, *(out[k].ctypes.data_as(dp) for k in ("E", "nu", "theta_c", "theta_s")))
+        self._check(lib().rd_adjoint_backward(self._h, gx.ctypes.data, gv.ctypes.data if gv is not None else None,
+                                              RD_HOST, ctypes.byref(g)), "rd_adjoint_backward")
+        return out
+
     def set_graphs(self, enable: bool):
         self._check(lib().rd_set_graphs(self._h, int(enable)), "rd_set_graphs")
 
@@ -354,6 +388,10 @@ class Batch(Simulation):
 
     @property
     def nscenes(self) -> int:
+        return len(self.scene_params)
+
+    @property
+    def num_scenes(self) -> int:
         return len(self.scene_params)
 
     def set_particles(self, scene, x, v, mass, B=None, FE=None, FP=None, Jp=None, volume=None, sync=True):

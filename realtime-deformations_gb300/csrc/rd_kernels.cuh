@@ -140,10 +140,11 @@ __global__ void __launch_bounds__(256) k_keys(DevParams<T> P0, DevBufs D, const 
 // Exclusive scan of the per-cell counts into the scatter cursor (the first
 // sorted slot of each cell), emission of the work items and reset of the
 // counts for the next histogram, over kScanTile-key tiles on all SMs:
-// k_tile_sums adds up each tile from the block counts, k_scan scans one tile
-// (64 whole blocks) per CTA after summing the tiles before it; only occupied
-// blocks read or write their cells, so empty grid space costs 4 bytes per
-// block.  A block of c particles becomes ceil(c / wp) work items of nearly
+// k_tile_sums adds up each tile from the block counts, k_tile_prefix turns
+// the tile sums into their exclusive prefix (one CTA), and k_scan scans one
+// tile (64 whole blocks) per CTA from its prefix; empty tiles return at once
+// and only occupied blocks read or write their cells, so empty grid space
+// costs 4 bytes per block.  A block of c particles becomes ceil(c / wp) work items of nearly
 // equal size; the items are appended to the list through an atomic counter
 // (their order does not matter) and the counter of the next sort is cleared
 // here.
@@ -182,32 +183,61 @@ __global__ void __launch_bounds__(256) k_tile_sums(const uint32_t* __restrict__ 
     if (lane == 0) tile_sums[t] = sum;
 }
 
+// In place: sums[t] -> sum of sums[0 .. t-1] for t < ntiles, sums[ntiles] =
+// the total (which must be the particle count); also clears the item counter
+// of the next sort.  One CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) k_tile_prefix(uint32_t* __restrict__ sums, int ntiles,
+                                                      uint32_t* __restrict__ nwork_next_sort, uint32_t n_expected,
+                                                      uint32_t* flags) {
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_carry;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) { s_carry = 0u; *nwork_next_sort = 0u; }
+    __syncthreads();
+    for (int base = 0; base < ntiles; base += 1024) {
+        const int t = base + tid;
+        const uint32_t v = t < ntiles ? sums[t] : 0u;
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_w[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t wsum = s_w[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, wsum, o);
+                if (lane >= o) wsum += y;
+            }
+            s_w[lane] = wsum;
+        }
+        __syncthreads();
+        const uint32_t incl = s_carry + (wid ? s_w[wid - 1] : 0u) + x;
+        if (t < ntiles) sums[t] = incl - v;
+        __syncthreads();
+        if (tid == 1023) s_carry = incl;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        sums[ntiles] = s_carry;
+        if (s_carry != n_expected) atomicOr(flags, 4u);
+    }
+}
+
 __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
                                                        uint32_t* __restrict__ bcount,
-                                                       const uint32_t* __restrict__ tile_sums, int nkeys,
+                                                       const uint32_t* __restrict__ tile_pre, int nkeys,
                                                        int4* __restrict__ work, uint32_t* __restrict__ nwork,
-                                                       uint32_t* __restrict__ nwork_next_sort, uint32_t n_expected,
                                                        uint32_t work_cap, uint32_t wp, uint32_t* flags,
                                                        const uint32_t* __restrict__ sblock, int nscenes) {
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_blk[kBlocksPerTile];  // particles per block of this tile
-    __shared__ uint32_t s_off;
     const int t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    // offset of this tile: sum of the tiles before it
-    uint32_t pre = 0;
-    for (int i = tid; i < t; i += blockDim.x) pre += tile_sums[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(0xffffffffu, pre, o);
-    if (lane == 0) s_w[wid] = pre;
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t tot = 0;
-        for (int w = 0; w < kScanThreads / 32; ++w) tot += s_w[w];
-        s_off = tot;
-        if (t == 0) *nwork_next_sort = 0u;
-        if (t == (int)gridDim.x - 1 && tot + tile_sums[t] != n_expected) atomicOr(flags, 4u);
-    }
-    __syncthreads();
+    const uint32_t s_off = tile_pre[t];
+    if (tile_pre[t + 1] == s_off) return;  // no particle in this tile
     const int k0 = t * kScanTile + tid * kScanPer;
     // the cell counts of an empty block are zero and its cursor is never read:
     // only occupied blocks touch their 64 cells
@@ -316,9 +346,8 @@ __device__ __forceinline__ bool make_stencil(const DevParams<T>& P, const T x[3]
 // are formed without cancellation from G = F - I (exact in floating point):
 // J - 1 = tr G + (sum of the principal 2x2 minors of G) + det G.
 template <typename T>
-__device__ __forceinline__ void stress_PFt(const DevParams<T>& P, const T F[9], T Jp, T out[9]) {
-    T U[9], s[3], sm1[3], V[9];
-    svd3_near(F, U, s, sm1, V);
+__device__ __forceinline__ void stress_PFt_svd(const DevParams<T>& P, const T F[9], T Jp, const T U[9], const T s[3],
+                                               const T sm1[3], T out[9]) {
     T G[9];
 #pragma unroll
     for (int e = 0; e < 9; ++e) G[e] = F[e];
@@ -345,6 +374,13 @@ __device__ __forceinline__ void stress_PFt(const DevParams<T>& P, const T F[9], 
         for (int c = 0; c < 3; ++c)
             out[3 * r + c] = U[3 * r] * dg[0] * U[3 * c] + U[3 * r + 1] * dg[1] * U[3 * c + 1] +
                              U[3 * r + 2] * dg[2] * U[3 * c + 2] + (r == c ? iso : T(0));
+}
+
+template <typename T>
+__device__ __forceinline__ void stress_PFt(const DevParams<T>& P, const T F[9], T Jp, T out[9]) {
+    T U[9], s[3], sm1[3], V[9];
+    svd3_near(F, U, s, sm1, V);
+    stress_PFt_svd(P, F, Jp, U, s, sm1, out);
 }
 
 // The clamped split of F_E* = U S V^T that updateDeformationGradient makes,
@@ -495,7 +531,8 @@ __device__ __forceinline__ void mark_stencil(const DevParams<T>& P, uint8_t* mar
 }
 
 // Zeroes the node blocks marked in marks and clears the marks: a warp looks
-// at 32 blocks, then zeroes each marked one together (two nodes a lane).
+// at 32 blocks, each lane finds its block's scene and grid geometry, then the
+// warp zeroes the marked blocks one after the other (two nodes a lane).
 template <typename T, bool BATCH>
 __global__ void __launch_bounds__(256) k_grid_clear(DevParams<T> P0, DevBufs D, vec4<T>* __restrict__ grid0,
                                                     uint8_t* __restrict__ marks, int nblocks) {
@@ -505,23 +542,34 @@ __global__ void __launch_bounds__(256) k_grid_clear(DevParams<T> P0, DevBufs D, 
     for (int b0 = warp * 32; b0 < nblocks; b0 += nwarps * 32) {
         const int mine = b0 + lane;
         const bool m = mine < nblocks && marks[mine] != 0;
+        int key = 0, nb1 = 1, nb2 = 1, m0 = 0, m1 = 0, m2 = 0;
+        unsigned long long goff = 0;
+        if (m) {
+            const DevParams<T>* sp = &P0;
+            if (BATCH)
+                sp = static_cast<const DevParams<T>*>(D.scenes) + scene_of(D.sblock, D.nscenes, (uint32_t)mine);
+            key = mine - (int)sp->block_base;
+            nb1 = sp->NB[1]; nb2 = sp->NB[2];
+            m0 = sp->M[0]; m1 = sp->M[1]; m2 = sp->M[2];
+            goff = sp->goff;
+        }
         uint32_t todo = __ballot_sync(0xffffffffu, m);
         while (todo) {
             const int l = __ffs(todo) - 1;
             todo &= todo - 1;
-            const int gblk = b0 + l;
-            const DevParams<T>* sp = &P0;
-            if (BATCH) sp = static_cast<const DevParams<T>*>(D.scenes) + scene_of(D.sblock, D.nscenes, (uint32_t)gblk);
-            const int key = gblk - (int)sp->block_base;
-            const int NB1 = sp->NB[1], NB2 = sp->NB[2];
-            const int bz = key % NB2, by = (key / NB2) % NB1, bx = key / (NB1 * NB2);
-            vec4<T>* grid = grid0 + sp->goff;
+            const int k = __shfl_sync(0xffffffffu, key, l);
+            const int NB1 = __shfl_sync(0xffffffffu, nb1, l), NB2 = __shfl_sync(0xffffffffu, nb2, l);
+            const int M0 = __shfl_sync(0xffffffffu, m0, l), M1 = __shfl_sync(0xffffffffu, m1, l);
+            const int M2 = __shfl_sync(0xffffffffu, m2, l);
+            const unsigned long long go = __shfl_sync(0xffffffffu, goff, l);
+            const int bz = k % NB2, by = (k / NB2) % NB1, bx = k / (NB1 * NB2);
+            vec4<T>* grid = grid0 + go;
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int node = lane + 32 * k;  // 0..63: x = node / 16, y = (node / 4) % 4, z = node % 4
+            for (int q = 0; q < 2; ++q) {
+                const int node = lane + 32 * q;  // 0..63: x = node / 16, y = (node / 4) % 4, z = node % 4
                 const int gx = bx * kBlk + node / 16, gy = by * kBlk + (node / 4) % 4, gz = bz * kBlk + node % 4;
-                if (gx < sp->M[0] && gy < sp->M[1] && gz < sp->M[2])
-                    grid[((size_t)gx * sp->M[1] + gy) * sp->M[2] + gz] = mk4<T>(T(0), T(0), T(0), T(0));
+                if (gx < M0 && gy < M1 && gz < M2)
+                    grid[((size_t)gx * M1 + gy) * M2 + gz] = mk4<T>(T(0), T(0), T(0), T(0));
             }
         }
         if (m) marks[mine] = 0;

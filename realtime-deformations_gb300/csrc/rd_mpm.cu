@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "rd_adjoint.cuh"
 #include "rd_kernels.cuh"
 #include "../../include/rd_mpm.h"
 
@@ -123,8 +124,43 @@ struct rd_graph {
     uint64_t launches = 0;
 };
 
+// Reverse-mode rollout: checkpoints of the forward states, the per-segment
+// stores of the recomputed states and grids, and the adjoint buffers.
+struct rd_adjoint_data {
+    bool recorded = false;
+    uint64_t version = 0;  // handle version the record belongs to
+    double dt = 0.0;
+    int steps = 0, every = 0;
+    size_t state_bytes = 0, grid_bytes = 0;
+    size_t nckpt = 0, nseg = 0;         // capacities (states)
+    void* ckpt = nullptr;               // nckpt states
+    void* sstore = nullptr;             // nseg states
+    void* gstore = nullptr;             // nseg grids (m, p) of those states
+    uint32_t* sperm = nullptr;          // nseg sorted permutations of those states
+    int4* swork = nullptr;              // nseg work lists
+    uint32_t* snwork = nullptr;         // nseg work-item counts
+    int occ_g2p = 1, occ_p2g = 1;       // resident CTAs per SM of the reverse kernels
+    bool tail_valid = false;            // the store holds the last segment of the record
+    // the reverse sweep captured as one CUDA graph, for one start assignment
+    // of the ping-pong buffers and one record shape
+    cudaGraphExec_t sweep = nullptr;
+    int sweep_key = -1, sweep_end = 0, sweep_steps = 0, sweep_every = 0, sweep_wp = 0, sweep_mult = 0;
+    double sweep_dt = 0.0;
+    uint64_t sweep_launches = 0;
+    void* final_state = nullptr;
+    // adjoints in slot order, 25 n reals each (x 3n | v 3n | B 9n | F 9n | J_P n):
+    // [0], [1] the states either side of the step being reversed, [2] the
+    // partials of the first reverse kernel (and staging at both ends)
+    void* adj[3] = {nullptr, nullptr, nullptr};
+    void* agrid = nullptr;
+    double* pacc = nullptr;             // 4 per particle slot
+    double* acc = nullptr;              // 4 per scene
+};
+
 struct rd_handle {
     rd_params prm{};                    // scene 0's (precision, device, flags for all)
+    uint64_t version = 0;               // bumped by every public call that changes the state
+    rd_adjoint_data adj;
     std::vector<rd_scene_info> scenes;  // one, or a batch
     void* d_scenes = nullptr;           // DevParams<T> per scene (batches)
     uint32_t* d_sblock = nullptr;       // first block of each scene, then the total
@@ -388,12 +424,12 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     long t = tmark_begin(h, RD_KERNEL_SCAN);
     k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, h->stream>>>(h->bcount, h->nblocks, ntiles,
                                                                              h->tile_sums);
+    k_tile_prefix<<<1, 1024, 0, h->stream>>>(h->tile_sums, ntiles, nw_next, (uint32_t)h->n, h->flags);
     k_scan<<<ntiles, kScanThreads, 0, h->stream>>>(h->counts, h->cursor, h->bcount, h->tile_sums, h->nkeys, h->work,
-                                                nw, nw_next,
-                                                (uint32_t)h->n, (uint32_t)h->work_cap, (uint32_t)work_size<T>(h),
-                                                h->flags, h->d_sblock, (int)h->scenes.size());
+                                                nw, (uint32_t)h->work_cap, (uint32_t)work_size<T>(h), h->flags,
+                                                h->d_sblock, (int)h->scenes.size());
     tmark_end(h, t);
-    RD_TRY(launched(h, "k_scan", 2));
+    RD_TRY(launched(h, "k_scan", 3));
     h->nb ^= 1;
     t = tmark_begin(h, RD_KERNEL_SCATTER);
     k_scatter<<<blocks_for(h->n, 256), 256, 0, h->stream>>>(h->n, h->keys[h->cur], h->cursor, h->perm);
@@ -724,6 +760,9 @@ void drop_graphs(rd_handle* h) {
     for (rd_graph& g : h->graphs)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     h->graphs.clear();
+    if (h->adj.sweep) cudaGraphExecDestroy(h->adj.sweep);
+    h->adj.sweep = nullptr;
+    h->adj.sweep_key = -1;
 }
 
 void release(rd_handle* h) {
@@ -731,6 +770,11 @@ void release(rd_handle* h) {
         if (e) cudaEventDestroy(e);
     h->ev.clear();
     drop_graphs(h);
+    rd_adjoint_data& a = h->adj;
+    void* aptrs[] = {a.ckpt, a.sstore, a.gstore, a.sperm, a.swork, a.snwork, a.final_state, a.adj[0], a.adj[1], a.adj[2],
+                     a.agrid, a.pacc, a.acc};
+    for (void* p : aptrs)
+        if (p) cudaFree(p);
     void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->bcount, h->gmark[0],
                     h->gmark[1], h->cursor, h->work,
                     h->nwork2, h->tile_sums, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
@@ -854,7 +898,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
         {(void**)&h->cursor, (size_t)h->nkeys * 4, true},
         {(void**)&h->work, h->work_cap * sizeof(int4), true},
         {(void**)&h->nwork2, 8, true},
-        {(void**)&h->tile_sums, (size_t)((h->nkeys + kScanTile - 1) / kScanTile) * 4, true},
+        {(void**)&h->tile_sums, (size_t)((h->nkeys + kScanTile - 1) / kScanTile + 1) * 4, true},
         {&h->grid[0], h->ncells * v4, true},
         {&h->grid[1], h->ncells * v4, true},
         {&h->gforce, h->ncells * v4, !batch},  // stage mode only
@@ -1028,6 +1072,296 @@ template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps
     return cleanup(st);
 }
 
+// ---------------------------------------------------------------- adjoint
+template <typename T> rd_status adj_occupancy(rd_handle* h) {
+    const int sg = (int)sizeof(AdjG2PShared<T>), sp = (int)sizeof(AdjP2GShared<T>);
+    const void* g2p[] = {(const void*)k_adj_g2p<T, false>, (const void*)k_adj_g2p<T, true>};
+    const void* p2g[] = {(const void*)k_adj_p2g<T, false>, (const void*)k_adj_p2g<T, true>};
+    for (const void* f : g2p)
+        RD_TRY(check_cuda(h, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sg), "smem attr"));
+    for (const void* f : p2g)
+        RD_TRY(check_cuda(h, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sp), "smem attr"));
+    int o = 0;
+    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_adj_g2p<T, false>, kAdjThreads, sg), "occ"));
+    h->adj.occ_g2p = std::max(1, o);
+    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_adj_p2g<T, false>, kAdjThreads, sp), "occ"));
+    h->adj.occ_p2g = std::max(1, o);
+    return RD_OK;
+}
+
+rd_status adj_alloc(rd_handle* h, int steps, int every) {
+    rd_adjoint_data& a = h->adj;
+    const size_t n = std::max<size_t>(1, (size_t)h->n);
+    a.state_bytes = (size_t)h->planes * n * 4 * h->esize;
+    a.grid_bytes = h->ncells * 4 * h->esize;
+    const size_t nckpt = (size_t)((steps + every - 1) / every), nseg = (size_t)every;
+    auto grow = [&](void** ptr, size_t bytes) -> rd_status {
+        drop_graphs(h);  // a captured sweep holds the old pointers
+        if (*ptr) cudaFree(*ptr);
+        *ptr = nullptr;
+        return check_cuda(h, cudaMalloc(ptr, bytes), "adjoint buffers");
+    };
+    if (a.nckpt < nckpt) {
+        RD_TRY(grow(&a.ckpt, nckpt * a.state_bytes));
+        a.nckpt = nckpt;
+    }
+    if (a.nseg < nseg) {
+        RD_TRY(grow(&a.sstore, nseg * a.state_bytes));
+        RD_TRY(grow(&a.gstore, nseg * a.grid_bytes));
+        RD_TRY(grow((void**)&a.sperm, nseg * n * sizeof(uint32_t)));
+        RD_TRY(grow((void**)&a.swork, nseg * h->work_cap * sizeof(int4)));
+        RD_TRY(grow((void**)&a.snwork, nseg * sizeof(uint32_t)));
+        a.nseg = nseg;
+    }
+    if (!a.final_state) {
+        RD_TRY(check_cuda(h, cudaMalloc(&a.final_state, a.state_bytes), "adjoint buffers"));
+        for (int k = 0; k < 3; ++k) RD_TRY(check_cuda(h, cudaMalloc(&a.adj[k], 25 * n * h->esize), "adjoint buffers"));
+        RD_TRY(check_cuda(h, cudaMalloc(&a.agrid, a.grid_bytes), "adjoint buffers"));
+        RD_TRY(check_cuda(h, cudaMalloc((void**)&a.pacc, kAccPerScene * n * sizeof(double)), "adjoint buffers"));
+        RD_TRY(check_cuda(h, cudaMalloc((void**)&a.acc, kAccPerScene * h->scenes.size() * sizeof(double)),
+                          "adjoint buffers"));
+        RD_TRY(h->prm.precision == RD_FP64 ? adj_occupancy<double>(h) : adj_occupancy<float>(h));
+    }
+    return RD_OK;
+}
+
+inline char* at(void* base, size_t i, size_t bytes) { return static_cast<char*>(base) + i * bytes; }
+
+// One forward step that keeps, in slot j of the segment store, the state it
+// starts from, the grid it reads and the sort of that state.
+template <typename T> rd_status stored_step(rd_handle* h, double dt, int j) {
+    rd_adjoint_data& a = h->adj;
+    const size_t n = (size_t)h->n;
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(at(a.sstore, (size_t)j, a.state_bytes), h->pl[h->cur], a.state_bytes,
+                                         cudaMemcpyDeviceToDevice, h->stream),
+                      "segment state"));
+    RD_TRY(step_fused<T>(h, dt));
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(at(a.gstore, (size_t)j, a.grid_bytes), h->grid[h->g ^ 1], a.grid_bytes,
+                                         cudaMemcpyDeviceToDevice, h->stream),
+                      "segment grid"));
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(a.sperm + (size_t)j * n, h->perm, n * sizeof(uint32_t),
+                                         cudaMemcpyDeviceToDevice, h->stream),
+                      "segment sort"));
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(a.swork + (size_t)j * h->work_cap, h->work, h->work_cap * sizeof(int4),
+                                         cudaMemcpyDeviceToDevice, h->stream),
+                      "segment sort"));
+    return check_cuda(h, cudaMemcpyAsync(a.snwork + j, h->nwork2 + h->nb, sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                                         h->stream),
+                      "segment sort");
+}
+
+template <typename T> rd_status adjoint_record_impl(rd_handle* h, double dt, int steps, int every) {
+    RD_TRY(adj_alloc(h, steps, every));
+    rd_adjoint_data& a = h->adj;
+    a.recorded = false;
+    a.tail_valid = false;
+    for (int s = 0; s < steps; s += every) {
+        RD_TRY(check_cuda(h, cudaMemcpyAsync(at(a.ckpt, (size_t)(s / every), a.state_bytes), h->pl[h->cur],
+                                             a.state_bytes, cudaMemcpyDeviceToDevice, h->stream),
+                          "checkpoint"));
+        const int len = std::min(every, steps - s);
+        if (s + every >= steps && h->n > 0) {  // the last segment goes straight into the store
+            for (int j = 0; j < len; ++j) RD_TRY(stored_step<T>(h, dt, j));
+            a.tail_valid = true;
+        } else {
+            RD_TRY(steps_impl<T>(h, dt, len));
+        }
+    }
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(a.final_state, h->pl[h->cur], a.state_bytes, cudaMemcpyDeviceToDevice,
+                                         h->stream),
+                      "final state"));
+    a.recorded = true;
+    a.dt = dt;
+    a.steps = steps;
+    a.every = every;
+    a.version = h->version;
+    return RD_OK;
+}
+
+template <typename T> AdjState<T> adj_view(rd_handle* h, int k) {
+    T* base = static_cast<T*>(h->adj.adj[k]);
+    const size_t n = (size_t)h->n;
+    return AdjState<T>{base, base + 3 * n, base + 6 * n, base + 15 * n, base + 24 * n};
+}
+
+// Puts the handle's state back to `src` (a stored state) for the next step.
+rd_status load_state(rd_handle* h, const void* src, size_t bytes) {
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(h->pl[h->cur], src, bytes, cudaMemcpyDeviceToDevice, h->stream), "restore"));
+    h->keys_valid = false;
+    h->sorted = false;
+    h->fgrid_valid = false;
+    h->grid_mode = GRID_NONE;
+    return RD_OK;
+}
+
+// The reverse sweep over all segments, last to first; nxt is the adjoint
+// buffer holding the adjoint of the final state on entry.  Ends with the
+// final state back in the handle.  Enqueues work only (capturable).
+template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
+    rd_adjoint_data& a = h->adj;
+    const size_t n = (size_t)h->n;
+    const double dt = a.dt;
+    const bool batch = batched(h);
+    const int nseg = (a.steps + a.every - 1) / a.every;
+    for (int seg = nseg - 1; seg >= 0 && n; --seg) {
+        const int c = seg * a.every, len = std::min(a.every, a.steps - c);
+        if (!(seg == nseg - 1 && a.tail_valid)) {  // recompute the segment into the store
+            RD_TRY(load_state(h, at(a.ckpt, (size_t)seg, a.state_bytes), a.state_bytes));
+            for (int j = 0; j < len; ++j) RD_TRY(stored_step<T>(h, dt, j));
+        }
+        // the handle now holds the state after the segment, in this pass's slot
+        // order: bring the adjoint of that state into the same order
+        const vec4<T>* after = static_cast<const vec4<T>*>(h->pl[h->cur]);
+        const unsigned nb256 = blocks_for(n, 256);
+        if (seg == nseg - 1) {  // dL/dx, dL/dv of the final state (staged in adj[2] by id)
+            const AdjState<T> S = adj_view<T>(h, 2);
+            k_adj_seed<T><<<nb256, 256, 0, h->stream>>>((int)n, after, S.x, S.v, adj_view<T>(h, nxt));
+            RD_TRY(launched(h, "k_adj_seed"));
+        } else {  // from the order of the next segment's checkpoint
+            const vec4<T>* ck = reinterpret_cast<const vec4<T>*>(at(a.ckpt, (size_t)seg + 1, a.state_bytes));
+            k_adj_to_id<T><<<nb256, 256, 0, h->stream>>>((int)n, ck, adj_view<T>(h, nxt), adj_view<T>(h, 2));
+            k_adj_from_id<T><<<nb256, 256, 0, h->stream>>>((int)n, after, adj_view<T>(h, 2), adj_view<T>(h, nxt));
+            RD_TRY(launched(h, "k_adj_remap", 2));
+        }
+        const DevParams<T> P = make_params<T>(h, dt, (T)dt);
+        const size_t max_items = n / WorkP<T>::value + std::min<size_t>((size_t)h->nblocks, n) + 1;
+        const unsigned gg = (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)h->sms * a.occ_g2p));
+        const unsigned gp = (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)h->sms * a.occ_p2g));
+        const size_t sg = sizeof(AdjG2PShared<T>), sp = sizeof(AdjP2GShared<T>);
+        for (int j = len - 1; j >= 0; --j) {
+            const int cur = nxt ^ 1;
+            const vec4<T>* st = reinterpret_cast<const vec4<T>*>(at(a.sstore, (size_t)j, a.state_bytes));
+            const vec4<T>* gr = reinterpret_cast<const vec4<T>*>(at(a.gstore, (size_t)j, a.grid_bytes));
+            vec4<T>* ag = static_cast<vec4<T>*>(a.agrid);
+            DevBufs D = bufs<T>(h);
+            D.perm = a.sperm + (size_t)j * n;
+            D.work = a.swork + (size_t)j * h->work_cap;
+            D.nwork = a.snwork + j;
+            RD_TRY(check_cuda(h, cudaMemsetAsync(a.agrid, 0, a.grid_bytes, h->stream), "adjoint grid"));
+            const AdjState<T> An = adj_view<T>(h, nxt), Ap = adj_view<T>(h, 2), Ac = adj_view<T>(h, cur);
+            long t = tmark_begin(h, RD_KERNEL_ADJ_G2P);
+            if (batch)
+                k_adj_g2p<T, true><<<gg, kAdjThreads, sg, h->stream>>>(P, D, st, gr, ag, An, Ap, a.pacc);
+            else
+                k_adj_g2p<T, false><<<gg, kAdjThreads, sg, h->stream>>>(P, D, st, gr, ag, An, Ap, a.pacc);
+            tmark_end(h, t);
+            t = tmark_begin(h, RD_KERNEL_ADJ_P2G);
+            if (batch)
+                k_adj_p2g<T, true><<<gp, kAdjThreads, sp, h->stream>>>(P, D, st, gr, ag, Ap, Ac, a.pacc);
+            else
+                k_adj_p2g<T, false><<<gp, kAdjThreads, sp, h->stream>>>(P, D, st, gr, ag, Ap, Ac, a.pacc);
+            tmark_end(h, t);
+            RD_TRY(launched(h, "adjoint step", 2));
+            nxt = cur;
+        }
+    }
+    return load_state(h, a.final_state, a.state_bytes);
+}
+
+// adjoint_sweep through a cached CUDA graph (captured on first use).  The
+// ping-pong assignment the sweep ends in is part of the cache entry.
+template <typename T> rd_status sweep_graph(rd_handle* h) {
+    rd_adjoint_data& a = h->adj;
+    const int key = (h->cur | (h->g << 1) | (h->nb << 2)) + (a.tail_valid ? 8 : 0);
+    const bool hit = a.sweep && a.sweep_key == key && a.sweep_dt == a.dt && a.sweep_steps == a.steps &&
+                     a.sweep_every == a.every && a.sweep_wp == h->wp && a.sweep_mult == h->grid_mult;
+    if (!hit) {
+        if (a.sweep) cudaGraphExecDestroy(a.sweep);
+        a.sweep = nullptr;
+        const uint64_t l0 = h->launches;
+        RD_TRY(check_cuda(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture"));
+        const rd_status st = adjoint_sweep<T>(h, 1);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        if (st != RD_OK || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return st != RD_OK ? st : check_cuda(h, e, "end capture");
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&a.sweep, graph, 0);
+        cudaGraphDestroy(graph);
+        RD_TRY(check_cuda(h, ie, "graph instantiate"));
+        a.sweep_key = key;
+        a.sweep_end = h->cur | (h->g << 1) | (h->nb << 2);
+        a.sweep_dt = a.dt;
+        a.sweep_steps = a.steps;
+        a.sweep_every = a.every;
+        a.sweep_wp = h->wp;
+        a.sweep_mult = h->grid_mult;
+        a.sweep_launches = h->launches - l0;
+    } else {
+        // the host-side state the sweep leaves behind
+        h->cur = a.sweep_end & 1;
+        h->g = (a.sweep_end >> 1) & 1;
+        h->nb = (a.sweep_end >> 2) & 1;
+        h->launches += a.sweep_launches;
+        h->keys_valid = false;
+        h->sorted = false;
+        h->fgrid_valid = false;
+        h->grid_mode = GRID_NONE;
+        h->last_dt = a.dt;
+    }
+    return check_cuda(h, cudaGraphLaunch(a.sweep, h->stream), "graph launch");
+}
+
+template <typename T>
+rd_status adjoint_backward_impl(rd_handle* h, const void* grad_x, const void* grad_v, int where, rd_grads* out) {
+    rd_adjoint_data& a = h->adj;
+    const size_t n = (size_t)h->n;
+    const bool batch = batched(h);
+    const cudaMemcpyKind kin = where == RD_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    int nxt = 1;
+    if (n) {  // dL/dx, dL/dv of the final state by particle id, staged for the sweep's seed
+        const AdjState<T> S = adj_view<T>(h, 2);
+        if (grad_x) RD_TRY(check_cuda(h, cudaMemcpyAsync(S.x, grad_x, 3 * n * sizeof(T), kin, h->stream), "adjoint seed"));
+        else RD_TRY(check_cuda(h, cudaMemsetAsync(S.x, 0, 3 * n * sizeof(T), h->stream), "adjoint seed"));
+        if (grad_v) RD_TRY(check_cuda(h, cudaMemcpyAsync(S.v, grad_v, 3 * n * sizeof(T), kin, h->stream), "adjoint seed"));
+        else RD_TRY(check_cuda(h, cudaMemsetAsync(S.v, 0, 3 * n * sizeof(T), h->stream), "adjoint seed"));
+    }
+    RD_TRY(check_cuda(h, cudaMemsetAsync(a.pacc, 0, kAccPerScene * std::max<size_t>(n, 1) * sizeof(double), h->stream),
+                      "adjoint acc"));
+    if (n) {
+        if (h->use_graphs && !h->timing)
+            RD_TRY(sweep_graph<T>(h));
+        else
+            RD_TRY(adjoint_sweep<T>(h, 1));
+        // the store now holds the first segment unless there was only one
+        a.tail_valid = a.tail_valid && a.steps <= a.every;
+    }
+    nxt = 1 ^ (a.steps & 1);  // the buffer the sweep left the start state's adjoint in
+    k_reduce_acc<<<(unsigned)h->scenes.size(), 256, 0, h->stream>>>(a.pacc, batch ? h->d_spoff : nullptr,
+                                                                   (int)h->scenes.size(), h->n, a.acc);
+    RD_TRY(launched(h, "k_reduce_acc"));
+    if (out && out->v0 && n) {  // dL/dv of the start state (checkpoint 0) in particle id order
+        T* dst = where == RD_HOST ? adj_view<T>(h, 2).v : static_cast<T*>(out->v0);
+        k_adj_out<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, static_cast<const vec4<T>*>(a.ckpt),
+                                                                 adj_view<T>(h, nxt), dst);
+        RD_TRY(launched(h, "k_adj_out"));
+        if (where == RD_HOST)
+            RD_TRY(check_cuda(h, cudaMemcpyAsync(out->v0, dst, 3 * n * sizeof(T), cudaMemcpyDeviceToHost, h->stream),
+                              "v0 gradient"));
+    }
+    std::vector<double> acc(kAccPerScene * h->scenes.size());
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(acc.data(), a.acc, acc.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                         h->stream),
+                      "parameter gradients"));
+    if (!n) RD_TRY(load_state(h, a.final_state, a.state_bytes));
+    RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "sync"));
+    if (out) {
+        for (size_t s = 0; s < h->scenes.size(); ++s) {
+            const double E = h->scenes[s].prm.E, nu = h->scenes[s].prm.nu;
+            const double mub = acc[kAccPerScene * s], lamb = acc[kAccPerScene * s + 1];
+            const double den = (1.0 + nu) * (1.0 - 2.0 * nu);
+            // mu0 = E / (2 (1 + nu)), lambda0 = E nu / ((1 + nu)(1 - 2 nu))
+            if (out->E) out->E[s] = mub / (2.0 * (1.0 + nu)) + lamb * nu / den;
+            if (out->nu) out->nu[s] = -mub * E / (2.0 * (1.0 + nu) * (1.0 + nu)) + lamb * E * (1.0 + 2.0 * nu * nu) / (den * den);
+            if (out->theta_c) out->theta_c[s] = acc[kAccPerScene * s + 2];
+            if (out->theta_s) out->theta_s[s] = acc[kAccPerScene * s + 3];
+        }
+    }
+    return RD_OK;
+}
+
 bool all_set(const rd_handle* h) {
     for (const rd_scene_info& sc : h->scenes)
         if (!sc.set && sc.n > 0) return false;
@@ -1064,6 +1398,7 @@ rd_status rd_destroy(rd_handle* h) {
 rd_status rd_batch_set_particles(rd_handle* h, int32_t scene, const rd_particles* in, int where) {
     if (!h || !in || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
     if (scene < 0 || scene >= (int32_t)h->scenes.size()) return fail(h, RD_INVALID_ARG, "no such scene");
+    ++h->version;
     cudaSetDevice(h->prm.device);
     return RD_DISPATCH(h, set_particles_impl, h, scene, in, where);
 }
@@ -1087,6 +1422,7 @@ rd_status rd_batch_step(rd_handle* h, double dt, int32_t nsteps) { return rd_ste
 rd_status rd_set_particles(rd_handle* h, const rd_particles* in, int where) {
     if (!h || !in || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
     if (batched(h)) return fail(h, RD_INVALID_ARG, "a batch takes its particles per scene (rd_batch_set_particles)");
+    ++h->version;
     cudaSetDevice(h->prm.device);
     return RD_DISPATCH(h, set_particles_impl, h, 0, in, where);
 }
@@ -1101,6 +1437,7 @@ rd_status rd_get_particles(rd_handle* h, rd_particles* out, int where) {
 rd_status rd_init_volumes(rd_handle* h) {
     if (!h) return RD_INVALID_ARG;
     if (!all_set(h)) return fail(h, RD_INVALID_ARG, "every scene needs its particles first");
+    ++h->version;
     cudaSetDevice(h->prm.device);
     return RD_DISPATCH(h, init_volumes_impl, h);
 }
@@ -1108,6 +1445,7 @@ rd_status rd_init_volumes(rd_handle* h) {
 rd_status rd_step(rd_handle* h, double dt, int32_t nsteps) {
     if (!h || nsteps < 0 || !std::isfinite(dt)) return RD_INVALID_ARG;
     if (!all_set(h)) return fail(h, RD_INVALID_ARG, "every scene needs its particles first");
+    ++h->version;
     cudaSetDevice(h->prm.device);
     return RD_DISPATCH(h, steps_impl, h, dt, nsteps);
 }
@@ -1115,6 +1453,7 @@ rd_status rd_step(rd_handle* h, double dt, int32_t nsteps) {
 rd_status rd_autotune(rd_handle* h, double dt, int32_t steps, rd_tune_result* result) {
     if (!h || !result || steps < 1 || !std::isfinite(dt)) return RD_INVALID_ARG;
     if (!all_set(h)) return fail(h, RD_INVALID_ARG, "every scene needs its particles first");
+    ++h->version;
     cudaSetDevice(h->prm.device);
     return RD_DISPATCH(h, autotune_impl, h, dt, steps, result);
 }
@@ -1139,6 +1478,23 @@ rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas
     return RD_OK;
 }
 
+rd_status rd_adjoint_record(rd_handle* h, double dt, int32_t steps, int32_t checkpoint_every) {
+    if (!h || steps < 1 || checkpoint_every < 1 || !std::isfinite(dt)) return RD_INVALID_ARG;
+    if (!h->prm.lagged_b) return fail(h, RD_NOT_SUPPORTED, "the adjoint follows the reference's lagged-B step");
+    if (!all_set(h)) return fail(h, RD_INVALID_ARG, "every scene needs its particles first");
+    cudaSetDevice(h->prm.device);
+    ++h->version;
+    return RD_DISPATCH(h, adjoint_record_impl, h, dt, steps, checkpoint_every);
+}
+
+rd_status rd_adjoint_backward(rd_handle* h, const void* grad_x, const void* grad_v, int where, rd_grads* grads) {
+    if (!h || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
+    if (!h->adj.recorded || h->adj.version != h->version)
+        return fail(h, RD_INVALID_ARG, "no adjoint record of the current state (rd_adjoint_record)");
+    cudaSetDevice(h->prm.device);
+    return RD_DISPATCH(h, adjoint_backward_impl, h, grad_x, grad_v, where, grads);
+}
+
 rd_status rd_set_graphs(rd_handle* h, int enable) {
     if (!h) return RD_INVALID_ARG;
     cudaSetDevice(h->prm.device);
@@ -1149,6 +1505,7 @@ rd_status rd_set_graphs(rd_handle* h, int enable) {
 
 rd_status rd_stage(rd_handle* h, int32_t stage, double dt) {
     if (!h || !std::isfinite(dt)) return RD_INVALID_ARG;
+    ++h->version;
     cudaSetDevice(h->prm.device);
     return RD_DISPATCH(h, stage_impl, h, stage, dt);
 }
@@ -1253,7 +1610,7 @@ struct NaScratch {
     uint32_t counts[kNaMaxKeys];
     uint32_t bcount[kNaMaxKeys / kCellsPerBlock];
     uint32_t cursor[kNaMaxKeys];
-    uint32_t tile_sums[kNaMaxTiles];
+    uint32_t tile_sums[kNaMaxTiles + 1];
     uint32_t nwork[2];
     uint32_t flags;
 };
@@ -1385,10 +1742,10 @@ extern "C" rd_status rd_rasterize_noalloc(const rd_params* params, const rd_part
         k_na_keys<<<blocks_for(n, 256), 256, 0, st>>>(P, static_cast<const float*>(in->x), sc->keys, sc->counts,
                                                       sc->bcount, &sc->flags);
         k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, st>>>(sc->bcount, hp.nblocks, ntiles, sc->tile_sums);
+        k_tile_prefix<<<1, 1024, 0, st>>>(sc->tile_sums, ntiles, &sc->nwork[1], (uint32_t)n, &sc->flags);
         k_scan<<<ntiles, kScanThreads, 0, st>>>(sc->counts, sc->cursor, sc->bcount, sc->tile_sums, hp.nkeys, sc->work,
-                                                &sc->nwork[0],
-                                                &sc->nwork[1], (uint32_t)n, work_cap, (uint32_t)WorkP<float>::value,
-                                                &sc->flags, nullptr, 1);
+                                                &sc->nwork[0], work_cap, (uint32_t)WorkP<float>::value, &sc->flags,
+                                                nullptr, 1);
         k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(n, sc->keys, sc->cursor, sc->perm);
         const size_t max_items = (size_t)n / WorkP<float>::value + (size_t)std::min<int64_t>(nblocks, n) + 1;
         const unsigned grid = (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)nd.sms * nd.occ));

@@ -95,8 +95,8 @@ def test_graph_replay_matches_eager_launches(built_pkg):
         s.step(sc.dt, 3)
         l0 = s.launch_count()
         s.step(sc.dt, 10)
-        # steady steps: tile sums, scan, scatter, grid clear and the fused kernel
-        assert s.launch_count() - l0 == 50
+        # steady steps: tile sums, tile prefix, scan, scatter, grid clear and the fused kernel
+        assert s.launch_count() - l0 == 60
         out.append(s.get_particles())
     for k in ("x", "v", "FE", "Jp"):
         assert rel(out[0][k], out[1][k]) < 1e-5
