@@ -322,6 +322,68 @@ def measure_adjoint(pkg, local, reps=3):
                         "loss ||centroid(x_T) - (0.55, 0.3, 0.5)||^2, FP32"}
 
 
+def measure_batched_adjoint(pkg, local):
+    """Batched forward + adjoint: 32 snowballs of log-uniform 16k-131k particles
+    on 64^3-96^3 grids, 100 steps, checkpoint every 10; per-scene loss = mean
+    squared position error against a target rollout run at E = 2e5,
+    theta = (2e-2, 5e-3); gradients w.r.t. each scene's E, theta_c, theta_s.
+    Host-clock time of record + backward against the batched forward of the
+    same steps."""
+    graft.load_package()
+    from rd_gb300 import scenes
+    batch = scenes.uneven_snowballs(seed=1, nscenes=32, n_lo=16384, n_hi=131072, g_lo=64, g_hi=96, steps=100)
+    steps, every, dt = 100, 10, batch[0].dt
+
+    def make(**over):
+        b = pkg.Batch([pkg.make_params(*s.grid, s.n, s.h, device=local, **s.params(**over)) for s in batch])
+        for i, s in enumerate(batch):
+            b.set_particles(i, s.x, s.v, s.mass)
+        b.init_volumes()
+        return b
+
+    tgt = make(E=2e5, theta_c=2e-2, theta_s=5e-3)
+    tgt.step(dt, steps)
+    xt = [tgt.get_particles(i, ("x",))["x"].astype(np.float64) for i in range(len(batch))]
+    tgt.close()
+    b = make()
+    t_fwd, t_fa = [], []
+    g = None
+    for _ in range(3):  # the first round warms up
+        for i, s in enumerate(batch):
+            b.set_particles(i, s.x, s.v, s.mass)
+        b.init_volumes()
+        b.synchronize()
+        t0 = time.perf_counter()
+        b.step(dt, steps)
+        b.synchronize()
+        t_fwd.append(time.perf_counter() - t0)
+        for i, s in enumerate(batch):
+            b.set_particles(i, s.x, s.v, s.mass)
+        b.init_volumes()
+        b.synchronize()
+        t0 = time.perf_counter()
+        b.adjoint_record(dt, steps, every)
+        gx, loss = [], []
+        for i, s in enumerate(batch):
+            x = b.get_particles(i, ("x",))["x"].astype(np.float64)
+            loss.append(float(np.mean(np.sum((x - xt[i]) ** 2, axis=1))))
+            gx.append((2.0 * (x - xt[i]) / s.n).astype(np.float32))
+        g = b.adjoint_backward(np.concatenate(gx))
+        t_fa.append(time.perf_counter() - t0)
+    n = b.n
+    b.close()
+    fwd, fa = min(t_fwd[1:]), min(t_fa[1:])
+    return {"value": n * steps / fa, "unit": "particle-steps/s (forward + adjoint)", "ms_forward": fwd * 1e3,
+            "ms_forward_adjoint": fa * 1e3, "ratio_vs_forward": fa / fwd, "scenes": len(batch), "particles": n,
+            "steps": steps, "checkpoint_every": every, "loss_mean": float(np.mean(loss)),
+            "grad_E_range": [float(np.min(g["E"])), float(np.max(g["E"]))],
+            "grad_theta_c_range": [float(np.min(g["theta_c"])), float(np.max(g["theta_c"]))],
+            "grad_theta_s_range": [float(np.min(g["theta_s"])), float(np.max(g["theta_s"]))],
+            "finite": bool(all(np.all(np.isfinite(g[k])) for k in ("v0", "E", "theta_c", "theta_s"))),
+            "workload": "uneven_snowballs (seed 1): 32 scenes, log-uniform 16k-131k particles, 64^3-96^3, "
+                        "target rollout at E = 2e5, theta = (2e-2, 5e-3), FP32"}
+
+
 def run_ours(args):
     import torch
 
@@ -437,6 +499,7 @@ def run_ours(args):
         out["batched_forward"] = measure_batched(pkg, local, args.batch_steps, max(args.warmup, 3), value)
     if args.adjoint:
         out["forward_adjoint"] = measure_adjoint(pkg, local)
+        out["batched_forward_adjoint"] = measure_batched_adjoint(pkg, local)
     if rank == 0 and ws == 1 and args.cpu_baseline:
         v, kind, sample = cpu_baseline_single_core(sc)
         out["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": kind, "sample": sample}

@@ -714,31 +714,72 @@ __device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int count) {
     const int k0 = (int)(((long long)total * warp) / nwarps), k1 = (int)(((long long)total * (warp + 1)) / nwarps);
     const T* recs = reinterpret_cast<const T*>(S.rec);
     int cur = -1;
-    T am[2] = {T(0), T(0)}, aq[2][3] = {{T(0), T(0), T(0)}, {T(0), T(0), T(0)}};
-    for (int k = k0; k < k1; ++k) {
-        const int j = S.order[k];
-        const int c = S.cellof[j];
-        if (c != cur) {
-            if (cur >= 0) p2g_flush_lane<T, CA>(S, cur, ox, oy, oz0, am, aq, MOM);
-            cur = c;
-            am[0] = am[1] = T(0);
-            aq[0][0] = aq[0][1] = aq[0][2] = aq[1][0] = aq[1][1] = aq[1][2] = T(0);
+    if constexpr (sizeof(T) == 4) {
+        // FP32: the lane's two nodes (z offsets oz0 and oz0 + 2) as float2
+        // pairs, two FMAs per instruction
+        const float2 fzz = make_float2(fz, fz + 2.f);
+        float2 am2 = make_float2(0.f, 0.f), qx2 = am2, qy2 = am2, qz2 = am2;
+        for (int k = k0; k < k1; ++k) {
+            const int j = S.order[k];
+            const int c = S.cellof[j];
+            if (c != cur) {
+                if (cur >= 0) {
+                    const T am[2] = {am2.x, am2.y};
+                    const T aq[2][3] = {{qx2.x, qy2.x, qz2.x}, {qx2.y, qy2.y, qz2.y}};
+                    p2g_flush_lane<T, CA>(S, cur, ox, oy, oz0, am, aq, MOM);
+                }
+                cur = c;
+                am2 = qx2 = qy2 = qz2 = make_float2(0.f, 0.f);
+            }
+            const T* rs = recs + j * (4 * kRecV4);
+            const float wxy = rs[ox] * rs[4 + oy];
+            const float2 w = __fmul2_rn(make_float2(wxy, wxy), make_float2(rs[8 + oz0], rs[10 + oz0]));
+            const vec4<T>* r = &S.rec[j * kRecV4];
+            const vec4<T> qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
+            // q' + h A o: the x and y offsets are common to both nodes
+            const float cx = qm.x + a4.x * fx + a4.w * fy;
+            const float cy = qm.y + a4.y * fx + b4.x * fy;
+            const float cz = qm.z + a4.z * fx + b4.y * fy;
+            const float2 px = __ffma2_rn(make_float2(b4.z, b4.z), fzz, make_float2(cx, cx));
+            const float2 py = __ffma2_rn(make_float2(b4.w, b4.w), fzz, make_float2(cy, cy));
+            const float2 pz = __ffma2_rn(make_float2(c4.x, c4.x), fzz, make_float2(cz, cz));
+            if (MOM) am2 = __ffma2_rn(w, make_float2(qm.w, qm.w), am2);
+            qx2 = __ffma2_rn(w, px, qx2);
+            qy2 = __ffma2_rn(w, py, qy2);
+            qz2 = __ffma2_rn(w, pz, qz2);
         }
-        const T* rs = recs + j * (4 * kRecV4);
-        const T wxy = rs[ox] * rs[4 + oy];
-        const T w0 = wxy * rs[8 + oz0], w1 = wxy * rs[10 + oz0];
-        const vec4<T>* r = &S.rec[j * kRecV4];
-        const vec4<T> qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
-        // q' + h A o; h A columns x (a4.x, a4.y, a4.z), y (a4.w, b4.x, b4.y), z (b4.z, b4.w, c4.x)
-        const T q0x = qm.x + a4.x * fx + a4.w * fy + b4.z * fz;
-        const T q0y = qm.y + a4.y * fx + b4.x * fy + b4.w * fz;
-        const T q0z = qm.z + a4.z * fx + b4.y * fy + c4.x * fz;
-        const T q1x = q0x + T(2) * b4.z, q1y = q0y + T(2) * b4.w, q1z = q0z + T(2) * c4.x;
-        if (MOM) { am[0] += w0 * qm.w; am[1] += w1 * qm.w; }
-        aq[0][0] += w0 * q0x; aq[0][1] += w0 * q0y; aq[0][2] += w0 * q0z;
-        aq[1][0] += w1 * q1x; aq[1][1] += w1 * q1y; aq[1][2] += w1 * q1z;
+        if (cur >= 0) {
+            const T am[2] = {am2.x, am2.y};
+            const T aq[2][3] = {{qx2.x, qy2.x, qz2.x}, {qx2.y, qy2.y, qz2.y}};
+            p2g_flush_lane<T, CA>(S, cur, ox, oy, oz0, am, aq, MOM);
+        }
+    } else {
+        T am[2] = {T(0), T(0)}, aq[2][3] = {{T(0), T(0), T(0)}, {T(0), T(0), T(0)}};
+        for (int k = k0; k < k1; ++k) {
+            const int j = S.order[k];
+            const int c = S.cellof[j];
+            if (c != cur) {
+                if (cur >= 0) p2g_flush_lane<T, CA>(S, cur, ox, oy, oz0, am, aq, MOM);
+                cur = c;
+                am[0] = am[1] = T(0);
+                aq[0][0] = aq[0][1] = aq[0][2] = aq[1][0] = aq[1][1] = aq[1][2] = T(0);
+            }
+            const T* rs = recs + j * (4 * kRecV4);
+            const T wxy = rs[ox] * rs[4 + oy];
+            const T w0 = wxy * rs[8 + oz0], w1 = wxy * rs[10 + oz0];
+            const vec4<T>* r = &S.rec[j * kRecV4];
+            const vec4<T> qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
+            // q' + h A o; h A columns x (a4.x, a4.y, a4.z), y (a4.w, b4.x, b4.y), z (b4.z, b4.w, c4.x)
+            const T q0x = qm.x + a4.x * fx + a4.w * fy + b4.z * fz;
+            const T q0y = qm.y + a4.y * fx + b4.x * fy + b4.w * fz;
+            const T q0z = qm.z + a4.z * fx + b4.y * fy + c4.x * fz;
+            const T q1x = q0x + T(2) * b4.z, q1y = q0y + T(2) * b4.w, q1z = q0z + T(2) * c4.x;
+            if (MOM) { am[0] += w0 * qm.w; am[1] += w1 * qm.w; }
+            aq[0][0] += w0 * q0x; aq[0][1] += w0 * q0y; aq[0][2] += w0 * q0z;
+            aq[1][0] += w1 * q1x; aq[1][1] += w1 * q1y; aq[1][2] += w1 * q1z;
+        }
+        if (cur >= 0) p2g_flush_lane<T, CA>(S, cur, ox, oy, oz0, am, aq, MOM);
     }
-    if (cur >= 0) p2g_flush_lane<T, CA>(S, cur, ox, oy, oz0, am, aq, MOM);
 }
 
 // Adds the tile (origin org) to the grid: one vector reduction per node that
