@@ -613,6 +613,7 @@ template <typename T, int CA> struct P2GTile {
     int off[NC];
     uint16_t order[WorkP<T>::value];
     uint8_t cellof[WorkP<T>::value];
+    uint8_t scell[WorkP<T>::value];  // cell of each sorted slot
 };
 
 template <typename T> __device__ __forceinline__ T pick4(const vec4<T>& v, int i) {
@@ -674,7 +675,11 @@ __device__ __forceinline__ void sort_records(P2GTile<T, CA>& S, int count) {
     __syncthreads();
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         const int c = S.cellof[j];
-        if (c != 0xff) S.order[atomicAdd(&S.cnt[c], 1)] = (uint16_t)j;
+        if (c != 0xff) {
+            const int k = atomicAdd(&S.cnt[c], 1);
+            S.order[k] = (uint16_t)j;
+            S.scell[k] = (uint8_t)c;
+        }
     }
     __syncthreads();
     for (int c = threadIdx.x; c < NC; c += blockDim.x) S.cnt[c] -= S.off[c];
@@ -721,7 +726,7 @@ __device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int count) {
         float2 am2 = make_float2(0.f, 0.f), qx2 = am2, qy2 = am2, qz2 = am2;
         for (int k = k0; k < k1; ++k) {
             const int j = S.order[k];
-            const int c = S.cellof[j];
+            const int c = S.scell[k];
             if (c != cur) {
                 if (cur >= 0) {
                     const T am[2] = {am2.x, am2.y};
