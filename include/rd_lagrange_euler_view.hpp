@@ -168,9 +168,30 @@ public:
     void computeParticleVolumesAndDensities() { stage(RD_STAGE_VOLUMES, 0.0); }
     void computeExplicitGridForces() { stage(RD_STAGE_FORCES, 0.0); }
     void gridVelocitiesUpdate(float timeDelta) { stage(RD_STAGE_GRID_VELOCITIES, timeDelta); }
+    // material_point_method.cpp:264-304.  The colliders are the reference's
+    // MeshColliders (or anything with mesh.translation, mesh.rotation (w, x, y, z),
+    // mesh.scale and velocity); they are uploaded when they changed since the
+    // last call, and rd_step applies the last set too.
     template <typename Colliders>
     void gridBasedCollisions(float timeDelta, const Colliders& objects) {
-        if (!objects.empty()) throw rd::Error(RD_NOT_SUPPORTED, "SDF colliders are not part of this path");
+        std::vector<rd_collider> cs;
+        for (const auto& o : objects) {
+            rd_collider c{};
+            for (int a = 0; a < 3; ++a) {
+                c.translation[a] = o.mesh.translation[a];
+                c.scale[a] = o.mesh.scale[a];
+                c.velocity[a] = o.velocity[a];
+            }
+            c.rotation[0] = o.mesh.rotation.w; c.rotation[1] = o.mesh.rotation.x;
+            c.rotation[2] = o.mesh.rotation.y; c.rotation[3] = o.mesh.rotation.z;
+            cs.push_back(c);
+        }
+        if (cs.size() != colliders_.size() ||
+            (!cs.empty() && std::memcmp(cs.data(), colliders_.data(), cs.size() * sizeof(rd_collider)) != 0)) {
+            check(rd_set_colliders(sim_, cs.data(), static_cast<int32_t>(cs.size()), RD_COLLIDE_REFERENCE, 0.5),
+                  "rd_set_colliders");
+            colliders_ = cs;
+        }
         stage(RD_STAGE_COLLISIONS, timeDelta);
     }
     void updateDeformationGradient(float timeDelta) { stage(RD_STAGE_DEFORMATION, timeDelta); }
@@ -248,6 +269,7 @@ private:
     rd_handle* sim_ = nullptr;
     std::vector<Particle> particles_;
     std::vector<float> host_;
+    std::vector<rd_collider> colliders_;
     bool dirty_host_ = false;
 };
 

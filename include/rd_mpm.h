@@ -176,6 +176,36 @@ rd_status rd_kernel_timing(rd_handle* h, int kernel, uint64_t* launches, double*
 /* Number of kernel launches issued by this handle so far. */
 rd_status rd_launch_count(rd_handle* h, uint64_t* count);
 
+/* ---- Box colliders (gridBasedCollisions, material_point_method.cpp:264-304) ----
+ * The reference's MeshCollider (material_point_method.hpp:74-93) as main.cpp
+ * builds it (main.cpp:119-160): a box mesh spanning [-1, 1]^3 placed by
+ * matrixWorld = T R S, with a rigid velocity.  Its signed distance is
+ * max_i(|p_i| - s_i) in the box frame p = R^T (x - t).  The grid update applies
+ * them in order to every node with mass: where the distance is <= 0 and the
+ * velocity relative to the box points inwards (v_n = v_rel . n < 0), the
+ * relative velocity becomes its tangential part with friction mu = `friction`
+ * (0.5 in the reference):
+ *   RD_COLLIDE_REFERENCE  as the reference computes it: n = central
+ *       differences of the distance with step 0.001 (mathy.hpp:40-56), and
+ *       v_t (1 + mu v_n / 3), sticking only when -mu v_n >= 3 - the reference
+ *       divides by glm's vec3::length(), which is the component count 3;
+ *   RD_COLLIDE_COULOMB    the Coulomb law it intends: n the outward face
+ *       normal, v_t (1 + mu v_n / |v_t|), sticking when |v_t| <= -mu v_n.
+ * Single-scene handles; up to RD_MAX_COLLIDERS. */
+#define RD_MAX_COLLIDERS 16
+enum { RD_COLLIDE_REFERENCE = 0, RD_COLLIDE_COULOMB = 1 };
+typedef struct rd_collider {
+    double translation[3]; /* t: the box centre (mesh.translation) */
+    double rotation[4];    /* R as a unit quaternion (w, x, y, z) (mesh.rotation) */
+    double scale[3];       /* s: the half extents (mesh.scale) */
+    double velocity[3];    /* MeshCollider::velocity */
+} rd_collider;
+/* Replaces the handle's colliders (count 0 removes them). */
+rd_status rd_set_colliders(rd_handle* h, const rd_collider* colliders, int32_t count, int32_t mode, double friction);
+/* MeshCollider::move (material_point_method.hpp:89-91) for every collider:
+ * t += dt * velocity.  main.cpp:188 calls it once per frame. */
+rd_status rd_move_colliders(rd_handle* h, double dt);
+
 /* ---- Batches: many independent scenes stepped together ----
  * No counterpart in the reference, which simulates one LagrangeEulerView per
  * process.  scenes[s] describes scene s exactly as rd_create's params do (its

@@ -365,6 +365,104 @@ void orc_grid_velocities(const orc_params* P, real dt, orc_grid* G) {
             }
 }
 
+/* Box colliders of gridBasedCollisions (material_point_method.cpp:264-304),
+ * the MeshCollider of material_point_method.hpp:74-93: per collider the
+ * world-from-box rotation R (row-major), the centre t, the half extents s and
+ * the velocity v.  Mode 0 follows the reference (finite-difference normal,
+ * glm's vec3::length() = 3 in the friction law), mode 1 the Coulomb law with
+ * the face normal. */
+#define ORC_MAX_COLLIDERS 16
+static int orc_ncol = 0, orc_col_mode = 0;
+static double orc_mu = 0.5;
+static double orc_cols[ORC_MAX_COLLIDERS][18]; /* R 9 | t 3 | s 3 | v 3 */
+
+/* spec: per collider t (3), unit quaternion (w, x, y, z), s (3), v (3). */
+void orc_set_colliders(int n, const double* spec, int mode, double mu) {
+    orc_ncol = n < 0 ? 0 : (n > ORC_MAX_COLLIDERS ? ORC_MAX_COLLIDERS : n);
+    orc_col_mode = mode;
+    orc_mu = mu;
+    for (int k = 0; k < orc_ncol; ++k) {
+        const double* c = spec + 13 * k;
+        double w = c[3], x = c[4], y = c[5], z = c[6];
+        const double nn = sqrt(w * w + x * x + y * y + z * z);
+        if (nn > 0) { w /= nn; x /= nn; y /= nn; z /= nn; }
+        double* o = orc_cols[k];
+        o[0] = 1 - 2 * (y * y + z * z); o[1] = 2 * (x * y - w * z);     o[2] = 2 * (x * z + w * y);
+        o[3] = 2 * (x * y + w * z);     o[4] = 1 - 2 * (x * x + z * z); o[5] = 2 * (y * z - w * x);
+        o[6] = 2 * (x * z - w * y);     o[7] = 2 * (y * z + w * x);     o[8] = 1 - 2 * (x * x + y * y);
+        for (int a = 0; a < 3; ++a) { o[9 + a] = c[a]; o[12 + a] = c[7 + a]; o[15 + a] = c[10 + a]; }
+    }
+}
+
+/* MeshCollider::move (material_point_method.hpp:89-91) */
+void orc_move_colliders(double dt) {
+    for (int k = 0; k < orc_ncol; ++k)
+        for (int a = 0; a < 3; ++a) orc_cols[k][9 + a] += dt * orc_cols[k][15 + a];
+}
+
+/* MeshCollider::sdf: |max(q, 0)| + min(max(q), 0) with q = |R^T (x - t)| - s. */
+static real box_sdf(const double* c, real x0, real x1, real x2) {
+    const real d[3] = {x0 - (real)c[9], x1 - (real)c[10], x2 - (real)c[11]};
+    real q[3];
+    for (int a = 0; a < 3; ++a) {
+        const real p = (real)c[a] * d[0] + (real)c[3 + a] * d[1] + (real)c[6 + a] * d[2];
+        q[a] = (real)fabs((double)p) - (real)c[12 + a];
+    }
+    real qm = q[0];
+    if (q[1] > qm) qm = q[1];
+    if (q[2] > qm) qm = q[2];
+    return (real)fabs((double)(qm > 0 ? qm : (real)0)) + (qm < 0 ? qm : (real)0);
+}
+
+/* gridBasedCollisions / bodyCollision on every node with mass. */
+void orc_collisions(const orc_params* P, orc_grid* G) {
+    if (!orc_ncol) return;
+    const real h = (real)P->h, mu = (real)orc_mu;
+    for (int i = 0; i < P->mi; ++i)
+        for (int j = 0; j < P->mj; ++j)
+            for (int k = 0; k < P->mk; ++k) {
+                const size_t cc = cidx(P, i, j, k);
+                if (G->mass[cc] == (real)0) continue;
+                const real x[3] = {(real)i * h, (real)j * h, (real)k * h};
+                real* v = G->vel + 3 * cc;
+                for (int o = 0; o < orc_ncol; ++o) {
+                    const double* c = orc_cols[o];
+                    if (box_sdf(c, x[0], x[1], x[2]) > 0) continue;
+                    real n[3];
+                    if (orc_col_mode == 0) { /* gradient(phi, pos, 3), delta 0.001 (mathy.hpp:40-56) */
+                        const real dl = (real)0.001f;
+                        for (int a = 0; a < 3; ++a) {
+                            real xp[3] = {x[0], x[1], x[2]}, xm[3] = {x[0], x[1], x[2]};
+                            xp[a] += dl;
+                            xm[a] -= dl;
+                            n[a] = (box_sdf(c, xp[0], xp[1], xp[2]) - box_sdf(c, xm[0], xm[1], xm[2])) / ((real)2 * dl);
+                        }
+                    } else { /* outward normal of the face of largest q */
+                        const real d[3] = {x[0] - (real)c[9], x[1] - (real)c[10], x[2] - (real)c[11]};
+                        real p[3], q[3];
+                        for (int a = 0; a < 3; ++a) {
+                            p[a] = (real)c[a] * d[0] + (real)c[3 + a] * d[1] + (real)c[6 + a] * d[2];
+                            q[a] = (real)fabs((double)p[a]) - (real)c[12 + a];
+                        }
+                        int f = 0;
+                        if (q[1] > q[f]) f = 1;
+                        if (q[2] > q[f]) f = 2;
+                        const real sg = p[f] < 0 ? (real)-1 : (real)1;
+                        for (int a = 0; a < 3; ++a) n[a] = sg * (real)c[3 * a + f];
+                    }
+                    const real rel[3] = {v[0] - (real)c[15], v[1] - (real)c[16], v[2] - (real)c[17]};
+                    const real vn = rel[0] * n[0] + rel[1] * n[1] + rel[2] * n[2];
+                    if (vn >= 0) continue;
+                    const real vt[3] = {rel[0] - n[0] * vn, rel[1] - n[1] * vn, rel[2] - n[2] * vn};
+                    const real len = orc_col_mode == 0 ? (real)3
+                                                       : (real)sqrt((double)(vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2]));
+                    real f = 0;
+                    if (len > -mu * vn && len > 0) f = (real)1 + mu * vn / len;
+                    for (int a = 0; a < 3; ++a) v[a] = vt[a] * f + (real)c[15 + a];
+                }
+            }
+}
+
 /* updateDeformationGradient (material_point_method.cpp:306-330):
  * Fhat = (I + dt B D^-1) F_E F_P; F_E* = Fhat F_P^-1 = W S Z^T;
  * F_E <- W clamp(S, 1 - theta_c, 1 + theta_s) Z^T; F_P <- F_E^-1 Fhat.
@@ -450,13 +548,14 @@ void orc_init(const orc_params* P, orc_state* S, orc_grid* G) {
     orc_volumes(P, S, G);
 }
 
-/* main.cpp:192-218 with an empty collider list; lagged_c = 0 swaps the F update
- * after G2P (the textbook order). */
+/* main.cpp:192-218 with the colliders of orc_set_colliders (none by default);
+ * lagged_c = 0 swaps the F update after G2P (the textbook order). */
 void orc_step(const orc_params* P, real dt, int nsteps, orc_state* S, orc_grid* G) {
     for (int s = 0; s < nsteps; ++s) {
         orc_rasterize(P, S, G);
         orc_forces(P, S, G);
         orc_grid_velocities(P, dt, G);
+        orc_collisions(P, G);
         if (P->lagged_c) {
             orc_update_F(P, dt, S);
             orc_g2p(P, S, G);

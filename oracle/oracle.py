@@ -126,6 +126,9 @@ def _lib(dtype):
         lib.orc_init.argtypes = [P, S, G]
         lib.orc_step.argtypes = [P, rt, ctypes.c_int, S, G]
         lib.orc_svd3.argtypes = [ctypes.c_void_p] * 4
+        lib.orc_set_colliders.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_double]
+        lib.orc_move_colliders.argtypes = [ctypes.c_double]
+        lib.orc_collisions.argtypes = [P, G]
         lib.orc_weight.argtypes = [rt]
         lib.orc_weight.restype = rt
         _LIBS[key] = lib
@@ -184,12 +187,23 @@ class OracleSim:
          "volumes": lambda: L.orc_volumes(cp, cs, cg),
          "forces": lambda: L.orc_forces(cp, cs, cg),
          "grid_velocities": lambda: L.orc_grid_velocities(cp, dt, cg),
+         "collisions": lambda: L.orc_collisions(cp, cg),
          "update_F": lambda: L.orc_update_F(cp, dt, cs),
          "g2p": lambda: L.orc_g2p(cp, cs, cg),
          "advect": lambda: L.orc_advect(cp, dt, cs)}[name]()
 
     def step(self, dt: float, nsteps: int = 1):
         self.lib.orc_step(ctypes.byref(self._cp), dt, nsteps, ctypes.byref(self._cs), ctypes.byref(self._cg))
+
+    def set_colliders(self, colliders, mode: int = 0, mu: float = 0.5):
+        """Box colliders (orc_set_colliders; one set per oracle library, shared
+        by every OracleSim of this precision)."""
+        spec = collider_spec(colliders)
+        self.lib.orc_set_colliders(len(colliders), spec.ctypes.data if len(colliders) else None, mode, mu)
+        self._spec = spec
+
+    def move_colliders(self, dt: float):
+        self.lib.orc_move_colliders(dt)
 
     @property
     def C(self):
@@ -198,6 +212,14 @@ class OracleSim:
     @property
     def Jp(self):
         return np.linalg.det(self.FP.reshape(-1, 3, 3).astype(np.float64))
+
+
+def collider_spec(colliders) -> np.ndarray:
+    """Flat float64 array, 13 per collider: translation (3), rotation as a
+    unit quaternion (w, x, y, z), scale (half extents, 3), velocity (3)."""
+    rows = [list(c["translation"]) + list(c["rotation"]) + list(c["scale"]) + list(c.get("velocity", (0, 0, 0)))
+            for c in colliders]
+    return np.ascontiguousarray(np.asarray(rows, np.float64).reshape(-1))
 
 
 def svd3(F: np.ndarray):
@@ -233,6 +255,8 @@ class RefSim:
             L.rdref_step.argtypes = [vp, ctypes.c_float, ctypes.c_int]
             L.rdref_get_mass.argtypes = [vp, ctypes.c_void_p]
             L.rdref_initialize_particles.argtypes = [vp, ctypes.c_uint] + [ctypes.c_float] * 6
+            L.rdref_set_colliders.argtypes = [ctypes.c_int, ctypes.c_void_p]
+            L.rdref_move_colliders.argtypes = [ctypes.c_float]
             cls._lib = L
         return cls._lib
 
@@ -254,6 +278,15 @@ class RefSim:
                    f32(FE, (self.n, 9)), f32(FP, (self.n, 9)), f32(vol, (self.n,))]
             L.rdref_set_particles(self.h, *[None if a is None else a.ctypes.data for a in ins])
         self.p4 = p4
+
+    def set_colliders(self, colliders):
+        """The reference's own MeshColliders for the collision stage (one list
+        per process, shared by every RefSim)."""
+        spec = collider_spec(colliders)
+        self.lib().rdref_set_colliders(len(colliders), spec.ctypes.data if len(colliders) else None)
+
+    def move_colliders(self, dt: float):
+        self.lib().rdref_move_colliders(dt)
 
     def initialize_particles(self, origin, velocity, seed: int = 1):
         """The reference's initializeParticles (material_point_method.cpp:18-63)."""

@@ -1,7 +1,8 @@
 // Headless C harness around the reference's own MaterialPointMethod::
 // LagrangeEulerView (material_point_method.hpp:174-233).  Test infrastructure:
 // it drives the unmodified step methods in the order main.cpp:192-218 calls
-// them, with an empty collider list, and copies state in and out.
+// them, with the reference's own MeshCollider boxes (none unless set), and
+// copies state in and out.
 //
 // Exchange layout: x, v are n x 3; B, FE, FP are n x 9 row-major in the math
 // sense (M[3*r + c] = M(r, c)); glm stores m[c][r] = M(r, c) (column-major).
@@ -10,6 +11,7 @@
 #include "material_point_method.hpp"
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 float rd_ref_E = 1.4e5f;
@@ -27,6 +29,16 @@ void cuP2G(MaterialPointMethod::Particle*, MaterialPointMethod::Cell*, int, int,
 void Mesh::draw() {}
 
 using MaterialPointMethod::LagrangeEulerView;
+using MaterialPointMethod::MeshCollider;
+
+namespace {
+// MeshCollider's sdf captures `this`: the objects live here (stable
+// addresses) and the list passed to gridBasedCollisions holds copies whose
+// sdf still reads these objects' meshes, as main.cpp's solidObjects does.
+std::vector<std::unique_ptr<MeshCollider>> g_objects;
+std::vector<MeshCollider> g_colliders;
+glm::mat4 g_vp(1.0f);
+}  // namespace
 
 namespace {
 inline void to_glm(glm::mat3& g, const float* m) {
@@ -121,12 +133,12 @@ void rdref_get_grid(void* p, float* mass, float* vel, float* force) {
 // 5 = particle velocities, 6 = positions, 7 = volumes (main.cpp:54).
 void rdref_stage(void* p, int stage, float dt) {
     auto* s = static_cast<LagrangeEulerView*>(p);
-    static const std::vector<MaterialPointMethod::MeshCollider> none;
+
     switch (stage) {
         case 0: s->rasterizeParticlesToGrid(); break;
         case 1: s->computeExplicitGridForces(); break;
         case 2: s->gridVelocitiesUpdate(dt); break;
-        case 3: s->gridBasedCollisions(dt, none); break;
+        case 3: s->gridBasedCollisions(dt, g_colliders); break;
         case 4: s->updateDeformationGradient(dt); break;
         case 5: s->updateParticleVelocities(); break;
         case 6: s->updateParticlePositions(dt); break;
@@ -141,6 +153,30 @@ void rdref_stage(void* p, int stage, float dt) {
 void rdref_initialize_particles(void* p, unsigned seed, float ox, float oy, float oz, float vx, float vy, float vz) {
     srand(seed);
     static_cast<LagrangeEulerView*>(p)->initializeParticles(glm::vec3(ox, oy, oz), glm::vec3(vx, vy, vz));
+}
+
+// Box colliders placed as main.cpp:119-160 places them: applyMatrix4(T R S)
+// on a box mesh, with a velocity.  spec: 13 doubles per box, translation (3),
+// rotation quaternion (w, x, y, z), scale (3), velocity (3).
+void rdref_set_colliders(int n, const double* spec) {
+    g_colliders.clear();
+    g_objects.clear();
+    for (int k = 0; k < n; ++k) {
+        const double* c = spec + 13 * k;
+        auto obj = std::make_unique<MeshCollider>(0u, g_vp, std::vector<GLfloat>{}, std::vector<GLfloat>{},
+                                                  glm::vec3((float)c[10], (float)c[11], (float)c[12]));
+        const glm::quat q((float)c[3], (float)c[4], (float)c[5], (float)c[6]);
+        obj->mesh.applyMatrix4(glm::translate(glm::mat4(), glm::vec3((float)c[0], (float)c[1], (float)c[2])) *
+                               glm::toMat4(q) *
+                               glm::scale(glm::mat4(), glm::vec3((float)c[7], (float)c[8], (float)c[9])));
+        g_objects.push_back(std::move(obj));
+    }
+    for (auto& o : g_objects) g_colliders.push_back(*o);
+}
+
+// main.cpp:188: box.move(delta) for every box.
+void rdref_move_colliders(float dt) {
+    for (auto& o : g_objects) o->move(dt);
 }
 
 // main.cpp:53-54

@@ -48,7 +48,8 @@ EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "
            "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_batch_create",
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
-           "rd_adjoint_record", "rd_adjoint_backward", "rd_rasterize_noalloc")
+           "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
+           "rd_rasterize_noalloc")
 KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g", "adj_g2p", "adj_p2g")
 
 
@@ -86,6 +87,15 @@ class _Particles(ctypes.Structure):
 
 _LIB = None
 _LIB_LOCK = threading.Lock()
+
+
+RD_COLLIDE_REFERENCE, RD_COLLIDE_COULOMB = 0, 1
+
+
+class Collider(ctypes.Structure):
+    """rd_collider: a box mesh spanning [-1, 1]^3 placed by T R S, with a velocity."""
+    _fields_ = [("translation", ctypes.c_double * 3), ("rotation", ctypes.c_double * 4),
+                ("scale", ctypes.c_double * 3), ("velocity", ctypes.c_double * 3)]
 
 
 class Grads(ctypes.Structure):
@@ -137,6 +147,8 @@ def lib():
             L.rd_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(TuneResult)]
             L.rd_set_tuning.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
             L.rd_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+            L.rd_set_colliders.argtypes = [vp, ctypes.POINTER(Collider), ctypes.c_int32, ctypes.c_int32, ctypes.c_double]
+            L.rd_move_colliders.argtypes = [vp, ctypes.c_double]
             L.rd_adjoint_record.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32]
             L.rd_adjoint_backward.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.POINTER(Grads)]
             L.rd_set_kernel_timing.argtypes = [vp, ctypes.c_int]
@@ -324,6 +336,22 @@ class Simulation:
     def num_scenes(self) -> int:
         return 1
 
+    def set_colliders(self, colliders, mode: int = RD_COLLIDE_REFERENCE, friction: float = 0.5):
+        """Box colliders for the grid update (rd_set_colliders): dicts with
+        translation, rotation (unit quaternion w, x, y, z), scale (half extents)
+        and velocity."""
+        arr = (Collider * max(1, len(colliders)))()
+        for k, c in enumerate(colliders):
+            arr[k].translation[:] = list(c["translation"])
+            arr[k].rotation[:] = list(c.get("rotation", (1.0, 0.0, 0.0, 0.0)))
+            arr[k].scale[:] = list(c["scale"])
+            arr[k].velocity[:] = list(c.get("velocity", (0.0, 0.0, 0.0)))
+        self._check(lib().rd_set_colliders(self._h, arr, len(colliders), int(mode), float(friction)),
+                    "rd_set_colliders")
+
+    def move_colliders(self, dt: float):
+        self._check(lib().rd_move_colliders(self._h, float(dt)), "rd_move_colliders")
+
     def adjoint_record(self, dt: float, steps: int, checkpoint_every: int = 10):
         """rd_adjoint_record: `steps` steps from the current state, keeping
         checkpoints for the reverse pass; the handle then holds the final state."""
@@ -456,8 +484,13 @@ class LagrangeEulerView:
         self.sim.stage("grid_velocities", timeDelta)
 
     def gridBasedCollisions(self, timeDelta: float, objects=()):
-        if len(objects):
-            raise NotImplementedError("SDF colliders are not part of this path")
+        """objects: box colliders as dicts (translation, rotation (w, x, y, z),
+        scale, velocity), the reference's MeshCollider fields; uploaded when
+        they change."""
+        objs = [dict(c) for c in objects]
+        if objs != getattr(self, "_colliders", []):
+            self.sim.set_colliders(objs)
+            self._colliders = objs
         self.sim.stage("collisions", timeDelta)
 
     def updateDeformationGradient(self, timeDelta: float):

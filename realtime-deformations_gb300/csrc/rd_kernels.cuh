@@ -34,6 +34,9 @@ template <typename T> struct DevParams {
     // 4x4x4 block among all scenes' blocks, and its first grid node.
     uint32_t block_base;
     unsigned long long goff;
+    // box colliders applied in the grid update (single scene): count, rule, mu
+    int ncol, col_mode;
+    T mu;
 };
 
 struct DevBufs {
@@ -58,7 +61,67 @@ struct DevBufs {
     const uint32_t* sblock;
     const uint32_t* spoff;
     int nscenes;
+    const void* colliders;  // Collider<T>[ncol]
 };
+
+// A box collider on the device: R (world from box, row-major), centre t, half
+// extents s, velocity v.
+template <typename T> struct Collider {
+    T R[9], t[3], s[3], v[3];
+};
+
+// MeshCollider::sdf (material_point_method.hpp:80-88): with p = R^T (x - t)
+// and q = |p| - s, the reference returns |max(q_x, q_y, q_z, 0)| +
+// min(max(q_x, q_y, q_z), 0), i.e. max_i q_i.
+template <typename T>
+__device__ __forceinline__ T box_sdf(const Collider<T>& c, T x0, T x1, T x2) {
+    const T d0 = x0 - c.t[0], d1 = x1 - c.t[1], d2 = x2 - c.t[2];
+    const T q0 = abs_(c.R[0] * d0 + c.R[3] * d1 + c.R[6] * d2) - c.s[0];
+    const T q1 = abs_(c.R[1] * d0 + c.R[4] * d1 + c.R[7] * d2) - c.s[1];
+    const T q2 = abs_(c.R[2] * d0 + c.R[5] * d1 + c.R[8] * d2) - c.s[2];
+    const T qm = q0 > q1 ? (q0 > q2 ? q0 : q2) : (q1 > q2 ? q1 : q2);
+    return abs_(qm > T(0) ? qm : T(0)) + (qm < T(0) ? qm : T(0));
+}
+
+// bodyCollision (material_point_method.cpp:264-300) for a grid node at x with
+// velocity v, over the colliders in order.
+template <typename T>
+__device__ __forceinline__ void collide_node(const DevParams<T>& P, const Collider<T>* __restrict__ cols, T x0, T x1,
+                                             T x2, T v[3]) {
+    for (int k = 0; k < P.ncol; ++k) {
+        const Collider<T>& c = cols[k];
+        if (box_sdf(c, x0, x1, x2) > T(0)) continue;
+        T n[3];
+        if (P.col_mode == 0) {  // gradient(phi, pos, 3): central differences, delta 0.001
+            const T dl = T(0.001f);
+            n[0] = (box_sdf(c, x0 + dl, x1, x2) - box_sdf(c, x0 - dl, x1, x2)) / (T(2) * dl);
+            n[1] = (box_sdf(c, x0, x1 + dl, x2) - box_sdf(c, x0, x1 - dl, x2)) / (T(2) * dl);
+            n[2] = (box_sdf(c, x0, x1, x2 + dl) - box_sdf(c, x0, x1, x2 - dl)) / (T(2) * dl);
+        } else {  // outward normal of the face of largest q
+            const T d0 = x0 - c.t[0], d1 = x1 - c.t[1], d2 = x2 - c.t[2];
+            T p[3], q[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                p[a] = c.R[a] * d0 + c.R[3 + a] * d1 + c.R[6 + a] * d2;
+                q[a] = abs_(p[a]) - c.s[a];
+            }
+            const int f = q[0] > q[1] ? (q[0] > q[2] ? 0 : 2) : (q[1] > q[2] ? 1 : 2);
+            const T sg = p[f] < T(0) ? T(-1) : T(1);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) n[a] = sg * c.R[3 * a + f];
+        }
+        const T r0 = v[0] - c.v[0], r1 = v[1] - c.v[1], r2 = v[2] - c.v[2];
+        const T vn = r0 * n[0] + r1 * n[1] + r2 * n[2];
+        if (vn >= T(0)) continue;
+        const T t0 = r0 - n[0] * vn, t1 = r1 - n[1] * vn, t2 = r2 - n[2] * vn;
+        const T len = P.col_mode == 0 ? T(3) : sqrt_(t0 * t0 + t1 * t1 + t2 * t2);
+        T f = T(0);
+        if (len > -P.mu * vn && len > T(0)) f = T(1) + P.mu * vn / len;
+        v[0] = t0 * f + c.v[0];
+        v[1] = t1 * f + c.v[1];
+        v[2] = t2 * f + c.v[2];
+    }
+}
 
 // The scene holding item v of a batch: the last s with starts[s] <= v.
 __device__ __forceinline__ int scene_of(const uint32_t* __restrict__ starts, int nscenes, uint32_t v) {
@@ -1013,9 +1076,13 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
                     v0 = g4.y / g4.x + P.dt * P.g[0];
                     v1 = g4.z / g4.x + P.dt * P.g[1];
                     v2 = g4.w / g4.x + P.dt * P.g[2];
-                    if (P.bc == 1) {
-                        const int ix = c / (kTile * kTile), iy = (c / kTile) % kTile, iz = c % kTile;
-                        if (wall_node(P, org[0] + ix, org[1] + iy, org[2] + iz)) v0 = v1 = v2 = T(0);
+                    const int ix = c / (kTile * kTile), iy = (c / kTile) % kTile, iz = c % kTile;
+                    if (P.bc == 1 && wall_node(P, org[0] + ix, org[1] + iy, org[2] + iz)) v0 = v1 = v2 = T(0);
+                    if (P.ncol) {
+                        T vv[3] = {v0, v1, v2};
+                        collide_node(P, static_cast<const Collider<T>*>(D.colliders), (T)(org[0] + ix) * P.h,
+                                     (T)(org[1] + iy) * P.h, (T)(org[2] + iz) * P.h, vv);
+                        v0 = vv[0]; v1 = vv[1]; v2 = vv[2];
                     }
                 }
             }
@@ -1131,6 +1198,21 @@ __global__ void k_grid_velocities(DevParams<T> P, vec4<T>* __restrict__ grid, co
         const int k = (int)(c % P.M[2]), j = (int)((c / P.M[2]) % P.M[1]), i = (int)(c / ((size_t)P.M[1] * P.M[2]));
         if (wall_node(P, i, j, k)) g.y = g.z = g.w = T(0);
     }
+    grid[c] = g;
+}
+
+// gridBasedCollisions as its own stage (grid holds (m, v)), in place.
+template <typename T>
+__global__ void k_grid_collide(DevParams<T> P, vec4<T>* __restrict__ grid, const Collider<T>* __restrict__ cols) {
+    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nc = (size_t)P.M[0] * P.M[1] * P.M[2];
+    if (c >= nc) return;
+    vec4<T> g = grid[c];
+    if (g.x == T(0)) return;
+    const int k = (int)(c % P.M[2]), j = (int)((c / P.M[2]) % P.M[1]), i = (int)(c / ((size_t)P.M[1] * P.M[2]));
+    T vv[3] = {g.y, g.z, g.w};
+    collide_node(P, cols, (T)i * P.h, (T)j * P.h, (T)k * P.h, vv);
+    g.y = vv[0]; g.z = vv[1]; g.w = vv[2];
     grid[c] = g;
 }
 
@@ -1270,7 +1352,7 @@ __global__ void k_volumes(DevParams<T> P0, DevBufs D, vec4<T>* __restrict__ pl, 
 // fused mode (m, p) -> v = p / m + dt g (+ walls) as k_g2p2g stages it.
 template <typename T, bool FUSED>
 __global__ void k_grid_export(DevParams<T> P, const vec4<T>* __restrict__ grid, T* __restrict__ mass,
-                              T* __restrict__ vel) {
+                              T* __restrict__ vel, const Collider<T>* __restrict__ cols) {
     const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t nc = (size_t)P.M[0] * P.M[1] * P.M[2];
     if (c >= nc) return;
@@ -1285,6 +1367,11 @@ __global__ void k_grid_export(DevParams<T> P, const vec4<T>* __restrict__ grid, 
             const int k = (int)(c % P.M[2]), j = (int)((c / P.M[2]) % P.M[1]),
                       i = (int)(c / ((size_t)P.M[1] * P.M[2]));
             if (P.bc == 1 && wall_node(P, i, j, k)) v0 = v1 = v2 = T(0);
+            if (P.ncol) {
+                T vv[3] = {v0, v1, v2};
+                collide_node(P, cols, (T)i * P.h, (T)j * P.h, (T)k * P.h, vv);
+                v0 = vv[0]; v1 = vv[1]; v2 = vv[2];
+            }
         }
     }
     if (mass) mass[c] = g.x;

@@ -171,6 +171,10 @@ struct rd_handle {
     size_t max_scene_cells = 0;
     std::vector<rd_graph> graphs;
     bool use_graphs = true;
+    std::vector<rd_collider> cols;  // box colliders (single scene)
+    int col_mode = RD_COLLIDE_REFERENCE;
+    double col_mu = 0.5;
+    void* d_col = nullptr;          // Collider<T>[RD_MAX_COLLIDERS]
     int wp = 0;         // particles per work item (<= WorkP)
     int grid_mult = 0;  // persistent CTAs per SM of the step kernels (0: occupancy)
     cudaStream_t stream = nullptr;
@@ -297,7 +301,11 @@ DevParams<T> params_of(const rd_params& p, const int NB[3], int nkeys, int n, do
 // Parameters of scene 0 (the whole handle for a single scene); n is the
 // particle count of all scenes, the stride of the particle planes.
 template <typename T> DevParams<T> make_params(const rd_handle* h, double dt, T fscale) {
-    return params_of<T>(h->prm, h->NB, h->nkeys, h->n, dt, fscale);
+    DevParams<T> P = params_of<T>(h->prm, h->NB, h->nkeys, h->n, dt, fscale);
+    P.ncol = (int)h->cols.size();
+    P.col_mode = h->col_mode;
+    P.mu = (T)h->col_mu;
+    return P;
 }
 
 template <typename T> DevParams<T> scene_params(const rd_handle* h, int s, double dt, T fscale) {
@@ -331,6 +339,7 @@ template <typename T> DevBufs bufs(rd_handle* h) {
     D.sblock = h->d_sblock;
     D.spoff = h->d_spoff;
     D.nscenes = (int)h->scenes.size();
+    D.colliders = h->d_col;
     return D;
 }
 
@@ -549,7 +558,11 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
                                                              static_cast<const vec4<T>*>(h->gforce));
             return launched(h, "k_grid_velocities");
         case RD_STAGE_COLLISIONS:
-            return RD_OK;  // empty collider list: bodyCollision is the identity
+            if (h->cols.empty()) return RD_OK;  // empty collider list: bodyCollision is the identity
+            if (h->grid_mode != GRID_V) return fail(h, RD_INVALID_ARG, "collision stage needs a grid");
+            k_grid_collide<T><<<cb, 256, 0, h->stream>>>(P, static_cast<vec4<T>*>(h->grid[h->g]),
+                                                          static_cast<const Collider<T>*>(h->d_col));
+            return launched(h, "k_grid_collide");
         case RD_STAGE_DEFORMATION:
             if (h->n == 0) return RD_OK;
             if (h->prm.track_fp)
@@ -662,10 +675,12 @@ rd_status get_grid_impl(rd_handle* h, int scene, void* mass, void* vel, void* fo
     const unsigned cb = blocks_for(nc, 256);
     if (h->grid_mode == GRID_FUSED)  // the grid the last step's G2P read
         k_grid_export<T, true><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g ^ 1]) + sc.goff,
-                                                          mass ? m_d : nullptr, vel ? v_d : nullptr);
+                                                          mass ? m_d : nullptr, vel ? v_d : nullptr,
+                                                          static_cast<const Collider<T>*>(h->d_col));
     else
         k_grid_export<T, false><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g]) + sc.goff,
-                                                           mass ? m_d : nullptr, vel ? v_d : nullptr);
+                                                           mass ? m_d : nullptr, vel ? v_d : nullptr,
+                                                           static_cast<const Collider<T>*>(h->d_col));
     RD_TRY(launched(h, "k_grid_export"));
     T* f_d = nullptr;
     if (force) {
@@ -673,7 +688,8 @@ rd_status get_grid_impl(rd_handle* h, int scene, void* mass, void* vel, void* fo
         if (h->grid_mode == GRID_FUSED) {
             RD_TRY(check_cuda(h, cudaMemsetAsync(f_d, 0, 3 * nc * sizeof(T), h->stream), "force"));
         } else {
-            k_grid_export<T, false><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->gforce), nullptr, f_d);
+            k_grid_export<T, false><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->gforce), nullptr, f_d,
+                                                               nullptr);
             RD_TRY(launched(h, "k_grid_export<force>"));
         }
     }
@@ -778,6 +794,7 @@ void release(rd_handle* h) {
     void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->bcount, h->gmark[0],
                     h->gmark[1], h->cursor, h->work,
                     h->nwork2, h->tile_sums, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
+                    h->d_col,
                     h->d_scenes, h->d_sblock, h->d_spoff};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -908,6 +925,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
         {&h->d_scenes, nscenes * psize, batch},
         {(void**)&h->d_sblock, (nscenes + 1) * sizeof(uint32_t), batch},
         {(void**)&h->d_spoff, (nscenes + 1) * sizeof(uint32_t), batch},
+        {&h->d_col, RD_MAX_COLLIDERS * sizeof(Collider<double>), !batch},
     };
     for (auto& a : allocs) {
         if (!a.need) continue;
@@ -1362,6 +1380,53 @@ rd_status adjoint_backward_impl(rd_handle* h, const void* grad_x, const void* gr
     return RD_OK;
 }
 
+// World-from-box rotation of a unit quaternion (w, x, y, z), row-major
+// (glm::mat3_cast); translation, half extents and velocity as they are.
+template <typename T> Collider<T> device_collider(const rd_collider& c) {
+    double w = c.rotation[0], x = c.rotation[1], y = c.rotation[2], z = c.rotation[3];
+    const double nn = std::sqrt(w * w + x * x + y * y + z * z);
+    if (nn > 0) { w /= nn; x /= nn; y /= nn; z /= nn; }
+    const double R[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - w * z),     2 * (x * z + w * y),
+                         2 * (x * y + w * z),     1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                         2 * (x * z - w * y),     2 * (y * z + w * x),     1 - 2 * (x * x + y * y)};
+    Collider<T> d{};
+    for (int e = 0; e < 9; ++e) d.R[e] = (T)R[e];
+    for (int a = 0; a < 3; ++a) {
+        d.t[a] = (T)c.translation[a];
+        d.s[a] = (T)c.scale[a];
+        d.v[a] = (T)c.velocity[a];
+    }
+    return d;
+}
+
+template <typename T> rd_status upload_colliders(rd_handle* h) {
+    std::vector<Collider<T>> d(h->cols.size());
+    for (size_t k = 0; k < d.size(); ++k) d[k] = device_collider<T>(h->cols[k]);
+    // the previous set may still be read by queued steps
+    RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "sync"));
+    if (!d.empty())
+        RD_TRY(check_cuda(h, cudaMemcpy(h->d_col, d.data(), d.size() * sizeof(Collider<T>), cudaMemcpyHostToDevice),
+                          "colliders"));
+    return RD_OK;
+}
+
+// MeshCollider::move on the device, in stream order with the steps.
+template <typename T> __global__ void k_move_colliders(Collider<T>* cols, int n, T dt) {
+    const int k = threadIdx.x;
+    if (k >= n) return;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) cols[k].t[a] += dt * cols[k].v[a];
+}
+
+template <typename T> rd_status move_colliders_impl(rd_handle* h, double dt) {
+    for (rd_collider& c : h->cols)
+        for (int a = 0; a < 3; ++a) c.translation[a] += dt * c.velocity[a];
+    if (h->cols.empty()) return RD_OK;
+    k_move_colliders<T><<<1, RD_MAX_COLLIDERS, 0, h->stream>>>(static_cast<Collider<T>*>(h->d_col),
+                                                               (int)h->cols.size(), (T)dt);
+    return launched(h, "k_move_colliders");
+}
+
 bool all_set(const rd_handle* h) {
     for (const rd_scene_info& sc : h->scenes)
         if (!sc.set && sc.n > 0) return false;
@@ -1478,8 +1543,30 @@ rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas
     return RD_OK;
 }
 
+rd_status rd_set_colliders(rd_handle* h, const rd_collider* colliders, int32_t count, int32_t mode, double friction) {
+    if (!h || count < 0 || count > RD_MAX_COLLIDERS || (count && !colliders) || !std::isfinite(friction) ||
+        (mode != RD_COLLIDE_REFERENCE && mode != RD_COLLIDE_COULOMB))
+        return RD_INVALID_ARG;
+    if (batched(h)) return fail(h, RD_NOT_SUPPORTED, "colliders act on single-scene handles");
+    cudaSetDevice(h->prm.device);
+    ++h->version;
+    h->cols.assign(colliders, colliders + count);
+    h->col_mode = mode;
+    h->col_mu = friction;
+    drop_graphs(h);  // the collider count and rule are launch parameters
+    return RD_DISPATCH(h, upload_colliders, h);
+}
+
+rd_status rd_move_colliders(rd_handle* h, double dt) {
+    if (!h || !std::isfinite(dt)) return RD_INVALID_ARG;
+    cudaSetDevice(h->prm.device);
+    ++h->version;
+    return RD_DISPATCH(h, move_colliders_impl, h, dt);
+}
+
 rd_status rd_adjoint_record(rd_handle* h, double dt, int32_t steps, int32_t checkpoint_every) {
     if (!h || steps < 1 || checkpoint_every < 1 || !std::isfinite(dt)) return RD_INVALID_ARG;
+    if (!h->cols.empty()) return fail(h, RD_NOT_SUPPORTED, "the adjoint has no collider backward");
     if (!h->prm.lagged_b) return fail(h, RD_NOT_SUPPORTED, "the adjoint follows the reference's lagged-B step");
     if (!all_set(h)) return fail(h, RD_INVALID_ARG, "every scene needs its particles first");
     cudaSetDevice(h->prm.device);

@@ -17,7 +17,16 @@ int main(int argc, char** argv) {
     MPM.rasterizeParticlesToGrid();
     MPM.computeParticleVolumesAndDensities();
     const float delta = 1e-5f;
-    const std::vector<int> solidObjects;  // no colliders
+    // the shape of the reference's MeshCollider (mesh transform + velocity);
+    // this scene has none, as the golden fixture was made without them
+    struct Box {
+        struct {
+            float translation[3], scale[3];
+            struct { float w, x, y, z; } rotation;
+        } mesh;
+        float velocity[3];
+    };
+    const std::vector<Box> solidObjects;
     if (fused) {
         MPM.step(delta);
     } else {

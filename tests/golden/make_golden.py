@@ -14,6 +14,13 @@ Fixtures (all FP32, matrices row-major n x 9, grids as sparse cell lists):
 * perturbed_16.npz - 512 particles in a sphere on a 16^3 grid, h = 1/16,
   random velocities, random APIC B and near-identity F_E, F_P, dt = 1e-4:
   the state after 1 and 2 steps (P4) and the step-1 grid.
+* colliders_32.npz - 1200 particles of a ball falling (v ~ (0.4, -3, 0.3))
+  onto the reference's own MeshCollider boxes, a floor box and a box turned
+  45 degrees about z moving at (0.1, 0, 0), on a 32^3 grid, dt = 1e-4: the
+  grid after the collision stage of step 1 and the state after 3 steps, the
+  boxes moved before each step as main.cpp:188 does (P4).
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT] [fixture ...]
 """
 import os
 import sys
@@ -83,12 +90,53 @@ def perturbed():
     return out
 
 
+def colliders():
+    rng = np.random.default_rng(77)
+    G, n = 32, 1200
+    h = np.float32(1.0 / G)
+    d = rng.normal(size=(n, 3))
+    d = d / np.linalg.norm(d, axis=1, keepdims=True) * (rng.uniform(size=(n, 1)) ** (1 / 3)) * 0.12
+    x = (d + np.array([0.5, 0.31, 0.5])).astype(np.float32)
+    v = (np.array([0.4, -3.0, 0.3]) + rng.normal(0, 0.3, (n, 3))).astype(np.float32)
+    m = np.full(n, 1e-4, np.float32)
+    s, c = np.sin(np.radians(22.5)), np.cos(np.radians(22.5))
+    cols = [dict(translation=(0.5, -0.2, 0.5), rotation=(1, 0, 0, 0), scale=(0.4, 0.4, 0.4), velocity=(0, 0, 0)),
+            dict(translation=(0.33, 0.33, 0.5), rotation=(c, 0, 0, s), scale=(0.06, 0.06, 0.3), velocity=(0.1, 0, 0))]
+    P = orc.Params(G, G, G, float(h))
+    r = orc.RefSim(P, x, v, m, p4=1)
+    r.set_colliders(cols)
+    out = {"grid": np.array([G, G, G]), "h": h, "dt": np.float32(1e-4), "n": n, "x0": x, "v0": v, "m0": m,
+           "colliders": orc.collider_spec(cols)}
+    r.init()
+    out["vol0"] = r.particles()["vol"]
+    for st in ("rasterize", "forces", "grid_velocities", "collisions"):
+        r.stage(st, 1e-4)
+    g = r.grid()
+    idx = np.nonzero(g["mass"] != 0)[0]
+    out["s1_grid_idx"] = idx.astype(np.int32)
+    out["s1_grid_mass"] = g["mass"][idx]
+    out["s1_grid_vel"] = g["vel"][idx]
+    # the state after 3 full steps from the initial state
+    r2 = orc.RefSim(P, x, v, m, p4=1)
+    r2.init()
+    for _ in range(3):
+        r2.move_colliders(1e-4)
+        r2.step(1e-4, 1)
+    out.update(state("s3", r2.particles()))
+    r.set_colliders([])
+    return out
+
+
+FIXTURES = {"ref_scene_20": ref_scene, "perturbed_16": perturbed, "colliders_32": colliders}
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    names = sys.argv[2:] or list(FIXTURES)
     if not orc.build_ref(root):
         raise SystemExit("headless reference not available")
-    np.savez_compressed(os.path.join(HERE, "ref_scene_20.npz"), **ref_scene())
-    np.savez_compressed(os.path.join(HERE, "perturbed_16.npz"), **perturbed())
+    for name in names:
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **FIXTURES[name]())
 
 
 if __name__ == "__main__":
