@@ -308,15 +308,21 @@ template <typename T> DevParams<T> make_params(const rd_handle* h, double dt, T 
     return P;
 }
 
+inline bool batched(const rd_handle* h) { return h->scenes.size() > 1; }
+
 template <typename T> DevParams<T> scene_params(const rd_handle* h, int s, double dt, T fscale) {
     const rd_scene_info& sc = h->scenes[s];
     DevParams<T> P = params_of<T>(sc.prm, sc.NB, sc.nblocks * kCellsPerBlock, h->n, dt, fscale);
     P.block_base = sc.block_base;
     P.goff = sc.goff;
+    if (!batched(h)) {  // colliders act on single-scene handles only
+        P.ncol = (int)h->cols.size();
+        P.col_mode = h->col_mode;
+        P.mu = (T)h->col_mu;
+    }
     return P;
 }
 
-inline bool batched(const rd_handle* h) { return h->scenes.size() > 1; }
 
 template <typename T> DevBufs bufs(rd_handle* h) {
     DevBufs D{};
