@@ -63,6 +63,8 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-baseline", type=int, default=1, help="time the single-core CPU baseline (rank 0, N=1)")
     ap.add_argument("--adjoint", type=int, default=1, help="measure forward + adjoint on the 65,536-particle cube")
+    ap.add_argument("--only", choices=("batched", "adjoint", "batched_adjoint"), default=None,
+                    help="run one secondary measurement alone and print its JSON (profiling runs)")
     ap.add_argument("--batch-steps", type=int, default=300,
                     help="timed steps of the batched-forward workload (64 uneven scenes); 0 skips it")
     return ap.parse_args()
@@ -580,8 +582,25 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_only(args):
+    import torch
+    torch.cuda.set_device(0)
+    pkg = graft.load_package()
+    pkg.build()
+    if args.only == "batched":
+        out = measure_batched(pkg, 0, args.steps, max(args.warmup, 3), float("nan"))
+    elif args.only == "adjoint":
+        out = measure_adjoint(pkg, 0)
+    else:
+        out = measure_batched_adjoint(pkg, 0)
+    print(json.dumps({"only": args.only, **out}), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.only:
+        run_only(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -139,6 +139,27 @@ rd_status rd_get_grid(rd_handle* h, void* mass, void* velocity, void* force, int
  * until the next mutating call.  Borrowed pointer. */
 rd_status rd_device_xyzs(rd_handle* h, float** xyzs);
 
+/* The colour stream of the same draw (Particle::r, g, b, a): rgba8 per particle in
+ * original order, white unless set.  rd_set_colors takes n x 4 bytes. */
+rd_status rd_set_colors(rd_handle* h, const uint8_t* rgba, int where);
+rd_status rd_device_colors(rd_handle* h, uint8_t** rgba);
+
+/* Point-splat image of the viewer feed, made with CUDA alone (no graphics API; a
+ * stand-in for drawParticles' billboards, main.cpp:255-300 and
+ * Particle.vertexshader): each particle covers the disc its camera-facing square
+ * of side `size` (0.02) projects to, the nearest particle wins each pixel and is
+ * shaded as a sphere impostor.  width x height rgba8 pixels, rows from the top,
+ * written to `image` (host or device per `where`). */
+typedef struct rd_view {
+    float view_projection[16]; /* column-major (glm): clip = VP * (x, y, z, 1) */
+    float camera_right[3];     /* world-space camera axes (the shader's uniforms) */
+    float camera_up[3];
+    int32_t width, height;
+    uint32_t background;       /* rgba8 */
+    int32_t max_radius;        /* pixels; 0 = 32 */
+} rd_view;
+rd_status rd_splat(rd_handle* h, const rd_view* view, void* image, int where);
+
 rd_status rd_get_flags(rd_handle* h, uint32_t* flags);
 rd_status rd_clear_flags(rd_handle* h);
 rd_status rd_synchronize(rd_handle* h);

@@ -335,3 +335,56 @@ class RefSim:
         m, v, f = np.zeros(nc, np.float32), np.zeros((nc, 3), np.float32), np.zeros((nc, 3), np.float32)
         self.lib().rdref_get_grid(self.h, m.ctypes.data, v.ctypes.data, f.ctypes.data)
         return {"mass": m, "vel": v, "force": f}
+
+
+def splat_image(xyzs, rgba, vp, right, up, width, height, background, max_radius=32):
+    """Restatement of rd_splat (test infrastructure): float32 numpy version of
+    project / splat_radius / the (depth, id) minimum / sphere shading.  xyzs:
+    n x 4 (x, y, z, size), rgba: n uint32, vp: 16 column-major.  Returns the
+    (h, w) uint32 image and the (h, w) id map (-1 where empty)."""
+    f = np.float32
+    xyzs = np.asarray(xyzs, f)
+    M = np.asarray(vp, f).reshape(4, 4).T  # row-major clip = M @ (x, y, z, 1)
+    right, up = np.asarray(right, f), np.asarray(up, f)
+
+    def project(p):
+        c = p @ M[:, :3].T + M[:, 3]
+        iw = f(1) / c[:, 3]
+        px = (c[:, 0] * iw * f(0.5) + f(0.5)) * f(width)
+        py = (f(0.5) - c[:, 1] * iw * f(0.5)) * f(height)
+        depth = c[:, 2] * iw * f(0.5) + f(0.5)
+        return px, py, depth, c[:, 3]
+
+    pos, size = xyzs[:, :3], xyzs[:, 3:4]
+    px, py, depth, w = project(pos)
+    ax, ay, _, _ = project(pos + right * size * f(0.5))
+    bx, by, _, _ = project(pos + up * size * f(0.5))
+    r = np.maximum(np.sqrt((ax - px) ** 2 + (ay - py) ** 2), np.sqrt((bx - px) ** 2 + (by - py) ** 2))
+    r = np.minimum(r, f(max_radius))
+    key = np.full(width * height, np.iinfo(np.uint64).max, np.uint64)
+    ok = (w > 0) & (depth >= 0) & (depth <= 1) & (r > 0)
+    dbits = depth.view(np.uint32).astype(np.uint64)
+    for i in np.nonzero(ok)[0]:
+        x0, x1 = max(0, int(np.floor(px[i] - r[i]))), min(width - 1, int(np.floor(px[i] + r[i])))
+        y0, y1 = max(0, int(np.floor(py[i] - r[i]))), min(height - 1, int(np.floor(py[i] + r[i])))
+        if x1 < x0 or y1 < y0:
+            continue
+        ys, xs = np.mgrid[y0:y1 + 1, x0:x1 + 1]
+        dx, dy = xs.astype(f) + f(0.5) - px[i], ys.astype(f) + f(0.5) - py[i]
+        m = dx * dx + dy * dy <= r[i] * r[i]
+        lin = (ys * width + xs)[m]
+        np.minimum.at(key, lin, (dbits[i] << np.uint64(32)) | np.uint64(i))
+    empty = key == np.iinfo(np.uint64).max
+    ids = np.where(empty, -1, (key & np.uint64(0xffffffff)).astype(np.int64))
+    img = np.full(width * height, background, np.uint32)
+    pix = np.nonzero(~empty)[0]
+    pid = ids[pix]
+    xs, ys = (pix % width).astype(f), (pix // width).astype(f)
+    dx, dy = xs + f(0.5) - px[pid], ys + f(0.5) - py[pid]
+    rr = r[pid]
+    q = np.where(rr > 0, np.minimum(f(1), (dx * dx + dy * dy) / (rr * rr)), f(1))
+    shade = f(0.35) + f(0.65) * np.sqrt(f(1) - q)
+    c = np.asarray(rgba, np.uint32)[pid]
+    chan = [np.minimum(f(255), ((c >> s) & 0xff).astype(f) * shade + f(0.5)).astype(np.uint32) for s in (0, 8, 16)]
+    img[pix] = chan[0] | (chan[1] << 8) | (chan[2] << 16) | np.uint32(0xff000000)
+    return img.reshape(height, width), ids.reshape(height, width)

@@ -49,7 +49,7 @@ EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
            "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
-           "rd_rasterize_noalloc")
+           "rd_set_colors", "rd_device_colors", "rd_splat", "rd_rasterize_noalloc")
 KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g", "adj_g2p", "adj_p2g")
 
 
@@ -96,6 +96,47 @@ class Collider(ctypes.Structure):
     """rd_collider: a box mesh spanning [-1, 1]^3 placed by T R S, with a velocity."""
     _fields_ = [("translation", ctypes.c_double * 3), ("rotation", ctypes.c_double * 4),
                 ("scale", ctypes.c_double * 3), ("velocity", ctypes.c_double * 3)]
+
+
+class View(ctypes.Structure):
+    """rd_view: camera of the point-splat image."""
+    _fields_ = [("view_projection", ctypes.c_float * 16), ("camera_right", ctypes.c_float * 3),
+                ("camera_up", ctypes.c_float * 3), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("background", ctypes.c_uint32), ("max_radius", ctypes.c_int32)]
+
+
+def look_at_view(eye, target, up=(0.0, 1.0, 0.0), fovy_deg=45.0, width=512, height=512, near=0.01, far=10.0,
+                 background=0xFF201A18, max_radius=0) -> View:
+    """A perspective camera like glm::lookAt / glm::perspective, as an rd_view."""
+    eye, target, up = (np.asarray(a, np.float64) for a in (eye, target, up))
+    f = target - eye
+    f /= np.linalg.norm(f)
+    r = np.cross(f, up)
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    view = np.eye(4)
+    view[0, :3], view[1, :3], view[2, :3] = r, u, -f
+    view[:3, 3] = [-r @ eye, -u @ eye, f @ eye]
+    t = 1.0 / np.tan(np.radians(fovy_deg) / 2)
+    proj = np.zeros((4, 4))
+    proj[0, 0], proj[1, 1] = t / (width / height), t
+    proj[2, 2], proj[2, 3] = -(far + near) / (far - near), -2 * far * near / (far - near)
+    proj[3, 2] = -1.0
+    vp = proj @ view
+    v = View()
+    v.view_projection[:] = list(vp.T.reshape(-1).astype(np.float32))  # column-major
+    v.camera_right[:] = list(r.astype(np.float32))
+    v.camera_up[:] = list(u.astype(np.float32))
+    v.width, v.height, v.background, v.max_radius = width, height, background, max_radius
+    return v
+
+
+def save_ppm(path: str, image: np.ndarray):
+    """Writes an (h, w, 4) rgba8 image as a binary PPM (alpha dropped)."""
+    h, w = image.shape[:2]
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(image[:, :, :3]).tobytes())
 
 
 class Grads(ctypes.Structure):
@@ -147,6 +188,9 @@ def lib():
             L.rd_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(TuneResult)]
             L.rd_set_tuning.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
             L.rd_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+            L.rd_set_colors.argtypes = [vp, vp, ctypes.c_int]
+            L.rd_device_colors.argtypes = [vp, ctypes.POINTER(vp)]
+            L.rd_splat.argtypes = [vp, ctypes.POINTER(View), vp, ctypes.c_int]
             L.rd_set_colliders.argtypes = [vp, ctypes.POINTER(Collider), ctypes.c_int32, ctypes.c_int32, ctypes.c_double]
             L.rd_move_colliders.argtypes = [vp, ctypes.c_double]
             L.rd_adjoint_record.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.c_int32]
@@ -351,6 +395,18 @@ class Simulation:
 
     def move_colliders(self, dt: float):
         self._check(lib().rd_move_colliders(self._h, float(dt)), "rd_move_colliders")
+
+    def set_colors(self, rgba):
+        """n x 4 uint8 colours in original particle order (the viewer's colour stream)."""
+        a = np.ascontiguousarray(np.asarray(rgba, np.uint8).reshape(self.n, 4))
+        self._check(lib().rd_set_colors(self._h, a.ctypes.data, RD_HOST), "rd_set_colors")
+        self.synchronize()
+
+    def splat(self, view: View) -> np.ndarray:
+        """rd_splat: the point-splat image of the current particles, (h, w, 4) uint8."""
+        img = np.zeros((view.height, view.width, 4), np.uint8)
+        self._check(lib().rd_splat(self._h, ctypes.byref(view), img.ctypes.data, RD_HOST), "rd_splat")
+        return img
 
     def adjoint_record(self, dt: float, steps: int, checkpoint_every: int = 10):
         """rd_adjoint_record: `steps` steps from the current state, keeping

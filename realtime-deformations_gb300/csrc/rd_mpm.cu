@@ -14,6 +14,7 @@
 
 #include "rd_adjoint.cuh"
 #include "rd_kernels.cuh"
+#include "rd_view.cuh"
 #include "../../include/rd_mpm.h"
 
 using namespace rd;
@@ -206,6 +207,10 @@ struct rd_handle {
     void* gforce = nullptr;
     uint32_t* flags = nullptr;
     float4* xyzs = nullptr;
+    uint32_t* rgba = nullptr;             // colour stream, original order
+    unsigned long long* zid = nullptr;    // splat depth / id per pixel (allocated on first use)
+    uint32_t* img = nullptr;              // splat image staging for host output
+    size_t img_pixels = 0;
     void* io = nullptr;  // device SoA staging for set/get (36 reals per particle)
     void* grid_io = nullptr;  // device staging for rd_get_grid to host (7 reals per cell)
     bool keys_valid = false;
@@ -800,7 +805,7 @@ void release(rd_handle* h) {
     void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->bcount, h->gmark[0],
                     h->gmark[1], h->cursor, h->work,
                     h->nwork2, h->tile_sums, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
-                    h->d_col,
+                    h->d_col, h->rgba, h->zid, h->img,
                     h->d_scenes, h->d_sblock, h->d_spoff};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -927,6 +932,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
         {&h->gforce, h->ncells * v4, !batch},  // stage mode only
         {(void**)&h->flags, 4, true},
         {(void**)&h->xyzs, n * sizeof(float4), true},
+        {(void**)&h->rgba, n * sizeof(uint32_t), true},
         {&h->io, align_up(36 * n * h->esize, 256), true},
         {&h->d_scenes, nscenes * psize, batch},
         {(void**)&h->d_sblock, (nscenes + 1) * sizeof(uint32_t), batch},
@@ -962,6 +968,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
     cudaMemsetAsync(h->perm, 0, n * 4, h->stream);  // every entry is a valid index from the start
     cudaMemsetAsync(h->flags, 0, 4, h->stream);
     cudaMemsetAsync(h->nwork2, 0, 8, h->stream);
+    cudaMemsetAsync(h->rgba, 0xff, n * sizeof(uint32_t), h->stream);  // white
     rd_status st = p.precision == RD_FP64 ? occupancy<double>(h) : occupancy<float>(h);
     if (st != RD_OK) return bail(st);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(RD_CUDA_ERROR);
@@ -1614,6 +1621,59 @@ rd_status rd_device_xyzs(rd_handle* h, float** xyzs) {
     if (!h || !xyzs) return RD_INVALID_ARG;
     cudaSetDevice(h->prm.device);
     return RD_DISPATCH(h, xyzs_impl, h, xyzs);
+}
+
+rd_status rd_set_colors(rd_handle* h, const uint8_t* rgba, int where) {
+    if (!h || !rgba || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
+    cudaSetDevice(h->prm.device);
+    if (h->n == 0) return RD_OK;
+    return check_cuda(h, cudaMemcpyAsync(h->rgba, rgba, (size_t)h->n * 4,
+                                         where == RD_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                                         h->stream),
+                      "colors");
+}
+
+rd_status rd_device_colors(rd_handle* h, uint8_t** rgba) {
+    if (!h || !rgba) return RD_INVALID_ARG;
+    *rgba = reinterpret_cast<uint8_t*>(h->rgba);
+    return RD_OK;
+}
+
+rd_status rd_splat(rd_handle* h, const rd_view* view, void* image, int where) {
+    if (!h || !view || !image || (where != RD_HOST && where != RD_DEVICE) || view->width < 1 || view->height < 1 ||
+        (int64_t)view->width * view->height > ((int64_t)1 << 28) || view->max_radius < 0)
+        return RD_INVALID_ARG;
+    cudaSetDevice(h->prm.device);
+    const size_t npix = (size_t)view->width * view->height;
+    if (h->img_pixels < npix) {  // the splat buffers follow the largest image asked for
+        if (h->zid) cudaFree(h->zid);
+        if (h->img) cudaFree(h->img);
+        h->zid = nullptr;
+        h->img = nullptr;
+        h->img_pixels = 0;
+        RD_TRY(check_cuda(h, cudaMalloc((void**)&h->zid, npix * sizeof(unsigned long long)), "splat buffers"));
+        RD_TRY(check_cuda(h, cudaMalloc((void**)&h->img, npix * sizeof(uint32_t)), "splat buffers"));
+        h->img_pixels = npix;
+    }
+    float* unused = nullptr;
+    RD_TRY(rd_device_xyzs(h, &unused));
+    ViewDev V{};
+    for (int e = 0; e < 16; ++e) V.vp[e] = view->view_projection[e];
+    for (int a = 0; a < 3; ++a) { V.right[a] = view->camera_right[a]; V.up[a] = view->camera_up[a]; }
+    V.width = view->width;
+    V.height = view->height;
+    V.background = view->background;
+    V.max_radius = view->max_radius > 0 ? view->max_radius : 32;
+    uint32_t* out = where == RD_DEVICE ? static_cast<uint32_t*>(image) : h->img;
+    k_splat_clear<<<blocks_for(npix, 256), 256, 0, h->stream>>>(h->zid, (int)npix);
+    if (h->n > 0) k_splat<<<blocks_for(h->n, 256), 256, 0, h->stream>>>(V, h->n, h->xyzs, h->zid);
+    k_splat_resolve<<<blocks_for(npix, 256), 256, 0, h->stream>>>(V, h->n, h->xyzs, h->rgba, h->zid, out);
+    RD_TRY(launched(h, "k_splat", h->n > 0 ? 3 : 2));
+    if (where == RD_HOST) {
+        RD_TRY(check_cuda(h, cudaMemcpyAsync(image, out, npix * 4, cudaMemcpyDeviceToHost, h->stream), "image"));
+        RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "sync"));
+    }
+    return RD_OK;
 }
 
 rd_status rd_get_flags(rd_handle* h, uint32_t* flags) {
