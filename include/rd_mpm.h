@@ -197,6 +197,26 @@ rd_status rd_kernel_timing(rd_handle* h, int kernel, uint64_t* launches, double*
 /* Number of kernel launches issued by this handle so far. */
 rd_status rd_launch_count(rd_handle* h, uint64_t* count);
 
+/* initializeParticles (material_point_method.cpp:18-63) on the device: the cells
+ * within radius / h of the origin, 8 points per cell at quarter offsets, each
+ * jittered inside a ball of a quarter cell, kept where within `radius` of the
+ * origin, placed from the last particle down with this velocity and mass (the
+ * reference: radius 0.2, mass 6e-5); particles left over stay at the origin with
+ * no mass.  RD_INIT_REFERENCE draws the jitter from the C library's rand()
+ * sequence after srand(seed) as the reference does (seed 1 when it never seeds),
+ * on one device thread, and reproduces the reference's particles;
+ * RD_INIT_PARALLEL draws it from a counter-based hash of (seed, candidate) on one
+ * thread per candidate, for large scenes.  *need_more (may be NULL) receives the
+ * number of kept points that found no particle.  Single-scene handles. */
+enum { RD_INIT_REFERENCE = 0, RD_INIT_PARALLEL = 1 };
+typedef struct rd_init_spec {
+    double origin[3], velocity[3];
+    double radius, mass;
+    uint32_t seed;
+    int32_t mode;
+} rd_init_spec;
+rd_status rd_initialize_particles(rd_handle* h, const rd_init_spec* spec, int32_t* need_more);
+
 /* ---- Box colliders (gridBasedCollisions, material_point_method.cpp:264-304) ----
  * The reference's MeshCollider (material_point_method.hpp:74-93) as main.cpp
  * builds it (main.cpp:119-160): a box mesh spanning [-1, 1]^3 placed by

@@ -49,7 +49,7 @@ EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
            "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
-           "rd_set_colors", "rd_device_colors", "rd_splat", "rd_rasterize_noalloc")
+           "rd_set_colors", "rd_device_colors", "rd_splat", "rd_initialize_particles", "rd_rasterize_noalloc")
 KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g", "adj_g2p", "adj_p2g")
 
 
@@ -96,6 +96,14 @@ class Collider(ctypes.Structure):
     """rd_collider: a box mesh spanning [-1, 1]^3 placed by T R S, with a velocity."""
     _fields_ = [("translation", ctypes.c_double * 3), ("rotation", ctypes.c_double * 4),
                 ("scale", ctypes.c_double * 3), ("velocity", ctypes.c_double * 3)]
+
+
+RD_INIT_REFERENCE, RD_INIT_PARALLEL = 0, 1
+
+
+class InitSpec(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_double * 3), ("velocity", ctypes.c_double * 3), ("radius", ctypes.c_double),
+                ("mass", ctypes.c_double), ("seed", ctypes.c_uint32), ("mode", ctypes.c_int32)]
 
 
 class View(ctypes.Structure):
@@ -188,6 +196,7 @@ def lib():
             L.rd_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(TuneResult)]
             L.rd_set_tuning.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
             L.rd_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+            L.rd_initialize_particles.argtypes = [vp, ctypes.POINTER(InitSpec), ctypes.POINTER(ctypes.c_int32)]
             L.rd_set_colors.argtypes = [vp, vp, ctypes.c_int]
             L.rd_device_colors.argtypes = [vp, ctypes.POINTER(vp)]
             L.rd_splat.argtypes = [vp, ctypes.POINTER(View), vp, ctypes.c_int]
@@ -395,6 +404,19 @@ class Simulation:
 
     def move_colliders(self, dt: float):
         self._check(lib().rd_move_colliders(self._h, float(dt)), "rd_move_colliders")
+
+    def initialize_particles(self, origin, velocity, radius: float = 0.2, mass: float = 6e-5, seed: int = 1,
+                             mode: int = RD_INIT_REFERENCE) -> int:
+        """rd_initialize_particles: the reference's jittered sphere generated on the
+        device; returns how many kept points found no particle."""
+        sp = InitSpec()
+        sp.origin[:] = list(origin)
+        sp.velocity[:] = list(velocity)
+        sp.radius, sp.mass, sp.seed, sp.mode = radius, mass, seed, mode
+        more = ctypes.c_int32()
+        self._check(lib().rd_initialize_particles(self._h, ctypes.byref(sp), ctypes.byref(more)),
+                    "rd_initialize_particles")
+        return more.value
 
     def set_colors(self, rgba):
         """n x 4 uint8 colours in original particle order (the viewer's colour stream)."""

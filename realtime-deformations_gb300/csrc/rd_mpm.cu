@@ -14,6 +14,7 @@
 
 #include "rd_adjoint.cuh"
 #include "rd_kernels.cuh"
+#include "rd_init.cuh"
 #include "rd_view.cuh"
 #include "../../include/rd_mpm.h"
 
@@ -1440,6 +1441,74 @@ template <typename T> rd_status move_colliders_impl(rd_handle* h, double dt) {
     return launched(h, "k_move_colliders");
 }
 
+template <typename T> rd_status initialize_impl(rd_handle* h, const rd_init_spec& sp, int32_t* need_more) {
+    const int n = h->n;
+    InitSpec S{};
+    const float hh = (float)h->prm.h;
+    for (int a = 0; a < 3; ++a) { S.origin[a] = (float)sp.origin[a]; S.vel[a] = (float)sp.velocity[a]; }
+    S.width = (float)sp.radius;
+    S.mass = (float)sp.mass;
+    S.h = hh;
+    S.seed = sp.seed;
+    // glm::ivec3(particlesOrigin / h), int(width / h), in float as the reference
+    volatile float ox = S.origin[0] / hh, oy = S.origin[1] / hh, oz = S.origin[2] / hh, wc = S.width / hh;
+    S.cx = (int)ox; S.cy = (int)oy; S.cz = (int)oz; S.wic = (int)wc;
+    if (S.wic < 0 || S.wic > 4096) return fail(h, RD_INVALID_ARG, "radius out of range");
+    vec4<T>* pl = static_cast<vec4<T>*>(h->pl[h->cur]);
+    int more = 0;
+    int* d_more = nullptr;
+    uint32_t* chunk = nullptr;
+    auto cleanup = [&](rd_status st) {
+        if (d_more) cudaFree(d_more);
+        if (chunk) cudaFree(chunk);
+        return st;
+    };
+    rd_status st = RD_OK;
+    if (n > 0) {
+        k_init_defaults<T><<<blocks_for(n, 256), 256, 0, h->stream>>>(S, n, pl);
+        st = launched(h, "k_init_defaults");
+    }
+    if (st == RD_OK && sp.mode == RD_INIT_REFERENCE) {
+        st = check_cuda(h, cudaMalloc((void**)&d_more, sizeof(int)), "init");
+        if (st == RD_OK) {
+            k_init_reference<T><<<1, 32, 0, h->stream>>>(S, n, pl, d_more);
+            st = launched(h, "k_init_reference");
+        }
+        if (st == RD_OK)
+            st = check_cuda(h, cudaMemcpyAsync(&more, d_more, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "init");
+    } else if (st == RD_OK) {
+        const uint64_t side = 2 * (uint64_t)S.wic;
+        const uint64_t ncand = side * side * side * 8;
+        if (ncand >= ((uint64_t)1 << 31)) return cleanup(fail(h, RD_TOO_LARGE, "too many candidate points"));
+        const unsigned nchunks = (unsigned)std::max<uint64_t>(1, (ncand + 1023) / 1024);
+        st = check_cuda(h, cudaMalloc((void**)&chunk, (nchunks + 3) * sizeof(uint32_t)), "init");
+        if (st == RD_OK) {
+            uint32_t* scratch = chunk + nchunks + 1;  // item counter and flags of k_tile_prefix, unused here
+            k_init_count<<<nchunks, 1024, 0, h->stream>>>(S, (uint32_t)ncand, chunk);
+            k_tile_prefix<<<1, 1024, 0, h->stream>>>(chunk, (int)nchunks, scratch, 0u, scratch + 1);
+            k_init_place<T><<<nchunks, 1024, 0, h->stream>>>(S, (uint32_t)ncand, chunk, n, pl);
+            st = launched(h, "k_init", 3);
+        }
+        uint32_t kept = 0;
+        if (st == RD_OK)
+            st = check_cuda(h, cudaMemcpyAsync(&kept, chunk + nchunks, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                               h->stream),
+                            "init");
+        if (st == RD_OK) st = check_cuda(h, cudaStreamSynchronize(h->stream), "sync");
+        more = (int)std::max<int64_t>(0, (int64_t)kept - n);
+    }
+    if (st == RD_OK) st = check_cuda(h, cudaStreamSynchronize(h->stream), "sync");
+    if (st == RD_OK) {
+        if (need_more) *need_more = more;
+        h->scenes[0].set = true;
+        h->keys_valid = false;
+        h->sorted = false;
+        h->fgrid_valid = false;
+        h->grid_mode = GRID_NONE;
+    }
+    return cleanup(st);
+}
+
 bool all_set(const rd_handle* h) {
     for (const rd_scene_info& sc : h->scenes)
         if (!sc.set && sc.n > 0) return false;
@@ -1554,6 +1623,16 @@ rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas
     *particles_per_item = h->wp > 0 ? std::min(h->wp, wmax) : wmax;
     *ctas_per_sm = h->grid_mult > 0 ? std::min(h->grid_mult, h->occ_g2p) : h->occ_g2p;
     return RD_OK;
+}
+
+rd_status rd_initialize_particles(rd_handle* h, const rd_init_spec* spec, int32_t* need_more) {
+    if (!h || !spec || !(spec->radius >= 0) || !std::isfinite(spec->mass) ||
+        (spec->mode != RD_INIT_REFERENCE && spec->mode != RD_INIT_PARALLEL))
+        return RD_INVALID_ARG;
+    if (batched(h)) return fail(h, RD_NOT_SUPPORTED, "the initialiser fills single-scene handles");
+    cudaSetDevice(h->prm.device);
+    ++h->version;
+    return RD_DISPATCH(h, initialize_impl, h, *spec, need_more);
 }
 
 rd_status rd_set_colliders(rd_handle* h, const rd_collider* colliders, int32_t count, int32_t mode, double friction) {
