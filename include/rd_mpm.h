@@ -160,6 +160,22 @@ typedef struct rd_view {
 } rd_view;
 rd_status rd_splat(rd_handle* h, const rd_view* view, void* image, int where);
 
+/* The reference's diagnostics (material_point_method.cpp:352-443) as device
+ * reductions over one scene (0 for a single-scene handle): particleMomentum and
+ * the particle mass; gridMass and gridMomentum over the nodes with mass of the
+ * grid the last step used (its velocities as G2P read them); the count of such
+ * nodes; averageParticleDensity (mean m / V over particles with V > 0);
+ * averageDeformationGradient (mean F_E F_P; without the full F_P (track_fp = 0)
+ * F_P is taken as J_P^(1/3) I).  All in double. */
+typedef struct rd_diagnostics {
+    double particle_mass, particle_momentum[3];
+    double grid_mass, grid_momentum[3];
+    int64_t used_cells;
+    double average_particle_density;
+    double average_deformation_gradient[9]; /* row-major */
+} rd_diagnostics;
+rd_status rd_get_diagnostics(rd_handle* h, int32_t scene, rd_diagnostics* out);
+
 rd_status rd_get_flags(rd_handle* h, uint32_t* flags);
 rd_status rd_clear_flags(rd_handle* h);
 rd_status rd_synchronize(rd_handle* h);

@@ -49,7 +49,8 @@ EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
            "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
-           "rd_set_colors", "rd_device_colors", "rd_splat", "rd_initialize_particles", "rd_rasterize_noalloc")
+           "rd_set_colors", "rd_device_colors", "rd_splat", "rd_initialize_particles", "rd_get_diagnostics",
+           "rd_rasterize_noalloc")
 KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g", "adj_g2p", "adj_p2g")
 
 
@@ -104,6 +105,13 @@ RD_INIT_REFERENCE, RD_INIT_PARALLEL = 0, 1
 class InitSpec(ctypes.Structure):
     _fields_ = [("origin", ctypes.c_double * 3), ("velocity", ctypes.c_double * 3), ("radius", ctypes.c_double),
                 ("mass", ctypes.c_double), ("seed", ctypes.c_uint32), ("mode", ctypes.c_int32)]
+
+
+class Diagnostics(ctypes.Structure):
+    _fields_ = [("particle_mass", ctypes.c_double), ("particle_momentum", ctypes.c_double * 3),
+                ("grid_mass", ctypes.c_double), ("grid_momentum", ctypes.c_double * 3),
+                ("used_cells", ctypes.c_int64), ("average_particle_density", ctypes.c_double),
+                ("average_deformation_gradient", ctypes.c_double * 9)]
 
 
 class View(ctypes.Structure):
@@ -196,6 +204,7 @@ def lib():
             L.rd_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(TuneResult)]
             L.rd_set_tuning.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
             L.rd_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+            L.rd_get_diagnostics.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Diagnostics)]
             L.rd_initialize_particles.argtypes = [vp, ctypes.POINTER(InitSpec), ctypes.POINTER(ctypes.c_int32)]
             L.rd_set_colors.argtypes = [vp, vp, ctypes.c_int]
             L.rd_device_colors.argtypes = [vp, ctypes.POINTER(vp)]
@@ -404,6 +413,16 @@ class Simulation:
 
     def move_colliders(self, dt: float):
         self._check(lib().rd_move_colliders(self._h, float(dt)), "rd_move_colliders")
+
+    def diagnostics(self, scene: int = 0) -> dict:
+        """rd_get_diagnostics: the reference's momentum / mass / density / F
+        diagnostics of one scene, reduced on the device."""
+        d = Diagnostics()
+        self._check(lib().rd_get_diagnostics(self._h, int(scene), ctypes.byref(d)), "rd_get_diagnostics")
+        return {"particle_mass": d.particle_mass, "particle_momentum": np.array(d.particle_momentum[:]),
+                "grid_mass": d.grid_mass, "grid_momentum": np.array(d.grid_momentum[:]), "used_cells": d.used_cells,
+                "average_particle_density": d.average_particle_density,
+                "average_deformation_gradient": np.array(d.average_deformation_gradient[:]).reshape(3, 3)}
 
     def initialize_particles(self, origin, velocity, radius: float = 0.2, mass: float = 6e-5, seed: int = 1,
                              mode: int = RD_INIT_REFERENCE) -> int:

@@ -1378,6 +1378,91 @@ __global__ void k_grid_export(DevParams<T> P, const vec4<T>* __restrict__ grid, 
     if (vel) { vel[3 * c] = v0; vel[3 * c + 1] = v1; vel[3 * c + 2] = v2; }
 }
 
+// ---------------------------------------------------------------- diagnostics
+// Block sums of k values per thread into acc (double atomics, one per block and value).
+template <int K>
+__device__ __forceinline__ void block_sum_to(double (&v)[K], double* __restrict__ acc) {
+    __shared__ double part[K][8];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0) part[k][threadIdx.x >> 5] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[threadIdx.x][w];
+        if (t != 0.0) atomicAdd(acc + threadIdx.x, t);
+    }
+}
+
+// particleMomentum, mass, averageParticleDensity, averageDeformationGradient
+// (material_point_method.cpp:361-367,410-421,437-443) over particles [off, off + cnt):
+// acc = mass | momentum 3 | sum m / V | count V > 0 | sum F_E F_P 9.
+template <typename T>
+__global__ void __launch_bounds__(256) k_diag_particles(int off, int cnt, int ntot, const vec4<T>* __restrict__ pl,
+                                                        int track_fp, double* __restrict__ acc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) v[k] = 0.0;
+    if (i < cnt) {
+        Particle<T> p;
+        load_particle(pl, (size_t)ntot, (size_t)(off + i), p);
+        v[0] = (double)p.m;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) v[1 + a] = (double)p.m * (double)p.v[a];
+        if (p.vol > T(0)) { v[4] = (double)p.m / (double)p.vol; v[5] = 1.0; }
+        T FP[9];
+        if (track_fp) {
+            load_fp(pl, (size_t)ntot, (size_t)(off + i), FP);
+        } else {
+            const T c = cbrt(p.Jp);
+#pragma unroll
+            for (int e = 0; e < 9; ++e) FP[e] = (e % 4 == 0) ? c : T(0);
+        }
+        T F[9];
+        matmul3(F, p.F, FP);
+#pragma unroll
+        for (int e = 0; e < 9; ++e) v[6 + e] = (double)F[e];
+    }
+    block_sum_to<15>(v, acc);
+}
+
+// gridMass, gridMomentum (material_point_method.cpp:352-359,370-376) and the
+// used-cell count over a scene's grid, its velocities as G2P reads them (in
+// fused mode v = p / m + dt g, then walls and colliders): acc = mass |
+// momentum 3 | count.
+template <typename T, bool FUSED>
+__global__ void __launch_bounds__(256) k_diag_grid(DevParams<T> P, const vec4<T>* __restrict__ grid,
+                                                   const Collider<T>* __restrict__ cols, double* __restrict__ acc) {
+    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nc = (size_t)P.M[0] * P.M[1] * P.M[2];
+    double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    if (c < nc) {
+        const vec4<T> g = grid[c];
+        if (g.x != T(0)) {
+            T vv[3] = {g.y, g.z, g.w};
+            if (FUSED) {
+                const int k = (int)(c % P.M[2]), j = (int)((c / P.M[2]) % P.M[1]),
+                          i = (int)(c / ((size_t)P.M[1] * P.M[2]));
+                vv[0] = g.y / g.x + P.dt * P.g[0];
+                vv[1] = g.z / g.x + P.dt * P.g[1];
+                vv[2] = g.w / g.x + P.dt * P.g[2];
+                if (P.bc == 1 && wall_node(P, i, j, k)) vv[0] = vv[1] = vv[2] = T(0);
+                if (P.ncol) collide_node(P, cols, (T)i * P.h, (T)j * P.h, (T)k * P.h, vv);
+            }
+            v[0] = (double)g.x;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) v[1 + a] = (double)g.x * (double)vv[a];
+            v[4] = 1.0;
+        }
+    }
+    block_sum_to<5>(v, acc);
+}
+
 // Viewer stream (main.cpp:259-271): float4 (x, y, z, size) in original order.
 template <typename T>
 __global__ void k_xyzs(int n, const vec4<T>* __restrict__ pl, float4* __restrict__ out, float size) {

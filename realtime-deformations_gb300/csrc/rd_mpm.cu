@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "rd_adjoint.cuh"
 #include "rd_kernels.cuh"
 #include "rd_init.cuh"
@@ -21,6 +23,12 @@
 using namespace rd;
 
 namespace {
+
+// A named range in profiler timelines (no cost without a profiler attached).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
 
 enum GridMode { GRID_NONE = 0, GRID_FUSED = 1, GRID_MV = 2, GRID_V = 3 };
 
@@ -1021,6 +1029,7 @@ bool steady(const rd_handle* h, double dt) {
 }
 
 template <typename T> rd_status steps_impl(rd_handle* h, double dt, int nsteps) {
+    NvtxRange range("rd_step");
     for (int s = 0; s < nsteps;) {
         if (nsteps - s >= 2 && steady(h, dt)) {
             RD_TRY(graph_two_steps<T>(h, dt));
@@ -1037,6 +1046,7 @@ template <typename T> rd_status steps_impl(rd_handle* h, double dt, int nsteps) 
 // (CTAs per SM) from the same saved state, keeps the fastest and puts the
 // state back as it was (the next step re-sorts and rebuilds the grid).
 template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps, rd_tune_result* res) {
+    NvtxRange range("rd_autotune");
     const int wps_f[] = {128, 192, 256}, wps_d[] = {64, 96, 128};
     const int* wps = sizeof(T) == 4 ? wps_f : wps_d;
     rd_tune_result best{WorkP<T>::value, 0, 0.0, 0};
@@ -1183,6 +1193,7 @@ template <typename T> rd_status stored_step(rd_handle* h, double dt, int j) {
 }
 
 template <typename T> rd_status adjoint_record_impl(rd_handle* h, double dt, int steps, int every) {
+    NvtxRange range("rd_adjoint_record");
     RD_TRY(adj_alloc(h, steps, every));
     rd_adjoint_data& a = h->adj;
     a.recorded = false;
@@ -1338,6 +1349,7 @@ template <typename T> rd_status sweep_graph(rd_handle* h) {
 
 template <typename T>
 rd_status adjoint_backward_impl(rd_handle* h, const void* grad_x, const void* grad_v, int where, rd_grads* out) {
+    NvtxRange range("rd_adjoint_backward");
     rd_adjoint_data& a = h->adj;
     const size_t n = (size_t)h->n;
     const bool batch = batched(h);
@@ -1507,6 +1519,43 @@ template <typename T> rd_status initialize_impl(rd_handle* h, const rd_init_spec
         h->grid_mode = GRID_NONE;
     }
     return cleanup(st);
+}
+
+template <typename T> rd_status diagnostics_impl(rd_handle* h, int scene, rd_diagnostics* out) {
+    const rd_scene_info& sc = h->scenes[scene];
+    double* acc = nullptr;
+    RD_TRY(check_cuda(h, cudaMalloc((void**)&acc, 20 * sizeof(double)), "diagnostics"));
+    auto done = [&](rd_status st) { cudaFree(acc); return st; };
+    rd_status st = check_cuda(h, cudaMemsetAsync(acc, 0, 20 * sizeof(double), h->stream), "diagnostics");
+    if (st == RD_OK && sc.n > 0) {
+        k_diag_particles<T><<<blocks_for(sc.n, 256), 256, 0, h->stream>>>(
+            (int)sc.poff, sc.n, h->n, static_cast<const vec4<T>*>(h->pl[h->cur]), h->prm.track_fp, acc);
+        st = launched(h, "k_diag_particles");
+    }
+    if (st == RD_OK && h->grid_mode != GRID_NONE) {
+        const DevParams<T> P = scene_params<T>(h, scene, h->last_dt, T(1));
+        const Collider<T>* cols = static_cast<const Collider<T>*>(h->d_col);
+        const unsigned cb = blocks_for(sc.ncells, 256);
+        if (h->grid_mode == GRID_FUSED)
+            k_diag_grid<T, true><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g ^ 1]) + sc.goff,
+                                                            cols, acc + 15);
+        else
+            k_diag_grid<T, false><<<cb, 256, 0, h->stream>>>(P, static_cast<const vec4<T>*>(h->grid[h->g]) + sc.goff,
+                                                             cols, acc + 15);
+        st = launched(h, "k_diag_grid");
+    }
+    double a[20];
+    if (st == RD_OK) st = check_cuda(h, cudaMemcpyAsync(a, acc, sizeof a, cudaMemcpyDeviceToHost, h->stream), "d2h");
+    if (st == RD_OK) st = check_cuda(h, cudaStreamSynchronize(h->stream), "sync");
+    if (st != RD_OK) return done(st);
+    std::memset(out, 0, sizeof(*out));
+    out->particle_mass = a[0];
+    for (int k = 0; k < 3; ++k) { out->particle_momentum[k] = a[1 + k]; out->grid_momentum[k] = a[16 + k]; }
+    out->average_particle_density = a[5] > 0 ? a[4] / a[5] : 0.0;
+    for (int e = 0; e < 9; ++e) out->average_deformation_gradient[e] = sc.n > 0 ? a[6 + e] / sc.n : 0.0;
+    out->grid_mass = a[15];
+    out->used_cells = (int64_t)a[19];
+    return done(RD_OK);
 }
 
 bool all_set(const rd_handle* h) {
@@ -1753,6 +1802,13 @@ rd_status rd_splat(rd_handle* h, const rd_view* view, void* image, int where) {
         RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "sync"));
     }
     return RD_OK;
+}
+
+rd_status rd_get_diagnostics(rd_handle* h, int32_t scene, rd_diagnostics* out) {
+    if (!h || !out) return RD_INVALID_ARG;
+    if (scene < 0 || scene >= (int32_t)h->scenes.size()) return fail(h, RD_INVALID_ARG, "no such scene");
+    cudaSetDevice(h->prm.device);
+    return RD_DISPATCH(h, diagnostics_impl, h, scene, out);
 }
 
 rd_status rd_get_flags(rd_handle* h, uint32_t* flags) {
