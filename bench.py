@@ -467,18 +467,31 @@ def run_ours(args):
     sim.step(sc.dt, args.warmup)
     sim.get_particles(fields, out=host)
     e2e_steps = max(1, args.e2e_steps)
-    sim.synchronize()
-    barrier(ws)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        sim.set_particles(host["x"], host["v"], host["mass"], B=host["B"], FE=host["FE"], Jp=host["Jp"],
-                          volume=host["volume"], sync=False)
-        sim.step(sc.dt, 1)
-        sim.get_particles(fields, out=host)
-    e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(ws, e2e_s, device=torch.device("cuda", local))
+
+    def e2e_pass(mapped):
+        """Every step: the whole state in from pinned host memory, one step, the
+        whole state back out, then the host waits for it.  Staged: rd_*_particles
+        with RD_HOST (copies to and from a device buffer around the pack and
+        unpack kernels); mapped: the same pinned buffers passed as RD_DEVICE, so
+        the pack and unpack kernels read and write host memory directly."""
+        sim.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            sim.set_particles(host["x"], host["v"], host["mass"], B=host["B"], FE=host["FE"], Jp=host["Jp"],
+                              volume=host["volume"], sync=False, mapped=mapped)
+            sim.step(sc.dt, 1)
+            sim.get_particles(fields, out=host, mapped=mapped)
+            if mapped:
+                sim.synchronize()
+        el = time.perf_counter() - t0
+        return max_over_ranks(ws, el, device=torch.device("cuda", local))
+
+    e2e_s = e2e_pass(False)
+    e2e_mapped_s = e2e_pass(True)
     io_bytes = sum(int(np.prod(shapes[k])) * 4 for k in fields)
     e2e_value = ws * sc.n * e2e_steps / e2e_s
+    e2e_mapped = ws * sc.n * e2e_steps / e2e_mapped_s
 
     out = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
@@ -490,7 +503,11 @@ def run_ours(args):
                    "l2": f"inputs larger than L2: {2 * 7 * 16 * sc.n / 1e6:.0f} MB of particle planes per step"},
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes, "steps": e2e_steps,
-                "path": "rd_set_particles(host) + rd_step + rd_get_particles(host), pinned buffers"},
+                "path": "rd_set_particles(host) + rd_step + rd_get_particles(host), pinned buffers "
+                        "(cudaMemcpyAsync to and from a device staging buffer around the pack / unpack kernels)",
+                "mapped_value": e2e_mapped,
+                "mapped_path": "the same pinned buffers passed as device-accessible pointers: the pack / unpack "
+                               "kernels read and write host memory directly (slower: strided small transfers)"},
         "roofline": {"bound": "hbm", "kernel": {"p2g": "k_p2g", "g2p2g": "k_g2p2g"}[dom],
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src,

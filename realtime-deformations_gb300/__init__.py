@@ -311,20 +311,29 @@ class Simulation:
         ps = _Particles(**{k: (out[k].ctypes.data if k in fields else None) for k in shapes})
         return ps, out
 
-    def set_particles(self, x, v, mass, B=None, FE=None, FP=None, Jp=None, volume=None, sync=True):
+    def set_particles(self, x, v, mass, B=None, FE=None, FP=None, Jp=None, volume=None, sync=True,
+                      mapped=False):
         """Copies host arrays in (rd_set_particles).  With sync=False the call
         returns once the copies are queued; the arrays must stay alive and
-        unchanged until the handle's stream reaches them."""
+        unchanged until the handle's stream reaches them.  mapped=True passes
+        the arrays as device-accessible pointers (RD_DEVICE): for pinned host
+        memory the packing kernel then reads them directly, with no staging
+        copy (unified addressing)."""
         ps, self._pending = self._particles_in(self.n, x, v, mass, B, FE, FP, Jp, volume)
-        self._check(lib().rd_set_particles(self._h, ctypes.byref(ps), RD_HOST), "rd_set_particles")
+        self._check(lib().rd_set_particles(self._h, ctypes.byref(ps), RD_DEVICE if mapped else RD_HOST),
+                    "rd_set_particles")
         if sync:
             self._check(lib().rd_synchronize(self._h), "rd_synchronize")
 
-    def get_particles(self, fields=("x", "v", "B", "FE", "FP", "Jp", "mass", "volume"), out=None):
+    def get_particles(self, fields=("x", "v", "B", "FE", "FP", "Jp", "mass", "volume"), out=None, mapped=False):
         """Copies the particle state out in the original particle order
-        (rd_get_particles).  ``out`` may supply the destination arrays."""
+        (rd_get_particles).  ``out`` may supply the destination arrays.  With
+        mapped=True (``out`` in pinned host memory) the unpacking kernel writes
+        them directly and the call returns without waiting: synchronize()
+        before reading."""
         ps, out = self._particles_out(self.n, fields, out)
-        self._check(lib().rd_get_particles(self._h, ctypes.byref(ps), RD_HOST), "rd_get_particles")
+        self._check(lib().rd_get_particles(self._h, ctypes.byref(ps), RD_DEVICE if mapped else RD_HOST),
+                    "rd_get_particles")
         return out
 
     def init_volumes(self):
