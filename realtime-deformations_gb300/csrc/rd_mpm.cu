@@ -157,6 +157,12 @@ struct rd_adjoint_data {
     int sweep_key = -1, sweep_end = 0, sweep_steps = 0, sweep_every = 0, sweep_wp = 0, sweep_mult = 0;
     double sweep_dt = 0.0;
     uint64_t sweep_launches = 0;
+    // the record (forward with checkpoints) captured the same way; the host
+    // state it starts from is part of the key, the one it ends in is replayed
+    cudaGraphExec_t record = nullptr;
+    int rec_key = -1, rec_end = 0, rec_steps = 0, rec_every = 0, rec_wp = 0, rec_mult = 0;
+    double rec_dt = 0.0;
+    uint64_t rec_launches = 0;
     void* final_state = nullptr;
     // adjoints in slot order, 25 n reals each (x 3n | v 3n | B 9n | F 9n | J_P n):
     // [0], [1] the states either side of the step being reversed, [2] the
@@ -181,6 +187,7 @@ struct rd_handle {
     size_t max_scene_cells = 0;
     std::vector<rd_graph> graphs;
     bool use_graphs = true;
+    bool capturing = false;  // inside a larger capture: no step-pair graphs
     std::vector<rd_collider> cols;  // box colliders (single scene)
     int col_mode = RD_COLLIDE_REFERENCE;
     double col_mu = 0.5;
@@ -799,6 +806,9 @@ void drop_graphs(rd_handle* h) {
     if (h->adj.sweep) cudaGraphExecDestroy(h->adj.sweep);
     h->adj.sweep = nullptr;
     h->adj.sweep_key = -1;
+    if (h->adj.record) cudaGraphExecDestroy(h->adj.record);
+    h->adj.record = nullptr;
+    h->adj.rec_key = -1;
 }
 
 void release(rd_handle* h) {
@@ -1023,7 +1033,7 @@ template <typename T> rd_status graph_two_steps(rd_handle* h, double dt) {
 }
 
 bool steady(const rd_handle* h, double dt) {
-    return h->use_graphs && !h->timing && h->n > 0 && h->keys_valid && !h->sorted && h->fgrid_valid &&
+    return h->use_graphs && !h->timing && !h->capturing && h->n > 0 && h->keys_valid && !h->sorted && h->fgrid_valid &&
            h->fgrid_dt == dt && h->grid_mode == GRID_FUSED &&
            (!batched(h) || (h->table_valid && h->table_dt == dt && h->table_fs == dt));
 }
@@ -1148,7 +1158,7 @@ rd_status adj_alloc(rd_handle* h, int steps, int every) {
         a.nckpt = nckpt;
     }
     if (a.nseg < nseg) {
-        RD_TRY(grow(&a.sstore, nseg * a.state_bytes));
+        RD_TRY(grow(&a.sstore, (nseg + 1) * a.state_bytes));  // slot len: the state after the segment
         RD_TRY(grow(&a.gstore, nseg * a.grid_bytes));
         RD_TRY(grow((void**)&a.sperm, nseg * n * sizeof(uint32_t)));
         RD_TRY(grow((void**)&a.swork, nseg * h->work_cap * sizeof(int4)));
@@ -1169,34 +1179,58 @@ rd_status adj_alloc(rd_handle* h, int steps, int every) {
 
 inline char* at(void* base, size_t i, size_t bytes) { return static_cast<char*>(base) + i * bytes; }
 
-// One forward step that keeps, in slot j of the segment store, the state it
-// starts from, the grid it reads and the sort of that state.
-template <typename T> rd_status stored_step(rd_handle* h, double dt, int j) {
+// `len` forward steps with the segment store as the particle buffers: step j
+// reads its state from slot j and writes the next one to slot j + 1 (slot 0
+// must hold the first state), sorts into slot j of the sort store, and its
+// grid is copied to slot j of the grid store.  The handle's own particle and
+// sort buffers are left alone; slot len ends up holding the state after the
+// segment.
+template <typename T> rd_status stored_segment(rd_handle* h, double dt, int len) {
     rd_adjoint_data& a = h->adj;
     const size_t n = (size_t)h->n;
-    RD_TRY(check_cuda(h, cudaMemcpyAsync(at(a.sstore, (size_t)j, a.state_bytes), h->pl[h->cur], a.state_bytes,
-                                         cudaMemcpyDeviceToDevice, h->stream),
-                      "segment state"));
-    RD_TRY(step_fused<T>(h, dt));
-    RD_TRY(check_cuda(h, cudaMemcpyAsync(at(a.gstore, (size_t)j, a.grid_bytes), h->grid[h->g ^ 1], a.grid_bytes,
-                                         cudaMemcpyDeviceToDevice, h->stream),
-                      "segment grid"));
-    RD_TRY(check_cuda(h, cudaMemcpyAsync(a.sperm + (size_t)j * n, h->perm, n * sizeof(uint32_t),
-                                         cudaMemcpyDeviceToDevice, h->stream),
-                      "segment sort"));
-    RD_TRY(check_cuda(h, cudaMemcpyAsync(a.swork + (size_t)j * h->work_cap, h->work, h->work_cap * sizeof(int4),
-                                         cudaMemcpyDeviceToDevice, h->stream),
-                      "segment sort"));
-    return check_cuda(h, cudaMemcpyAsync(a.snwork + j, h->nwork2 + h->nb, sizeof(uint32_t), cudaMemcpyDeviceToDevice,
-                                         h->stream),
-                      "segment sort");
+    void* const pl0 = h->pl[0];
+    void* const pl1 = h->pl[1];
+    uint32_t* const perm0 = h->perm;
+    int4* const work0 = h->work;
+    rd_status st = RD_OK;
+    for (int j = 0; j < len && st == RD_OK; ++j) {
+        h->pl[h->cur] = at(a.sstore, (size_t)j, a.state_bytes);
+        h->pl[h->cur ^ 1] = at(a.sstore, (size_t)j + 1, a.state_bytes);
+        h->perm = a.sperm + (size_t)j * n;
+        h->work = a.swork + (size_t)j * h->work_cap;
+        st = step_fused<T>(h, dt);
+        if (st == RD_OK)
+            st = check_cuda(h, cudaMemcpyAsync(at(a.gstore, (size_t)j, a.grid_bytes), h->grid[h->g ^ 1], a.grid_bytes,
+                                               cudaMemcpyDeviceToDevice, h->stream),
+                            "segment grid");
+        if (st == RD_OK)
+            st = check_cuda(h, cudaMemcpyAsync(a.snwork + j, h->nwork2 + h->nb, sizeof(uint32_t),
+                                               cudaMemcpyDeviceToDevice, h->stream),
+                            "segment sort");
+    }
+    h->pl[0] = pl0;
+    h->pl[1] = pl1;
+    h->perm = perm0;
+    h->work = work0;
+    return st;
 }
 
-template <typename T> rd_status adjoint_record_impl(rd_handle* h, double dt, int steps, int every) {
-    NvtxRange range("rd_adjoint_record");
-    RD_TRY(adj_alloc(h, steps, every));
+// Copies `src` into slot 0 of the segment store as a fresh state (no sort, no grid).
+rd_status begin_segment(rd_handle* h, const void* src) {
     rd_adjoint_data& a = h->adj;
-    a.recorded = false;
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(a.sstore, src, a.state_bytes, cudaMemcpyDeviceToDevice, h->stream),
+                      "segment start"));
+    h->keys_valid = false;
+    h->sorted = false;
+    h->fgrid_valid = false;
+    h->grid_mode = GRID_NONE;
+    return RD_OK;
+}
+
+// The record: checkpoints every `every` steps, the last segment straight into
+// the segment store, the final state kept.  Enqueues work only.
+template <typename T> rd_status record_body(rd_handle* h, double dt, int steps, int every) {
+    rd_adjoint_data& a = h->adj;
     a.tail_valid = false;
     for (int s = 0; s < steps; s += every) {
         RD_TRY(check_cuda(h, cudaMemcpyAsync(at(a.ckpt, (size_t)(s / every), a.state_bytes), h->pl[h->cur],
@@ -1204,15 +1238,88 @@ template <typename T> rd_status adjoint_record_impl(rd_handle* h, double dt, int
                           "checkpoint"));
         const int len = std::min(every, steps - s);
         if (s + every >= steps && h->n > 0) {  // the last segment goes straight into the store
-            for (int j = 0; j < len; ++j) RD_TRY(stored_step<T>(h, dt, j));
+            RD_TRY(begin_segment(h, h->pl[h->cur]));
+            RD_TRY(stored_segment<T>(h, dt, len));
+            // the handle holds the final state again
+            RD_TRY(check_cuda(h, cudaMemcpyAsync(h->pl[h->cur], at(a.sstore, (size_t)len, a.state_bytes), a.state_bytes,
+                                                 cudaMemcpyDeviceToDevice, h->stream),
+                              "final state"));
+            h->keys_valid = false;
+            h->sorted = false;
+            h->fgrid_valid = false;
+            h->grid_mode = GRID_NONE;
             a.tail_valid = true;
         } else {
             RD_TRY(steps_impl<T>(h, dt, len));
         }
     }
-    RD_TRY(check_cuda(h, cudaMemcpyAsync(a.final_state, h->pl[h->cur], a.state_bytes, cudaMemcpyDeviceToDevice,
+    return check_cuda(h, cudaMemcpyAsync(a.final_state, h->pl[h->cur], a.state_bytes, cudaMemcpyDeviceToDevice,
                                          h->stream),
-                      "final state"));
+                      "final state");
+}
+
+// Host-side step state (buffer assignment and validity flags) packed in an int.
+int host_state(const rd_handle* h, double dt) {
+    return h->cur | (h->g << 1) | (h->nb << 2) | (h->keys_valid << 3) | (h->sorted << 4) |
+           ((h->fgrid_valid && h->fgrid_dt == dt) << 5) | (h->grid_mode << 6);
+}
+void set_host_state(rd_handle* h, int s, double dt) {
+    h->cur = s & 1;
+    h->g = (s >> 1) & 1;
+    h->nb = (s >> 2) & 1;
+    h->keys_valid = (s >> 3) & 1;
+    h->sorted = (s >> 4) & 1;
+    h->fgrid_valid = (s >> 5) & 1;
+    h->fgrid_dt = dt;
+    h->grid_mode = (s >> 6) & 3;
+    h->last_dt = dt;
+}
+
+template <typename T> rd_status adjoint_record_impl(rd_handle* h, double dt, int steps, int every) {
+    NvtxRange range("rd_adjoint_record");
+    RD_TRY(adj_alloc(h, steps, every));
+    rd_adjoint_data& a = h->adj;
+    a.recorded = false;
+    if (batched(h)) RD_TRY(ensure_table<T>(h, dt, (T)dt));  // no synchronisation inside a capture
+    if (!h->use_graphs || h->timing || h->n == 0) {
+        RD_TRY(record_body<T>(h, dt, steps, every));
+    } else {
+        const int key = host_state(h, dt);
+        const bool hit = a.record && a.rec_key == key && a.rec_dt == dt && a.rec_steps == steps &&
+                         a.rec_every == every && a.rec_wp == h->wp && a.rec_mult == h->grid_mult;
+        if (!hit) {
+            if (a.record) cudaGraphExecDestroy(a.record);
+            a.record = nullptr;
+            const uint64_t l0 = h->launches;
+            RD_TRY(check_cuda(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture"));
+            h->capturing = true;
+            const rd_status st = record_body<T>(h, dt, steps, every);
+            h->capturing = false;
+            cudaGraph_t graph = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+            if (st != RD_OK || e != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                cudaGetLastError();
+                return st != RD_OK ? st : check_cuda(h, e, "end capture");
+            }
+            const cudaError_t ie = cudaGraphInstantiate(&a.record, graph, 0);
+            cudaGraphDestroy(graph);
+            RD_TRY(check_cuda(h, ie, "graph instantiate"));
+            a.rec_key = key;
+            a.rec_end = host_state(h, dt);
+            a.rec_dt = dt;
+            a.rec_steps = steps;
+            a.rec_every = every;
+            a.rec_wp = h->wp;
+            a.rec_mult = h->grid_mult;
+            a.rec_launches = h->launches - l0;
+        } else {
+            set_host_state(h, a.rec_end, dt);
+            h->launches += a.rec_launches;
+            a.tail_valid = h->n > 0;
+        }
+        RD_TRY(check_cuda(h, cudaGraphLaunch(a.record, h->stream), "graph launch"));
+    }
     a.recorded = true;
     a.dt = dt;
     a.steps = steps;
@@ -1249,12 +1356,12 @@ template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
     for (int seg = nseg - 1; seg >= 0 && n; --seg) {
         const int c = seg * a.every, len = std::min(a.every, a.steps - c);
         if (!(seg == nseg - 1 && a.tail_valid)) {  // recompute the segment into the store
-            RD_TRY(load_state(h, at(a.ckpt, (size_t)seg, a.state_bytes), a.state_bytes));
-            for (int j = 0; j < len; ++j) RD_TRY(stored_step<T>(h, dt, j));
+            RD_TRY(begin_segment(h, at(a.ckpt, (size_t)seg, a.state_bytes)));
+            RD_TRY(stored_segment<T>(h, dt, len));
         }
-        // the handle now holds the state after the segment, in this pass's slot
+        // slot len holds the state after the segment, in this pass's slot
         // order: bring the adjoint of that state into the same order
-        const vec4<T>* after = static_cast<const vec4<T>*>(h->pl[h->cur]);
+        const vec4<T>* after = reinterpret_cast<const vec4<T>*>(at(a.sstore, (size_t)len, a.state_bytes));
         const unsigned nb256 = blocks_for(n, 256);
         if (seg == nseg - 1) {  // dL/dx, dL/dv of the final state (staged in adj[2] by id)
             const AdjState<T> S = adj_view<T>(h, 2);
