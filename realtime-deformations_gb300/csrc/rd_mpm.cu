@@ -144,11 +144,16 @@ struct rd_adjoint_data {
     size_t state_bytes = 0, grid_bytes = 0;
     size_t nckpt = 0, nseg = 0;         // capacities (states)
     void* ckpt = nullptr;               // nckpt states
-    void* sstore = nullptr;             // nseg states
-    void* gstore = nullptr;             // nseg grids (m, p) of those states
-    uint32_t* sperm = nullptr;          // nseg sorted permutations of those states
-    int4* swork = nullptr;              // nseg work lists
-    uint32_t* snwork = nullptr;         // nseg work-item counts
+    // two segment stores, so that the recomputation of one segment runs
+    // beside the reverse kernels of the next (a second stream)
+    void* sstore[2] = {nullptr, nullptr};    // nseg + 1 states
+    void* gstore[2] = {nullptr, nullptr};    // nseg grids (m, p) of those states
+    uint32_t* sperm[2] = {nullptr, nullptr}; // nseg sorted permutations of those states
+    int4* swork[2] = {nullptr, nullptr};     // nseg work lists
+    uint32_t* snwork[2] = {nullptr, nullptr};// nseg work-item counts
+    int tail_store = 0;                 // the store the record's last segment is in
+    cudaStream_t stream2 = nullptr;     // the reverse kernels
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_rev[2] = {nullptr, nullptr};
     int occ_g2p = 1, occ_p2g = 1;       // resident CTAs per SM of the reverse kernels
     bool tail_valid = false;            // the store holds the last segment of the record
     // the reverse sweep captured as one CUDA graph, for one start assignment
@@ -817,7 +822,16 @@ void release(rd_handle* h) {
     h->ev.clear();
     drop_graphs(h);
     rd_adjoint_data& a = h->adj;
-    void* aptrs[] = {a.ckpt, a.sstore, a.gstore, a.sperm, a.swork, a.snwork, a.final_state, a.adj[0], a.adj[1], a.adj[2],
+    for (int b = 0; b < 2; ++b) {
+        void* sp[] = {a.sstore[b], a.gstore[b], a.sperm[b], a.swork[b], a.snwork[b]};
+        for (void* p : sp)
+            if (p) cudaFree(p);
+    }
+    cudaEvent_t evs[] = {a.ev_fork, a.ev_join, a.ev_rec[0], a.ev_rec[1], a.ev_rev[0], a.ev_rev[1]};
+    for (cudaEvent_t e : evs)
+        if (e) cudaEventDestroy(e);
+    if (a.stream2) cudaStreamDestroy(a.stream2);
+    void* aptrs[] = {a.ckpt, a.final_state, a.adj[0], a.adj[1], a.adj[2],
                      a.agrid, a.pacc, a.acc};
     for (void* p : aptrs)
         if (p) cudaFree(p);
@@ -1158,14 +1172,20 @@ rd_status adj_alloc(rd_handle* h, int steps, int every) {
         a.nckpt = nckpt;
     }
     if (a.nseg < nseg) {
-        RD_TRY(grow(&a.sstore, (nseg + 1) * a.state_bytes));  // slot len: the state after the segment
-        RD_TRY(grow(&a.gstore, nseg * a.grid_bytes));
-        RD_TRY(grow((void**)&a.sperm, nseg * n * sizeof(uint32_t)));
-        RD_TRY(grow((void**)&a.swork, nseg * h->work_cap * sizeof(int4)));
-        RD_TRY(grow((void**)&a.snwork, nseg * sizeof(uint32_t)));
+        for (int b = 0; b < 2; ++b) {
+            RD_TRY(grow(&a.sstore[b], (nseg + 1) * a.state_bytes));  // slot len: the state after the segment
+            RD_TRY(grow(&a.gstore[b], nseg * a.grid_bytes));
+            RD_TRY(grow((void**)&a.sperm[b], nseg * n * sizeof(uint32_t)));
+            RD_TRY(grow((void**)&a.swork[b], nseg * h->work_cap * sizeof(int4)));
+            RD_TRY(grow((void**)&a.snwork[b], nseg * sizeof(uint32_t)));
+        }
         a.nseg = nseg;
     }
     if (!a.final_state) {
+        RD_TRY(check_cuda(h, cudaStreamCreateWithFlags(&a.stream2, cudaStreamNonBlocking), "adjoint stream"));
+        cudaEvent_t* evs[] = {&a.ev_fork, &a.ev_join, &a.ev_rec[0], &a.ev_rec[1], &a.ev_rev[0], &a.ev_rev[1]};
+        for (cudaEvent_t* e : evs)
+            RD_TRY(check_cuda(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "adjoint events"));
         RD_TRY(check_cuda(h, cudaMalloc(&a.final_state, a.state_bytes), "adjoint buffers"));
         for (int k = 0; k < 3; ++k) RD_TRY(check_cuda(h, cudaMalloc(&a.adj[k], 25 * n * h->esize), "adjoint buffers"));
         RD_TRY(check_cuda(h, cudaMalloc(&a.agrid, a.grid_bytes), "adjoint buffers"));
@@ -1185,7 +1205,7 @@ inline char* at(void* base, size_t i, size_t bytes) { return static_cast<char*>(
 // grid is copied to slot j of the grid store.  The handle's own particle and
 // sort buffers are left alone; slot len ends up holding the state after the
 // segment.
-template <typename T> rd_status stored_segment(rd_handle* h, double dt, int len) {
+template <typename T> rd_status stored_segment(rd_handle* h, double dt, int len, int b) {
     rd_adjoint_data& a = h->adj;
     const size_t n = (size_t)h->n;
     void* const pl0 = h->pl[0];
@@ -1194,17 +1214,17 @@ template <typename T> rd_status stored_segment(rd_handle* h, double dt, int len)
     int4* const work0 = h->work;
     rd_status st = RD_OK;
     for (int j = 0; j < len && st == RD_OK; ++j) {
-        h->pl[h->cur] = at(a.sstore, (size_t)j, a.state_bytes);
-        h->pl[h->cur ^ 1] = at(a.sstore, (size_t)j + 1, a.state_bytes);
-        h->perm = a.sperm + (size_t)j * n;
-        h->work = a.swork + (size_t)j * h->work_cap;
+        h->pl[h->cur] = at(a.sstore[b], (size_t)j, a.state_bytes);
+        h->pl[h->cur ^ 1] = at(a.sstore[b], (size_t)j + 1, a.state_bytes);
+        h->perm = a.sperm[b] + (size_t)j * n;
+        h->work = a.swork[b] + (size_t)j * h->work_cap;
         st = step_fused<T>(h, dt);
         if (st == RD_OK)
-            st = check_cuda(h, cudaMemcpyAsync(at(a.gstore, (size_t)j, a.grid_bytes), h->grid[h->g ^ 1], a.grid_bytes,
+            st = check_cuda(h, cudaMemcpyAsync(at(a.gstore[b], (size_t)j, a.grid_bytes), h->grid[h->g ^ 1], a.grid_bytes,
                                                cudaMemcpyDeviceToDevice, h->stream),
                             "segment grid");
         if (st == RD_OK)
-            st = check_cuda(h, cudaMemcpyAsync(a.snwork + j, h->nwork2 + h->nb, sizeof(uint32_t),
+            st = check_cuda(h, cudaMemcpyAsync(a.snwork[b] + j, h->nwork2 + h->nb, sizeof(uint32_t),
                                                cudaMemcpyDeviceToDevice, h->stream),
                             "segment sort");
     }
@@ -1216,9 +1236,9 @@ template <typename T> rd_status stored_segment(rd_handle* h, double dt, int len)
 }
 
 // Copies `src` into slot 0 of the segment store as a fresh state (no sort, no grid).
-rd_status begin_segment(rd_handle* h, const void* src) {
+rd_status begin_segment(rd_handle* h, const void* src, int b) {
     rd_adjoint_data& a = h->adj;
-    RD_TRY(check_cuda(h, cudaMemcpyAsync(a.sstore, src, a.state_bytes, cudaMemcpyDeviceToDevice, h->stream),
+    RD_TRY(check_cuda(h, cudaMemcpyAsync(a.sstore[b], src, a.state_bytes, cudaMemcpyDeviceToDevice, h->stream),
                       "segment start"));
     h->keys_valid = false;
     h->sorted = false;
@@ -1237,11 +1257,13 @@ template <typename T> rd_status record_body(rd_handle* h, double dt, int steps, 
                                              a.state_bytes, cudaMemcpyDeviceToDevice, h->stream),
                           "checkpoint"));
         const int len = std::min(every, steps - s);
-        if (s + every >= steps && h->n > 0) {  // the last segment goes straight into the store
-            RD_TRY(begin_segment(h, h->pl[h->cur]));
-            RD_TRY(stored_segment<T>(h, dt, len));
+        if (s + every >= steps && h->n > 0) {  // the last segment goes straight into its store
+            const int b = (s / every) & 1;
+            a.tail_store = b;
+            RD_TRY(begin_segment(h, h->pl[h->cur], b));
+            RD_TRY(stored_segment<T>(h, dt, len, b));
             // the handle holds the final state again
-            RD_TRY(check_cuda(h, cudaMemcpyAsync(h->pl[h->cur], at(a.sstore, (size_t)len, a.state_bytes), a.state_bytes,
+            RD_TRY(check_cuda(h, cudaMemcpyAsync(h->pl[h->cur], at(a.sstore[b], (size_t)len, a.state_bytes), a.state_bytes,
                                                  cudaMemcpyDeviceToDevice, h->stream),
                               "final state"));
             h->keys_valid = false;
@@ -1317,6 +1339,7 @@ template <typename T> rd_status adjoint_record_impl(rd_handle* h, double dt, int
             set_host_state(h, a.rec_end, dt);
             h->launches += a.rec_launches;
             a.tail_valid = h->n > 0;
+            a.tail_store = (((steps + every - 1) / every) - 1) & 1;
         }
         RD_TRY(check_cuda(h, cudaGraphLaunch(a.record, h->stream), "graph launch"));
     }
@@ -1347,30 +1370,46 @@ rd_status load_state(rd_handle* h, const void* src, size_t bytes) {
 // The reverse sweep over all segments, last to first; nxt is the adjoint
 // buffer holding the adjoint of the final state on entry.  Ends with the
 // final state back in the handle.  Enqueues work only (capturable).
+// Segment k uses store k & 1: the handle's stream recomputes a segment into
+// its store while the second stream runs the reverse kernels of the segment
+// after it from the other store; events order each store's reuse.
 template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
     rd_adjoint_data& a = h->adj;
     const size_t n = (size_t)h->n;
     const double dt = a.dt;
     const bool batch = batched(h);
     const int nseg = (a.steps + a.every - 1) / a.every;
+    const bool two = !h->timing && a.stream2;  // per-kernel event timing runs on the handle's stream only
+    cudaStream_t rs = two ? a.stream2 : h->stream;
+    if (two) {  // the reverse stream follows everything queued so far (and joins a capture)
+        RD_TRY(check_cuda(h, cudaEventRecord(a.ev_fork, h->stream), "event"));
+        RD_TRY(check_cuda(h, cudaStreamWaitEvent(rs, a.ev_fork, 0), "event"));
+    }
     for (int seg = nseg - 1; seg >= 0 && n; --seg) {
         const int c = seg * a.every, len = std::min(a.every, a.steps - c);
-        if (!(seg == nseg - 1 && a.tail_valid)) {  // recompute the segment into the store
-            RD_TRY(begin_segment(h, at(a.ckpt, (size_t)seg, a.state_bytes)));
-            RD_TRY(stored_segment<T>(h, dt, len));
+        const int b = (seg == nseg - 1 && a.tail_valid) ? a.tail_store : (seg & 1);
+        if (!(seg == nseg - 1 && a.tail_valid)) {  // recompute the segment into store b
+            if (two && seg + 2 <= nseg - 1)        // once the reverse of segment seg + 2 is done with it
+                RD_TRY(check_cuda(h, cudaStreamWaitEvent(h->stream, a.ev_rev[b], 0), "event"));
+            RD_TRY(begin_segment(h, at(a.ckpt, (size_t)seg, a.state_bytes), b));
+            RD_TRY(stored_segment<T>(h, dt, len, b));
+        }
+        if (two) {
+            RD_TRY(check_cuda(h, cudaEventRecord(a.ev_rec[b], h->stream), "event"));
+            RD_TRY(check_cuda(h, cudaStreamWaitEvent(rs, a.ev_rec[b], 0), "event"));
         }
         // slot len holds the state after the segment, in this pass's slot
         // order: bring the adjoint of that state into the same order
-        const vec4<T>* after = reinterpret_cast<const vec4<T>*>(at(a.sstore, (size_t)len, a.state_bytes));
+        const vec4<T>* after = reinterpret_cast<const vec4<T>*>(at(a.sstore[b], (size_t)len, a.state_bytes));
         const unsigned nb256 = blocks_for(n, 256);
         if (seg == nseg - 1) {  // dL/dx, dL/dv of the final state (staged in adj[2] by id)
             const AdjState<T> S = adj_view<T>(h, 2);
-            k_adj_seed<T><<<nb256, 256, 0, h->stream>>>((int)n, after, S.x, S.v, adj_view<T>(h, nxt));
+            k_adj_seed<T><<<nb256, 256, 0, rs>>>((int)n, after, S.x, S.v, adj_view<T>(h, nxt));
             RD_TRY(launched(h, "k_adj_seed"));
         } else {  // from the order of the next segment's checkpoint
             const vec4<T>* ck = reinterpret_cast<const vec4<T>*>(at(a.ckpt, (size_t)seg + 1, a.state_bytes));
-            k_adj_to_id<T><<<nb256, 256, 0, h->stream>>>((int)n, ck, adj_view<T>(h, nxt), adj_view<T>(h, 2));
-            k_adj_from_id<T><<<nb256, 256, 0, h->stream>>>((int)n, after, adj_view<T>(h, 2), adj_view<T>(h, nxt));
+            k_adj_to_id<T><<<nb256, 256, 0, rs>>>((int)n, ck, adj_view<T>(h, nxt), adj_view<T>(h, 2));
+            k_adj_from_id<T><<<nb256, 256, 0, rs>>>((int)n, after, adj_view<T>(h, 2), adj_view<T>(h, nxt));
             RD_TRY(launched(h, "k_adj_remap", 2));
         }
         const DevParams<T> P = make_params<T>(h, dt, (T)dt);
@@ -1380,30 +1419,35 @@ template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
         const size_t sg = sizeof(AdjG2PShared<T>), sp = sizeof(AdjP2GShared<T>);
         for (int j = len - 1; j >= 0; --j) {
             const int cur = nxt ^ 1;
-            const vec4<T>* st = reinterpret_cast<const vec4<T>*>(at(a.sstore, (size_t)j, a.state_bytes));
-            const vec4<T>* gr = reinterpret_cast<const vec4<T>*>(at(a.gstore, (size_t)j, a.grid_bytes));
+            const vec4<T>* st = reinterpret_cast<const vec4<T>*>(at(a.sstore[b], (size_t)j, a.state_bytes));
+            const vec4<T>* gr = reinterpret_cast<const vec4<T>*>(at(a.gstore[b], (size_t)j, a.grid_bytes));
             vec4<T>* ag = static_cast<vec4<T>*>(a.agrid);
             DevBufs D = bufs<T>(h);
-            D.perm = a.sperm + (size_t)j * n;
-            D.work = a.swork + (size_t)j * h->work_cap;
-            D.nwork = a.snwork + j;
-            RD_TRY(check_cuda(h, cudaMemsetAsync(a.agrid, 0, a.grid_bytes, h->stream), "adjoint grid"));
+            D.perm = a.sperm[b] + (size_t)j * n;
+            D.work = a.swork[b] + (size_t)j * h->work_cap;
+            D.nwork = a.snwork[b] + j;
+            RD_TRY(check_cuda(h, cudaMemsetAsync(a.agrid, 0, a.grid_bytes, rs), "adjoint grid"));
             const AdjState<T> An = adj_view<T>(h, nxt), Ap = adj_view<T>(h, 2), Ac = adj_view<T>(h, cur);
             long t = tmark_begin(h, RD_KERNEL_ADJ_G2P);
             if (batch)
-                k_adj_g2p<T, true><<<gg, kAdjThreads, sg, h->stream>>>(P, D, st, gr, ag, An, Ap, a.pacc);
+                k_adj_g2p<T, true><<<gg, kAdjThreads, sg, rs>>>(P, D, st, gr, ag, An, Ap, a.pacc);
             else
-                k_adj_g2p<T, false><<<gg, kAdjThreads, sg, h->stream>>>(P, D, st, gr, ag, An, Ap, a.pacc);
+                k_adj_g2p<T, false><<<gg, kAdjThreads, sg, rs>>>(P, D, st, gr, ag, An, Ap, a.pacc);
             tmark_end(h, t);
             t = tmark_begin(h, RD_KERNEL_ADJ_P2G);
             if (batch)
-                k_adj_p2g<T, true><<<gp, kAdjThreads, sp, h->stream>>>(P, D, st, gr, ag, Ap, Ac, a.pacc);
+                k_adj_p2g<T, true><<<gp, kAdjThreads, sp, rs>>>(P, D, st, gr, ag, Ap, Ac, a.pacc);
             else
-                k_adj_p2g<T, false><<<gp, kAdjThreads, sp, h->stream>>>(P, D, st, gr, ag, Ap, Ac, a.pacc);
+                k_adj_p2g<T, false><<<gp, kAdjThreads, sp, rs>>>(P, D, st, gr, ag, Ap, Ac, a.pacc);
             tmark_end(h, t);
             RD_TRY(launched(h, "adjoint step", 2));
             nxt = cur;
         }
+        if (two) RD_TRY(check_cuda(h, cudaEventRecord(a.ev_rev[b], rs), "event"));
+    }
+    if (two) {  // the handle's stream waits for the reverse kernels
+        RD_TRY(check_cuda(h, cudaEventRecord(a.ev_join, rs), "event"));
+        RD_TRY(check_cuda(h, cudaStreamWaitEvent(h->stream, a.ev_join, 0), "event"));
     }
     return load_state(h, a.final_state, a.state_bytes);
 }
