@@ -212,6 +212,8 @@ rd_status rd_set_kernel_timing(rd_handle* h, int enable);
 rd_status rd_kernel_timing(rd_handle* h, int kernel, uint64_t* launches, double* total_ms);
 /* Number of kernel launches issued by this handle so far. */
 rd_status rd_launch_count(rd_handle* h, uint64_t* count);
+/* Number of two-step CUDA graphs this handle has replayed (rd_set_graphs). */
+rd_status rd_graph_replays(rd_handle* h, uint64_t* count);
 
 /* initializeParticles (material_point_method.cpp:18-63) on the device: the cells
  * within radius / h of the origin, 8 points per cell at quarter offsets, each

@@ -45,7 +45,7 @@ STAGES = {"rasterize": 0, "forces": 1, "grid_velocities": 2, "collisions": 3,
 EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "rd_get_particles",
            "rd_init_volumes", "rd_step", "rd_stage", "rd_get_grid", "rd_device_xyzs", "rd_get_flags",
            "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort",
-           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_batch_create",
+           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_graph_replays", "rd_batch_create",
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
            "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
@@ -193,6 +193,7 @@ def lib():
             L.rd_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
             L.rd_debug_sort.argtypes = [vp, vp, vp, ctypes.c_int]
             L.rd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+            L.rd_graph_replays.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
             L.rd_rasterize_noalloc.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(_Particles), vp, vp]
             L.rd_batch_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int32, ctypes.POINTER(vp)]
             L.rd_batch_num_scenes.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
@@ -401,6 +402,12 @@ class Simulation:
     def launch_count(self) -> int:
         c = ctypes.c_uint64()
         self._check(lib().rd_launch_count(self._h, ctypes.byref(c)), "rd_launch_count")
+        return c.value
+
+    def graph_replays(self) -> int:
+        """Two-step CUDA graphs replayed so far."""
+        c = ctypes.c_uint64()
+        self._check(lib().rd_graph_replays(self._h, ctypes.byref(c)), "rd_graph_replays")
         return c.value
 
     @property

@@ -238,7 +238,7 @@ struct rd_handle {
     bool sorted = false;
     int grid_mode = GRID_NONE;
     double last_dt = 0.0;
-    uint64_t launches = 0;
+    uint64_t launches = 0, graph_replays = 0;
     int occ_p2g = 1, occ_g2p = 1;
     std::string err;
     // per-kernel event timing (rd_set_kernel_timing)
@@ -1020,6 +1020,7 @@ template <typename T> rd_status graph_two_steps(rd_handle* h, double dt) {
         if (g.key == key && g.dt == dt) {
             RD_TRY(check_cuda(h, cudaGraphLaunch(g.exec, h->stream), "graph launch"));
             h->launches += g.launches;
+            ++h->graph_replays;
             return RD_OK;
         }
     if (h->graphs.size() >= 8) drop_graphs(h);
@@ -1043,13 +1044,16 @@ template <typename T> rd_status graph_two_steps(rd_handle* h, double dt) {
     cudaGraphDestroy(graph);
     RD_TRY(check_cuda(h, ie, "graph instantiate"));
     h->graphs.push_back(g);
+    ++h->graph_replays;
     return check_cuda(h, cudaGraphLaunch(g.exec, h->stream), "graph launch");
 }
 
 bool steady(const rd_handle* h, double dt) {
+    // the table's force scale is dt in the arithmetic type (ensure_table(h, dt, (T)dt))
+    const double fs = h->prm.precision == RD_FP64 ? dt : (double)(float)dt;
     return h->use_graphs && !h->timing && !h->capturing && h->n > 0 && h->keys_valid && !h->sorted && h->fgrid_valid &&
            h->fgrid_dt == dt && h->grid_mode == GRID_FUSED &&
-           (!batched(h) || (h->table_valid && h->table_dt == dt && h->table_fs == dt));
+           (!batched(h) || (h->table_valid && h->table_dt == dt && h->table_fs == fs));
 }
 
 template <typename T> rd_status steps_impl(rd_handle* h, double dt, int nsteps) {
@@ -2026,6 +2030,12 @@ rd_status rd_kernel_timing(rd_handle* h, int kernel, uint64_t* launches, double*
 rd_status rd_launch_count(rd_handle* h, uint64_t* count) {
     if (!h || !count) return RD_INVALID_ARG;
     *count = h->launches;
+    return RD_OK;
+}
+
+rd_status rd_graph_replays(rd_handle* h, uint64_t* count) {
+    if (!h || !count) return RD_INVALID_ARG;
+    *count = h->graph_replays;
     return RD_OK;
 }
 

@@ -102,6 +102,27 @@ def test_graph_replay_matches_eager_launches(built_pkg):
         assert rel(out[0][k], out[1][k]) < 1e-5
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_steady_steps_replay_graphs_in_batches_and_single_scenes(built_pkg, precision):
+    """dt = 1e-4 has no exact FP32 value: the batch's scene table, built with
+    dt in the arithmetic type, still counts as current for the graph."""
+    batch = small_batch(seed=8, nscenes=3)
+    dt_ = np.float64 if precision else np.float32
+    handles = [built_pkg.Batch([scene_params(built_pkg, sc, precision=precision) for sc in batch]),
+               built_pkg.Simulation(scene_params(built_pkg, batch[0], precision=precision))]
+    for i, sc in enumerate(batch):
+        handles[0].set_particles(i, sc.x.astype(dt_), sc.v.astype(dt_), sc.mass.astype(dt_))
+    sc = batch[0]
+    handles[1].set_particles(sc.x.astype(dt_), sc.v.astype(dt_), sc.mass.astype(dt_))
+    for h in handles:
+        h.init_volumes()
+        h.step(1e-4, 3)
+        r0 = h.graph_replays()
+        h.step(1e-4, 10)
+        assert h.graph_replays() - r0 == 5
+        assert h.flags() == 0
+
+
 def test_autotune_picks_a_valid_pair_and_restores_state(built_pkg):
     batch = small_batch(seed=7, nscenes=4)
     dt = batch[0].dt
