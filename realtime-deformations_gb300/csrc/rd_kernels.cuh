@@ -204,10 +204,11 @@ __global__ void __launch_bounds__(256) k_keys(DevParams<T> P0, DevBufs D, const 
 // sorted slot of each cell), emission of the work items and reset of the
 // counts for the next histogram, over kScanTile-key tiles on all SMs:
 // k_tile_sums adds up each tile from the block counts, k_tile_prefix turns
-// the tile sums into their exclusive prefix (one CTA), and k_scan scans one
-// tile (64 whole blocks) per CTA from its prefix; empty tiles return at once
-// and only occupied blocks read or write their cells, so empty grid space
-// costs 4 bytes per block.  A block of c particles becomes ceil(c / wp) work items of nearly
+// the tile sums into their exclusive prefix and lists the non-empty tiles (one
+// CTA), and k_scan, a persistent grid over that list, scans one tile (64 whole
+// blocks) per CTA trip from its prefix; empty tiles cost no CTA and only
+// occupied blocks read or write their cells, so empty grid space costs 4 bytes
+// per block.  A block of c particles becomes ceil(c / wp) work items of nearly
 // equal size; the items are appended to the list through an atomic counter
 // (their order does not matter) and the counter of the next sort is cleared
 // here.
@@ -248,110 +249,135 @@ __global__ void __launch_bounds__(256) k_tile_sums(const uint32_t* __restrict__ 
 
 // In place: sums[t] -> sum of sums[0 .. t-1] for t < ntiles, sums[ntiles] =
 // the total (which must be the particle count); also clears the item counter
-// of the next sort.  One CTA of 1024 threads.
+// of the next sort.  With `list` given, the indices of the non-empty tiles
+// go to list[0 ..) in ascending order and their number to list[ntiles].  One
+// CTA of 1024 threads; each thread takes kPrefixPer consecutive tiles per
+// trip, loaded together, so the trips (and their barriers) are few.
+constexpr int kPrefixPer = 8;
+
 __global__ void __launch_bounds__(1024) k_tile_prefix(uint32_t* __restrict__ sums, int ntiles,
                                                       uint32_t* __restrict__ nwork_next_sort, uint32_t n_expected,
-                                                      uint32_t* flags) {
-    __shared__ uint32_t s_w[32];
-    __shared__ uint32_t s_carry;
+                                                      uint32_t* flags, uint32_t* __restrict__ list) {
+    __shared__ uint2 s_w[32];   // per warp: (particles, non-empty tiles)
+    __shared__ uint2 s_carry;   // totals of the previous trips
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) { s_carry = 0u; *nwork_next_sort = 0u; }
+    if (tid == 0) { s_carry = make_uint2(0u, 0u); *nwork_next_sort = 0u; }
     __syncthreads();
-    for (int base = 0; base < ntiles; base += 1024) {
-        const int t = base + tid;
-        const uint32_t v = t < ntiles ? sums[t] : 0u;
-        uint32_t x = v;
+    for (int base = 0; base < ntiles; base += 1024 * kPrefixPer) {
+        const int t0 = base + tid * kPrefixPer;
+        uint32_t v[kPrefixPer];
+        uint32_t s = 0u, o = 0u;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
+        for (int j = 0; j < kPrefixPer; ++j) v[j] = t0 + j < ntiles ? sums[t0 + j] : 0u;
+#pragma unroll
+        for (int j = 0; j < kPrefixPer; ++j) { s += v[j]; o += v[j] != 0u; }
+        uint32_t xs = s, xo = o;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t ys = __shfl_up_sync(0xffffffffu, xs, d), yo = __shfl_up_sync(0xffffffffu, xo, d);
+            if (lane >= d) { xs += ys; xo += yo; }
         }
-        if (lane == 31) s_w[wid] = x;
+        if (lane == 31) s_w[wid] = make_uint2(xs, xo);
         __syncthreads();
         if (wid == 0) {
-            uint32_t wsum = s_w[lane];
+            uint2 w = s_w[lane];
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, wsum, o);
-                if (lane >= o) wsum += y;
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t ys = __shfl_up_sync(0xffffffffu, w.x, d), yo = __shfl_up_sync(0xffffffffu, w.y, d);
+                if (lane >= d) { w.x += ys; w.y += yo; }
             }
-            s_w[lane] = wsum;
+            s_w[lane] = w;  // inclusive over warps
         }
         __syncthreads();
-        const uint32_t incl = s_carry + (wid ? s_w[wid - 1] : 0u) + x;
-        if (t < ntiles) sums[t] = incl - v;
-        __syncthreads();
-        if (tid == 1023) s_carry = incl;
+        const uint2 c = s_carry;
+        const uint2 wp = wid ? s_w[wid - 1] : make_uint2(0u, 0u);
+        uint32_t es = c.x + wp.x + xs - s, eo = c.y + wp.y + xo - o;
+#pragma unroll
+        for (int j = 0; j < kPrefixPer; ++j) {
+            if (t0 + j < ntiles) {
+                sums[t0 + j] = es;
+                if (list && v[j]) list[eo++] = (uint32_t)(t0 + j);
+                es += v[j];
+            }
+        }
+        __syncthreads();  // s_carry and s_w read by every thread
+        if (tid == 0) s_carry = make_uint2(c.x + s_w[31].x, c.y + s_w[31].y);
         __syncthreads();
     }
     if (tid == 0) {
-        sums[ntiles] = s_carry;
-        if (s_carry != n_expected) atomicOr(flags, 4u);
+        sums[ntiles] = s_carry.x;
+        if (list) list[ntiles] = s_carry.y;
+        if (s_carry.x != n_expected) atomicOr(flags, 4u);
     }
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ counts, uint32_t* __restrict__ cursor,
                                                        uint32_t* __restrict__ bcount,
-                                                       const uint32_t* __restrict__ tile_pre, int nkeys,
+                                                       const uint32_t* __restrict__ tile_pre,
+                                                       const uint32_t* __restrict__ tile_list, int ntiles, int nkeys,
                                                        int4* __restrict__ work, uint32_t* __restrict__ nwork,
                                                        uint32_t work_cap, uint32_t wp, uint32_t* flags,
                                                        const uint32_t* __restrict__ sblock, int nscenes) {
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_blk[kBlocksPerTile];  // particles per block of this tile
-    const int t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const uint32_t s_off = tile_pre[t];
-    if (tile_pre[t + 1] == s_off) return;  // no particle in this tile
-    const int k0 = t * kScanTile + tid * kScanPer;
-    // the cell counts of an empty block are zero and its cursor is never read:
-    // only occupied blocks touch their 64 cells
-    const int gblk = k0 / kCellsPerBlock;
-    const uint32_t bsum = gblk * kCellsPerBlock < nkeys ? bcount[gblk] : 0u;
-    const uint4 c = bsum ? ld4_or_zero(counts, k0, nkeys) : make_uint4(0u, 0u, 0u, 0u);
-    const uint32_t tc = c.x + c.y + c.z + c.w;
-    if ((tid & (kThreadsPerBlockKeys - 1)) == 0) s_blk[tid / kThreadsPerBlockKeys] = bsum;
-    uint32_t ic = tc;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, ic, o);
-        if (lane >= o) ic += y;
-    }
-    __syncthreads();
-    if (lane == 31) s_w[wid] = ic;
-    __syncthreads();
-    if (wid == 0) {
-        uint32_t wc = s_w[lane];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t nocc = tile_list[ntiles];
+    for (uint32_t it = blockIdx.x; it < nocc; it += gridDim.x) {
+        const int t = (int)tile_list[it];
+        const uint32_t s_off = tile_pre[t];
+        const int k0 = t * kScanTile + tid * kScanPer;
+        // the cell counts of an empty block are zero and its cursor is never read:
+        // only occupied blocks touch their 64 cells
+        const int gblk = k0 / kCellsPerBlock;
+        const uint32_t bsum = gblk * kCellsPerBlock < nkeys ? bcount[gblk] : 0u;
+        const uint4 c = bsum ? ld4_or_zero(counts, k0, nkeys) : make_uint4(0u, 0u, 0u, 0u);
+        const uint32_t tc = c.x + c.y + c.z + c.w;
+        if ((tid & (kThreadsPerBlockKeys - 1)) == 0) s_blk[tid / kThreadsPerBlockKeys] = bsum;
+        uint32_t ic = tc;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, wc, o);
-            if (lane >= o) wc += y;
+            const uint32_t y = __shfl_up_sync(0xffffffffu, ic, o);
+            if (lane >= o) ic += y;
         }
-        s_w[lane] = wc;  // inclusive prefix over warps
-    }
-    __syncthreads();
-    const uint32_t st0 = s_off + (wid ? s_w[wid - 1] : 0u) + ic - tc;
-    if (bsum) {
-        st4(cursor, k0, nkeys, make_uint4(st0, st0 + c.x, st0 + c.x + c.y, st0 + c.x + c.y + c.z));
-        st4(counts, k0, nkeys, make_uint4(0u, 0u, 0u, 0u));
-    }
-    // the first thread of each block emits the block's work items and clears
-    // the block count for the next histogram
-    if ((tid & (kThreadsPerBlockKeys - 1)) == 0) {
-        const int b = tid / kThreadsPerBlockKeys;
-        const uint32_t bc = s_blk[b];
-        if (bc) bcount[gblk] = 0u;
-        const uint32_t ni = (bc + wp - 1) / wp;
-        if (ni) {
-            const uint32_t blk = (uint32_t)(t * kBlocksPerTile + b);
-            const int scene = nscenes > 1 ? scene_of(sblock, nscenes, blk) : 0;
-            uint32_t oi = atomicAdd(nwork, ni);
-            uint32_t st = st0;
-            for (uint32_t j = 0; j < ni; ++j, ++oi) {
-                const uint32_t cnt = bc / ni + (j < bc % ni ? 1u : 0u);
-                if (oi < work_cap) work[oi] = make_int4((int)blk, (int)st, (int)cnt, scene);
-                else atomicOr(flags, 4u);
-                st += cnt;
+        __syncthreads();
+        if (lane == 31) s_w[wid] = ic;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t wc = s_w[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, wc, o);
+                if (lane >= o) wc += y;
+            }
+            s_w[lane] = wc;  // inclusive prefix over warps
+        }
+        __syncthreads();
+        const uint32_t st0 = s_off + (wid ? s_w[wid - 1] : 0u) + ic - tc;
+        if (bsum) {
+            st4(cursor, k0, nkeys, make_uint4(st0, st0 + c.x, st0 + c.x + c.y, st0 + c.x + c.y + c.z));
+            st4(counts, k0, nkeys, make_uint4(0u, 0u, 0u, 0u));
+        }
+        // the first thread of each block emits the block's work items and clears
+        // the block count for the next histogram
+        if ((tid & (kThreadsPerBlockKeys - 1)) == 0) {
+            const int b = tid / kThreadsPerBlockKeys;
+            const uint32_t bc = s_blk[b];
+            if (bc) bcount[gblk] = 0u;
+            const uint32_t ni = (bc + wp - 1) / wp;
+            if (ni) {
+                const uint32_t blk = (uint32_t)(t * kBlocksPerTile + b);
+                const int scene = nscenes > 1 ? scene_of(sblock, nscenes, blk) : 0;
+                uint32_t oi = atomicAdd(nwork, ni);
+                uint32_t st = st0;
+                for (uint32_t j = 0; j < ni; ++j, ++oi) {
+                    const uint32_t cnt = bc / ni + (j < bc % ni ? 1u : 0u);
+                    if (oi < work_cap) work[oi] = make_int4((int)blk, (int)st, (int)cnt, scene);
+                    else atomicOr(flags, 4u);
+                    st += cnt;
+                }
             }
         }
+        __syncthreads();  // s_blk and s_w are refilled by the next tile
     }
 }
 

@@ -220,6 +220,7 @@ struct rd_handle {
     uint32_t* nwork2 = nullptr;  // two item counters: the current sort's and the next's
     int nb = 0;                  // nwork2[nb] belongs to the last sort
     uint32_t* tile_sums = nullptr;
+    uint32_t* tile_list = nullptr;  // non-empty tiles of the current sort, their count last
     size_t work_cap = 0;
     void* grid[2] = {nullptr, nullptr};  // (m, p) of this step / the next (fused); (m, v) in stage mode
     int g = 0;                           // current grid buffer
@@ -465,10 +466,12 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     long t = tmark_begin(h, RD_KERNEL_SCAN);
     k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, h->stream>>>(h->bcount, h->nblocks, ntiles,
                                                                              h->tile_sums);
-    k_tile_prefix<<<1, 1024, 0, h->stream>>>(h->tile_sums, ntiles, nw_next, (uint32_t)h->n, h->flags);
-    k_scan<<<ntiles, kScanThreads, 0, h->stream>>>(h->counts, h->cursor, h->bcount, h->tile_sums, h->nkeys, h->work,
-                                                nw, (uint32_t)h->work_cap, (uint32_t)work_size<T>(h), h->flags,
-                                                h->d_sblock, (int)h->scenes.size());
+    k_tile_prefix<<<1, 1024, 0, h->stream>>>(h->tile_sums, ntiles, nw_next, (uint32_t)h->n, h->flags, h->tile_list);
+    const unsigned scan_grid = (unsigned)std::min<size_t>((size_t)ntiles, (size_t)h->sms * 2);
+    k_scan<<<scan_grid, kScanThreads, 0, h->stream>>>(h->counts, h->cursor, h->bcount, h->tile_sums, h->tile_list,
+                                                      ntiles, h->nkeys, h->work, nw, (uint32_t)h->work_cap,
+                                                      (uint32_t)work_size<T>(h), h->flags, h->d_sblock,
+                                                      (int)h->scenes.size());
     tmark_end(h, t);
     RD_TRY(launched(h, "k_scan", 3));
     h->nb ^= 1;
@@ -837,7 +840,7 @@ void release(rd_handle* h) {
         if (p) cudaFree(p);
     void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->bcount, h->gmark[0],
                     h->gmark[1], h->cursor, h->work,
-                    h->nwork2, h->tile_sums, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
+                    h->nwork2, h->tile_sums, h->tile_list, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
                     h->d_col, h->rgba, h->zid, h->img,
                     h->d_scenes, h->d_sblock, h->d_spoff};
     for (void* p : ptrs)
@@ -960,6 +963,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
         {(void**)&h->work, h->work_cap * sizeof(int4), true},
         {(void**)&h->nwork2, 8, true},
         {(void**)&h->tile_sums, (size_t)((h->nkeys + kScanTile - 1) / kScanTile + 1) * 4, true},
+        {(void**)&h->tile_list, (size_t)((h->nkeys + kScanTile - 1) / kScanTile + 1) * 4, true},
         {&h->grid[0], h->ncells * v4, true},
         {&h->grid[1], h->ncells * v4, true},
         {&h->gforce, h->ncells * v4, !batch},  // stage mode only
@@ -1652,7 +1656,7 @@ template <typename T> rd_status initialize_impl(rd_handle* h, const rd_init_spec
         if (st == RD_OK) {
             uint32_t* scratch = chunk + nchunks + 1;  // item counter and flags of k_tile_prefix, unused here
             k_init_count<<<nchunks, 1024, 0, h->stream>>>(S, (uint32_t)ncand, chunk);
-            k_tile_prefix<<<1, 1024, 0, h->stream>>>(chunk, (int)nchunks, scratch, 0u, scratch + 1);
+            k_tile_prefix<<<1, 1024, 0, h->stream>>>(chunk, (int)nchunks, scratch, 0u, scratch + 1, nullptr);
             k_init_place<T><<<nchunks, 1024, 0, h->stream>>>(S, (uint32_t)ncand, chunk, n, pl);
             st = launched(h, "k_init", 3);
         }
@@ -2060,6 +2064,7 @@ struct NaScratch {
     uint32_t bcount[kNaMaxKeys / kCellsPerBlock];
     uint32_t cursor[kNaMaxKeys];
     uint32_t tile_sums[kNaMaxTiles + 1];
+    uint32_t tile_list[kNaMaxTiles + 1];
     uint32_t nwork[2];
     uint32_t flags;
 };
@@ -2191,10 +2196,12 @@ extern "C" rd_status rd_rasterize_noalloc(const rd_params* params, const rd_part
         k_na_keys<<<blocks_for(n, 256), 256, 0, st>>>(P, static_cast<const float*>(in->x), sc->keys, sc->counts,
                                                       sc->bcount, &sc->flags);
         k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, st>>>(sc->bcount, hp.nblocks, ntiles, sc->tile_sums);
-        k_tile_prefix<<<1, 1024, 0, st>>>(sc->tile_sums, ntiles, &sc->nwork[1], (uint32_t)n, &sc->flags);
-        k_scan<<<ntiles, kScanThreads, 0, st>>>(sc->counts, sc->cursor, sc->bcount, sc->tile_sums, hp.nkeys, sc->work,
-                                                &sc->nwork[0], work_cap, (uint32_t)WorkP<float>::value, &sc->flags,
-                                                nullptr, 1);
+        k_tile_prefix<<<1, 1024, 0, st>>>(sc->tile_sums, ntiles, &sc->nwork[1], (uint32_t)n, &sc->flags,
+                                          sc->tile_list);
+        const unsigned scan_grid = (unsigned)std::min<size_t>((size_t)ntiles, (size_t)nd.sms * 2);
+        k_scan<<<scan_grid, kScanThreads, 0, st>>>(sc->counts, sc->cursor, sc->bcount, sc->tile_sums, sc->tile_list,
+                                                   ntiles, hp.nkeys, sc->work, &sc->nwork[0], work_cap,
+                                                   (uint32_t)WorkP<float>::value, &sc->flags, nullptr, 1);
         k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(n, sc->keys, sc->cursor, sc->perm);
         const size_t max_items = (size_t)n / WorkP<float>::value + (size_t)std::min<int64_t>(nblocks, n) + 1;
         const unsigned grid = (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)nd.sms * nd.occ));
