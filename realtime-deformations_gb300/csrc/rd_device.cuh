@@ -71,15 +71,27 @@ __device__ __forceinline__ void load_particle(const vec4<T>* __restrict__ pl, si
     p.F[7] = g.x; p.F[8] = g.y; p.Jp = g.z; p.id = real_to_id<T>(g.w);
 }
 
+// Planes 0-4 (x, m, v, volume, B, F00..F02) and planes 5-6 (F10..F22, J_P,
+// id) can be stored apart: the F_E / J_P part is final before the G2P gather.
 template <typename T>
-__device__ __forceinline__ void store_particle(vec4<T>* __restrict__ pl, size_t n, size_t i, const Particle<T>& p) {
+__device__ __forceinline__ void store_particle_front(vec4<T>* __restrict__ pl, size_t n, size_t i,
+                                                     const Particle<T>& p) {
     st_stream(pl + 0 * n + i, mk4<T>(p.x[0], p.x[1], p.x[2], p.m));
     st_stream(pl + 1 * n + i, mk4<T>(p.v[0], p.v[1], p.v[2], p.vol));
     st_stream(pl + 2 * n + i, mk4<T>(p.B[0], p.B[1], p.B[2], p.B[3]));
     st_stream(pl + 3 * n + i, mk4<T>(p.B[4], p.B[5], p.B[6], p.B[7]));
     st_stream(pl + 4 * n + i, mk4<T>(p.B[8], p.F[0], p.F[1], p.F[2]));
+}
+template <typename T>
+__device__ __forceinline__ void store_particle_back(vec4<T>* __restrict__ pl, size_t n, size_t i,
+                                                    const Particle<T>& p) {
     st_stream(pl + 5 * n + i, mk4<T>(p.F[3], p.F[4], p.F[5], p.F[6]));
     st_stream(pl + 6 * n + i, mk4<T>(p.F[7], p.F[8], p.Jp, id_to_real<T>(p.id)));
+}
+template <typename T>
+__device__ __forceinline__ void store_particle(vec4<T>* __restrict__ pl, size_t n, size_t i, const Particle<T>& p) {
+    store_particle_front(pl, n, i, p);
+    store_particle_back(pl, n, i, p);
 }
 
 template <typename T>

@@ -532,11 +532,14 @@ __device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T
     }
 }
 
-// P F^T of F = U sc V^T (the split just made), as stress_PFt computes it
-// from an SVD of F: U diag(2 mu (sc - d) sc) U^T + lambda (J - 1) J I with
-// J = sgn prod sc and J - 1 expanded in sc - 1 so nothing cancels.
+// scale * P F^T of F = U sc V^T (the split just made), as stress_PFt computes
+// it from an SVD of F: U diag(2 mu (sc - d) sc) U^T + lambda (J - 1) J I with
+// J = sgn prod sc and J - 1 expanded in sc - 1 so nothing cancels.  The
+// matrix is symmetric; its entries 00 01 02 11 12 22 go to out, each formed
+// as sum_k (U_rk U_ck) dg_k so that the rounding is symmetric too.
 template <typename T>
-__device__ __forceinline__ void stress_from_split(const DevParams<T>& P, const Split<T>& sp, T Jp, T out[9]) {
+__device__ __forceinline__ void stress_from_split(const DevParams<T>& P, const Split<T>& sp, T Jp, T scale,
+                                                  T out[6]) {
     const T e0 = sp.scm1[0], e1 = sp.scm1[1], e2 = sp.scm1[2];
     const T pm1 = (e0 + e1 + e2) + (e0 * e1 + e0 * e2 + e1 * e2) + e0 * e1 * e2;  // prod sc - 1
     const T J = sp.sgn > T(0) ? T(1) + pm1 : -(T(1) + pm1);
@@ -553,12 +556,18 @@ __device__ __forceinline__ void stress_from_split(const DevParams<T>& P, const S
         dg[c] = T(2) * mu * sm * sp.sc[c];
     }
     const T iso = lam * jm1 * J;
+    int k = 0;
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-            out[3 * r + c] = sp.U[3 * r] * dg[0] * sp.U[3 * c] + sp.U[3 * r + 1] * dg[1] * sp.U[3 * c + 1] +
-                             sp.U[3 * r + 2] * dg[2] * sp.U[3 * c + 2] + (r == c ? iso : T(0));
+        for (int c = r; c < 3; ++c, ++k)
+            out[k] = scale * ((sp.U[3 * r] * sp.U[3 * c]) * dg[0] + (sp.U[3 * r + 1] * sp.U[3 * c + 1]) * dg[1] +
+                              (sp.U[3 * r + 2] * sp.U[3 * c + 2]) * dg[2] + (r == c ? iso : T(0)));
+}
+
+// Index into the 6 entries of a symmetric 3x3 matrix (00 01 02 11 12 22).
+__host__ __device__ constexpr int sym6(int r, int c) {
+    return r <= c ? (r == 0 ? c : (r == 1 ? 2 + c : 5)) : (c == 0 ? r : (c == 1 ? 2 + r : 5));
 }
 
 template <typename T>
@@ -1068,8 +1077,28 @@ __device__ __forceinline__ void g2p_gather(const vec4<T>* __restrict__ gv, const
     }
 }
 
-// One work item of k_g2p2g; P is the item's scene.
+// updateDeformationGradient of one particle with velocity gradient Bm (the
+// lagged B, or the one just gathered): F_E, J_P (and F_P) updated and
+// stored (planes 5-6 and the F_P planes), the finite check of those, and
+// the scaled stress sc P F^T of the next P2G as 6 symmetric entries.
 template <typename T, bool TRACK_FP>
+__device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T>& p, T FP[9], const T Bm[9],
+                                               vec4<T>* __restrict__ pout, size_t n, size_t s, T G6[6],
+                                               bool& finite) {
+    Split<T> sp;
+    update_F<T, TRACK_FP>(P, Bm, p.F, p.Jp, FP, sp);
+    stress_from_split(P, sp, p.Jp, P.fscale * (p.vol * P.dinv), G6);
+    store_particle_back(pout, n, s, p);
+    if (TRACK_FP) store_fp(pout, n, s, FP);
+    finite = isfinite(p.Jp);
+#pragma unroll
+    for (int e = 0; e < 9; ++e) finite = finite && isfinite(p.F[e]);
+}
+
+// One work item of k_g2p2g; P is the item's scene.  LAGGED: the F update
+// uses the B of the previous G2P (the reference's order), else the B just
+// gathered.
+template <typename T, bool TRACK_FP, bool LAGGED>
 __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
                                            const int4 it) {
     constexpr int CA = kBlk + 2;
@@ -1119,29 +1148,32 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         __syncthreads();
         if (j < count) {
             const int s = it.y + j;
+            // the plastic split first: the stress of the next P2G (6 entries)
+            // and the F_E / J_P / F_P planes are final after it, so none of the
+            // split is live across the gather
+            T G6[6];
+            bool finite = true;
+            if constexpr (LAGGED) split_particle<T, TRACK_FP>(P, p, FP, p.B, pout, n, s, G6, finite);
             Stencil<T> St;
             const bool ok = make_stencil(P, p.x, org, St);
             if (!ok) raise_flag(D.flags, 4u);
-            Split<T> sp;
-            if (P.lagged) update_F<T, TRACK_FP>(P, p.B, p.F, p.Jp, FP, sp);
             T vp[3] = {T(0), T(0), T(0)};
             T Bp[9];
 #pragma unroll
             for (int e = 0; e < 9; ++e) Bp[e] = T(0);
             if (ok) g2p_gather(S.gv, St, vp, Bp);
-            if (!P.lagged) update_F<T, TRACK_FP>(P, Bp, p.F, p.Jp, FP, sp);
+            if constexpr (!LAGGED) split_particle<T, TRACK_FP>(P, p, FP, Bp, pout, n, s, G6, finite);
 #pragma unroll
             for (int a = 0; a < 3; ++a) p.v[a] = vp[a];
 #pragma unroll
             for (int e = 0; e < 9; ++e) p.B[e] = Bp[e];
 #pragma unroll
             for (int a = 0; a < 3; ++a) p.x[a] = clampx(p.x[a] + p.v[a] * P.dt, P.xlo, P.xhi[a]);
-            store_particle(pout, n, s, p);
-            if (TRACK_FP) store_fp(pout, n, s, FP);
-            bool finite = isfinite(p.x[0]) && isfinite(p.x[1]) && isfinite(p.x[2]) && isfinite(p.v[0]) &&
-                          isfinite(p.v[1]) && isfinite(p.v[2]) && isfinite(p.Jp);
+            store_particle_front(pout, n, s, p);
+            finite = finite && isfinite(p.x[0]) && isfinite(p.x[1]) && isfinite(p.x[2]) && isfinite(p.v[0]) &&
+                     isfinite(p.v[1]) && isfinite(p.v[2]);
 #pragma unroll
-            for (int e = 0; e < 9; ++e) finite = finite && isfinite(p.F[e]) && isfinite(p.B[e]);
+            for (int e = 0; e < 9; ++e) finite = finite && isfinite(p.B[e]);
             if (!finite) raise_flag(D.flags, 2u);
             // next step's P2G record
             Stencil<T> S2;
@@ -1150,11 +1182,11 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             D.keys_out[s] = key;
             count_key(D.counts, D.bcount, key);
             if (!stencil_in_grid(P, S2.b)) raise_flag(D.flags, 1u);
-            T G[9], A[9], mv[3];
-            stress_from_split(P, sp, p.Jp, G);
-            const T sc = P.fscale * (p.vol * P.dinv);
+            T A[9], mv[3];
 #pragma unroll
-            for (int e = 0; e < 9; ++e) A[e] = p.m * (p.B[e] * P.dinv) - sc * G[e];
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) A[3 * r + c] = p.m * (p.B[3 * r + c] * P.dinv) - G6[sym6(r, c)];
 #pragma unroll
             for (int a = 0; a < 3; ++a) mv[a] = p.m * p.v[a];
             vec4<T>* rec = &S.p.rec[j * kRecV4];
@@ -1180,7 +1212,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
 
 // BATCH: the work items belong to different scenes (D.scenes); otherwise all
 // to the scene P0.
-template <typename T, bool TRACK_FP, bool BATCH>
+template <typename T, bool TRACK_FP, bool BATCH, bool LAGGED>
 __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlocks : 1)
     k_g2p2g(DevParams<T> P0, DevBufs D) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -1191,9 +1223,9 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
         if constexpr (BATCH) {
             copy_scene(S.par, D.scenes, it.w);
             __syncthreads();
-            g2p2g_item<T, TRACK_FP>(S.par, D, S, it);
+            g2p2g_item<T, TRACK_FP, LAGGED>(S.par, D, S, it);
         } else {
-            g2p2g_item<T, TRACK_FP>(P0, D, S, it);
+            g2p2g_item<T, TRACK_FP, LAGGED>(P0, D, S, it);
         }
     }
 }

@@ -484,6 +484,16 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     return RD_OK;
 }
 
+// The k_g2p2g instantiation for this handle: batch or single scene, with or
+// without the full F_P, and the order of the F update.
+template <typename T> using FusedKernel = void (*)(DevParams<T>, DevBufs);
+template <typename T> FusedKernel<T> fused_kernel(const rd_handle* h) {
+    const bool lag = h->prm.lagged_b != 0;
+    if (batched(h)) return lag ? k_g2p2g<T, false, true, true> : k_g2p2g<T, false, true, false>;
+    if (h->prm.track_fp) return lag ? k_g2p2g<T, true, false, true> : k_g2p2g<T, true, false, false>;
+    return lag ? k_g2p2g<T, false, false, true> : k_g2p2g<T, false, false, false>;
+}
+
 template <typename T> unsigned persistent_grid(const rd_handle* h, int occ) {
     const size_t max_items = (size_t)h->n / work_size<T>(h) + (size_t)std::min<int64_t>(h->nblocks, h->n) + 1;
     const int per_sm = h->grid_mult > 0 ? std::min(h->grid_mult, occ) : occ;
@@ -537,12 +547,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
     DevBufs D = bufs<T>(h);
     t = tmark_begin(h, RD_KERNEL_G2P2G);
     const unsigned fg = persistent_grid<T>(h, h->occ_g2p);
-    if (batch)
-        k_g2p2g<T, false, true><<<fg, kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
-    else if (h->prm.track_fp)
-        k_g2p2g<T, true, false><<<fg, kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
-    else
-        k_g2p2g<T, false, false><<<fg, kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
+    fused_kernel<T>(h)<<<fg, kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
     tmark_end(h, t);
     RD_TRY(launched(h, "k_g2p2g"));
     h->cur ^= 1;
@@ -797,11 +802,8 @@ template <typename T> rd_status occupancy(rd_handle* h) {
     RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true, false>, kThreads, sm), "occ"));
     h->occ_p2g = std::max(1, o);
     const int fsm = (int)sizeof(FusedShared<T>);
-    const void* fused[] = {(const void*)k_g2p2g<T, true, false>, (const void*)k_g2p2g<T, false, false>,
-                           (const void*)k_g2p2g<T, false, true>};
-    for (const void* f : fused)
-        RD_TRY(check_cuda(h, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm), "smem attr"));
-    const void* used = batched(h) ? fused[2] : (h->prm.track_fp ? fused[0] : fused[1]);
+    const void* used = (const void*)fused_kernel<T>(h);
+    RD_TRY(check_cuda(h, cudaFuncSetAttribute(used, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm), "smem attr"));
     RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, used, kFusedThreads, fsm), "occ"));
     h->occ_g2p = std::max(1, o);
     return RD_OK;
