@@ -23,6 +23,7 @@ template <typename T> struct DevParams {
     int nkeys;     // blocks x 64 cells
     int n;         // particles
     T h, dinv, dt;
+    T hinv_pow2;   // 1 / h when h is a power of two (x / h == x * hinv_pow2 exactly), else 0
     T mu0, lambda0, xi;
     T lo, hi;      // singular value clamp
     T g[3];
@@ -415,7 +416,7 @@ __device__ __forceinline__ bool make_stencil(const DevParams<T>& P, const T x[3]
     bool ok = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const T t = div_rn(x[a], P.h);
+        const T t = P.hinv_pow2 != T(0) ? x[a] * P.hinv_pow2 : div_rn(x[a], P.h);
         S.b[a] = (int)t;
         bspline4(t, S.b[a], S.w[a]);
 #pragma unroll
@@ -807,6 +808,48 @@ __device__ __forceinline__ void p2g_flush_lane(P2GTile<T, CA>& S, int c, int ox,
     }
 }
 
+// Counting sort of the records by cell when every record already holds its
+// rank among its cell's records (the value its count atomic returned): one
+// scan of the counts into S.off, then each thread places its own record
+// (cell 0xff: none).  S.cnt keeps the counts.  Called by every thread.
+template <typename T, int CA>
+__device__ __forceinline__ void sort_ranked(P2GTile<T, CA>& S, int j, int cell, int rank) {
+    constexpr int NC = P2GTile<T, CA>::NC;
+    constexpr int PER = (NC + 31) / 32;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int l = threadIdx.x;
+        int loc[PER];
+        int tot = 0;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int c = l * PER + k;
+            loc[k] = c < NC ? S.cnt[c] : 0;
+            tot += loc[k];
+        }
+        int x = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (l >= o) x += y;
+        }
+        int run = x - tot;
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int c = l * PER + k;
+            if (c < NC) S.off[c] = run;
+            run += loc[k];
+        }
+    }
+    __syncthreads();
+    if (cell != 0xff) {
+        const int k = S.off[cell] + rank;
+        S.order[k] = (uint16_t)j;
+        S.scell[k] = (uint8_t)cell;
+    }
+    __syncthreads();
+}
+
 template <typename T, bool MOM, int CA>
 __device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int count) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -1146,6 +1189,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         for (int c = threadIdx.x; c < 4 * P2GTile<T, CA>::TC; c += blockDim.x) S.p.tile[c] = T(0);
         for (int c = threadIdx.x; c < P2GTile<T, CA>::NC; c += blockDim.x) S.p.cnt[c] = 0;
         __syncthreads();
+        int rcell = 0xff, rrank = 0;  // this thread's record: cell and rank within it
         if (j < count) {
             const int s = it.y + j;
             // the plastic split first: the stress of the next P2G (6 entries)
@@ -1192,16 +1236,16 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             vec4<T>* rec = &S.p.rec[j * kRecV4];
             write_record<T, true>(rec, S2, p.x, A, mv, p.m, P.h);
             if (in_space) {
-                const int cell = (S2.rel[0] * CA + S2.rel[1]) * CA + S2.rel[2];
-                S.p.cellof[j] = (uint8_t)cell;
-                atomicAdd(&S.p.cnt[cell], 1);
+                rcell = (S2.rel[0] * CA + S2.rel[1]) * CA + S2.rel[2];
+                S.p.cellof[j] = (uint8_t)rcell;
+                rrank = atomicAdd(&S.p.cnt[rcell], 1);
             } else {
                 S.p.cellof[j] = 0xff;
                 p2g_direct(P, rec, S2.b, gnext);
                 mark_stencil(P, D.gmark_next, S2.b);
             }
         }
-        sort_records<T, CA>(S.p, count);
+        sort_ranked<T, CA>(S.p, j, rcell, rrank);
         p2g_tasks<T, true, CA>(S.p, count);
         __syncthreads();
         p2g_flush<T, CA>(P, S.p, porg, gnext);

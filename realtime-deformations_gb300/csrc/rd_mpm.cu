@@ -296,6 +296,8 @@ DevParams<T> params_of(const rd_params& p, const int NB[3], int nkeys, int n, do
     const T hh = (T)p.h;
     P.h = hh;
     P.dinv = reference_dinv<T>(hh);
+    int he = 0;
+    P.hinv_pow2 = std::frexp((double)hh, &he) == 0.5 ? (T)std::ldexp(1.0, 1 - he) : T(0);
     P.dt = (T)dt;
     // material_point_method.cpp:237-242, in the element type
     volatile T E = (T)p.E, nu = (T)p.nu;
