@@ -279,7 +279,7 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
         }
         S.gv[c] = mk4<T>(vh[0], vh[1], vh[2], T(0));
     }
-    for (int c = threadIdx.x; c < 4 * P2GTile<T, kBlk>::TC; c += blockDim.x) S.p.tile[c] = T(0);
+    zero_tile(S.p);
     for (int c = threadIdx.x; c < P2GTile<T, kBlk>::NC; c += blockDim.x) S.p.cnt[c] = 0;
     __syncthreads();
     const int j = threadIdx.x;

@@ -706,7 +706,7 @@ template <typename T, int CA> struct P2GTile {
     static constexpr int TS = CA + 3;
     static constexpr int TC = TS * TS * TS;
     static constexpr int NC = CA * CA * CA;
-    T tile[4 * TC];
+    alignas(16) T tile[4 * TC];
     vec4<T> rec[WorkP<T>::value * kRecV4];
     int cnt[NC];
     int off[NC];
@@ -714,6 +714,15 @@ template <typename T, int CA> struct P2GTile {
     uint8_t cellof[WorkP<T>::value];
     uint8_t scell[WorkP<T>::value];  // cell of each sorted slot
 };
+
+// Zeroes the four channel planes of a P2G tile with 16-byte stores.
+template <typename T, int CA>
+__device__ __forceinline__ void zero_tile(P2GTile<T, CA>& S) {
+    static_assert((4 * P2GTile<T, CA>::TC * sizeof(T)) % 16 == 0, "16-byte stores");
+    float4* t = reinterpret_cast<float4*>(S.tile);
+    for (int c = threadIdx.x; c < (int)(4 * P2GTile<T, CA>::TC * sizeof(T) / 16); c += blockDim.x)
+        t[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
 
 template <typename T> __device__ __forceinline__ T pick4(const vec4<T>& v, int i) {
     return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
@@ -973,7 +982,7 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
     const vec4<T>* __restrict__ pl = static_cast<const vec4<T>*>(D.pin);
     vec4<T>* __restrict__ grid = static_cast<vec4<T>*>(MOM ? D.grid : D.gforce) + P.goff;
     const size_t n = (size_t)P.n;
-    for (int c = threadIdx.x; c < 4 * P2GTile<T, kBlk>::TC; c += blockDim.x) S.tile[c] = T(0);
+    zero_tile(S);
     for (int c = threadIdx.x; c < P2GTile<T, kBlk>::NC; c += blockDim.x) S.cnt[c] = 0;
     int org[3];
     tile_origin(P, it.x, org);
@@ -1186,7 +1195,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             }
             S.gv[c] = mk4<T>(v0, v1, v2, T(0));
         }
-        for (int c = threadIdx.x; c < 4 * P2GTile<T, CA>::TC; c += blockDim.x) S.p.tile[c] = T(0);
+        zero_tile(S.p);
         for (int c = threadIdx.x; c < P2GTile<T, CA>::NC; c += blockDim.x) S.p.cnt[c] = 0;
         __syncthreads();
         int rcell = 0xff, rrank = 0;  // this thread's record: cell and rank within it
