@@ -259,7 +259,23 @@ def measure_batched(pkg, local, steps, warmup, plain_value):
         seq_ms += e0.elapsed_time(e1)
         one.close()
     seq_value = b.n * seq_steps / (seq_ms / 1e3)
+    # the plain forward at the batch's particle density: the two-ball scene at 8
+    # particles per cell (474,282 particles; the 1.1M headline scene holds ~18.6)
+    tb = scenes.two_balls()
+    one = pkg.Simulation(pkg.make_params(*tb.grid, tb.n, tb.h, device=local, **tb.params()))
+    one.set_particles(tb.x, tb.v, tb.mass)
+    one.init_volumes()
+    one.step(tb.dt, warmup)
+    st = torch.cuda.ExternalStream(one.stream(), device=local)
+    one.synchronize()
+    e0.record(st)
+    one.step(tb.dt, steps)
+    e1.record(st)
+    e1.synchronize()
+    dens_value = tb.n * steps / (e0.elapsed_time(e1) / 1e3)
+    one.close()
     return {"value": value, "unit": "particle-steps/s", "vs_plain_forward": value / plain_value,
+            "plain_forward_8_per_cell": dens_value, "vs_plain_forward_8_per_cell": value / dens_value,
             "plain_forward_one_scene_at_a_time": seq_value, "vs_one_scene_at_a_time": value / seq_value,
             "steps": steps, "warmup": warmup, "ms_per_step": ms / steps, "gpu_launches": launches,
             "scenes": len(batch), "particles": b.n, "grid_nodes": int(sum(np.prod(s.grid) for s in batch)),
