@@ -729,7 +729,10 @@ template <typename T> __device__ __forceinline__ T pick4(const vec4<T>& v, int i
 }
 
 // The record of one particle: node base - 1 + o receives w_o (m, q' + h A o),
-// q' = m v + A e with e = (base - 1) h - x.
+// q' = m v + A e with e = (base - 1) h - x.  r[0], r[1]: the x and y weights
+// at offsets 0..3; r[2]: the z weights in the order 0, 2, 1, 3, so that the two
+// z nodes of a scatter lane (oz and oz + 2) are adjacent; r[3] = (q', m);
+// r[4..6]: h A.
 template <typename T, bool MOM>
 __device__ __forceinline__ void write_record(vec4<T>* r, const Stencil<T>& St, const T x[3], const T A[9],
                                              const T mv[3], T m, T h) {
@@ -741,7 +744,7 @@ __device__ __forceinline__ void write_record(vec4<T>* r, const Stencil<T>& St, c
     for (int r = 0; r < 3; ++r) qp[r] = mv[r] + (A[3 * r] * e3[0] + A[3 * r + 1] * e3[1] + A[3 * r + 2] * e3[2]);
     r[0] = mk4<T>(St.w[0][0], St.w[0][1], St.w[0][2], St.w[0][3]);
     r[1] = mk4<T>(St.w[1][0], St.w[1][1], St.w[1][2], St.w[1][3]);
-    r[2] = mk4<T>(St.w[2][0], St.w[2][1], St.w[2][2], St.w[2][3]);
+    r[2] = mk4<T>(St.w[2][0], St.w[2][2], St.w[2][1], St.w[2][3]);  // z pairs (0, 2), (1, 3)
     r[3] = mk4<T>(qp[0], qp[1], qp[2], MOM ? m : T(0));
     r[4] = mk4<T>(h * A[0], h * A[3], h * A[6], h * A[1]);
     r[5] = mk4<T>(h * A[4], h * A[7], h * A[2], h * A[5]);
@@ -888,7 +891,7 @@ __device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int count) {
             }
             const T* rs = recs + j * (4 * kRecV4);
             const float wxy = rs[ox] * rs[4 + oy];
-            const float2 w = __fmul2_rn(make_float2(wxy, wxy), make_float2(rs[8 + oz0], rs[10 + oz0]));
+            const float2 w = __fmul2_rn(make_float2(wxy, wxy), *reinterpret_cast<const float2*>(rs + 8 + 2 * oz0));
             const vec4<T>* r = &S.rec[j * kRecV4];
             const vec4<T> qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
             // q' + h A o: the x and y offsets are common to both nodes
@@ -921,7 +924,7 @@ __device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int count) {
             }
             const T* rs = recs + j * (4 * kRecV4);
             const T wxy = rs[ox] * rs[4 + oy];
-            const T w0 = wxy * rs[8 + oz0], w1 = wxy * rs[10 + oz0];
+            const T w0 = wxy * rs[8 + 2 * oz0], w1 = wxy * rs[9 + 2 * oz0];
             const vec4<T>* r = &S.rec[j * kRecV4];
             const vec4<T> qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
             // q' + h A o; h A columns x (a4.x, a4.y, a4.z), y (a4.w, b4.x, b4.y), z (b4.z, b4.w, c4.x)
@@ -960,7 +963,7 @@ template <typename T>
 __device__ void p2g_direct(const DevParams<T>& P, const vec4<T>* r, const int b[3], vec4<T>* __restrict__ grid) {
     const vec4<T> wx4 = r[0], wy4 = r[1], wz4 = r[2], qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
     const T wx[4] = {wx4.x, wx4.y, wx4.z, wx4.w}, wy[4] = {wy4.x, wy4.y, wy4.z, wy4.w},
-            wz[4] = {wz4.x, wz4.y, wz4.z, wz4.w};
+            wz[4] = {wz4.x, wz4.z, wz4.y, wz4.w};
     for (int ox = 0; ox < 4; ++ox)
         for (int oy = 0; oy < 4; ++oy)
             for (int oz = 0; oz < 4; ++oz) {
