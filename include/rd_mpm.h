@@ -50,7 +50,8 @@ enum { RD_BC_NONE = 0, RD_BC_STICKY = 1 };
 enum {
     RD_FLAG_OUT_OF_DOMAIN = 1u << 0, /* a stencil node fell outside the grid; dropped */
     RD_FLAG_NONFINITE = 1u << 1,     /* NaN/Inf in particle state after a step */
-    RD_FLAG_BAD_WORK = 1u << 2       /* internal work-list inconsistency */
+    RD_FLAG_BAD_WORK = 1u << 2,      /* internal work-list inconsistency */
+    RD_FLAG_WAIT_TIMEOUT = 1u << 3   /* a kernel's bounded wait for a tile copy gave up; the step stopped */
 };
 
 /* Stage ids for rd_stage, in the order main.cpp:192-218 calls them. */
@@ -190,6 +191,11 @@ rd_status rd_last_error(rd_handle* h, char* buf, size_t len);
  * block * 64 + cell: block = b / 4 per axis linearised x-major like the grid,
  * cell = (b % 4) linearised the same way.  Host or device arrays per `where`. */
 rd_status rd_debug_sort(rd_handle* h, uint32_t* keys, uint32_t* order, int where);
+/* Exercises the bounded wait of the fused kernel's tile copies: one CTA waits
+ * `tries` polls on an mbarrier that nothing arrives at, raises
+ * RD_FLAG_WAIT_TIMEOUT and returns; *gave_up = 1 when the wait ran out.  No
+ * copy is issued, so nothing is left in flight. */
+rd_status rd_debug_wait_timeout(rd_handle* h, int32_t tries, int32_t* gave_up);
 /* Kernel ids for the per-kernel event timing below. */
 enum {
     RD_KERNEL_KEYS = 0,     /* block keys + histogram (when not fused into G2P) */

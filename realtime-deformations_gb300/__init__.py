@@ -37,14 +37,14 @@ STATUS_NAMES = {0: "RD_OK", 1: "RD_INVALID_ARG", 2: "RD_OOM", 3: "RD_CUDA_ERROR"
 RD_FP32, RD_FP64 = 0, 1
 RD_HOST, RD_DEVICE = 0, 1
 RD_BC_NONE, RD_BC_STICKY = 0, 1
-FLAG_OUT_OF_DOMAIN, FLAG_NONFINITE, FLAG_BAD_WORK = 1, 2, 4
+FLAG_OUT_OF_DOMAIN, FLAG_NONFINITE, FLAG_BAD_WORK, FLAG_WAIT_TIMEOUT = 1, 2, 4, 8
 STAGES = {"rasterize": 0, "forces": 1, "grid_velocities": 2, "collisions": 3,
           "deformation": 4, "particle_velocities": 5, "positions": 6, "volumes": 7}
 
 # Every symbol include/rd_mpm.h declares.
 EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "rd_get_particles",
            "rd_init_volumes", "rd_step", "rd_stage", "rd_get_grid", "rd_device_xyzs", "rd_get_flags",
-           "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort",
+           "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort", "rd_debug_wait_timeout",
            "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_graph_replays", "rd_batch_create",
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
@@ -192,6 +192,7 @@ def lib():
             L.rd_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
             L.rd_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
             L.rd_debug_sort.argtypes = [vp, vp, vp, ctypes.c_int]
+            L.rd_debug_wait_timeout.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
             L.rd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
             L.rd_graph_replays.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
             L.rd_rasterize_noalloc.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(_Particles), vp, vp]
@@ -403,6 +404,13 @@ class Simulation:
         c = ctypes.c_uint64()
         self._check(lib().rd_launch_count(self._h, ctypes.byref(c)), "rd_launch_count")
         return c.value
+
+    def debug_wait_timeout(self, tries: int = 64) -> bool:
+        """Runs the tile-copy wait against an mbarrier nothing arrives at;
+        True when it gave up (and raised RD_FLAG_WAIT_TIMEOUT)."""
+        g = ctypes.c_int32()
+        self._check(lib().rd_debug_wait_timeout(self._h, int(tries), ctypes.byref(g)), "rd_debug_wait_timeout")
+        return bool(g.value)
 
     def graph_replays(self) -> int:
         """Two-step CUDA graphs replayed so far."""

@@ -330,6 +330,49 @@ __device__ __forceinline__ void svd3_near(const T F[9], T U[9], T s[3], T sm1[3]
     }
 }
 
+// ---------------------------------------------------------------- TMA
+// Tile copies with the tensor memory accelerator: cp.async.bulk.tensor into
+// shared memory, completion tracked by an mbarrier (one arrival with the
+// expected byte count per copy).  The tensor map lives in global memory.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One elected thread: the 4-D box at (0, z, y, x) of the tensor map into dst
+// (128-byte aligned), signalling bar with `bytes`.  The innermost coordinate
+// is 0, so the copy starts on a 16-byte boundary whatever the box origin;
+// parts of the box outside the tensor read as zero.
+__device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, uint64_t* bar, uint32_t bytes, int z, int y,
+                                            int x) {
+    const uint32_t b = smem_addr(bar);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(smem_addr(dst)),
+        "l"(tmap), "r"(0), "r"(z), "r"(y), "r"(x), "r"(b)
+        : "memory");
+}
+
+// Waits for the phase `parity` of bar to complete, for at most `tries`
+// polls; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int tries) {
+    const uint32_t b = smem_addr(bar);
+    for (int i = 0; i < tries; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(b), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 // ---------------------------------------------------------------- misc
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;

@@ -63,6 +63,9 @@ struct DevBufs {
     const uint32_t* spoff;
     int nscenes;
     const void* colliders;  // Collider<T>[ncol]
+    // tensor maps (128 bytes each, one per scene) of `grid` for the fused
+    // kernel's tile copies: the grid as (channel, z, y, x), box 4 x kTile^3
+    const void* tmaps;
 };
 
 // A box collider on the device: R (world from box, row-major), centre t, half
@@ -1081,10 +1084,44 @@ constexpr int kFusedMinBlocks = 3;
 static_assert(WorkP<float>::value <= kFusedThreads && WorkP<double>::value <= kFusedThreads,
               "k_g2p2g runs at most one particle per thread");
 template <typename T> struct FusedShared {
+    alignas(128) vec4<T> graw[kTileCells];  // (m, p) tile of this step's grid, copied by TMA
     vec4<T> gv[kTileCells];  // grid velocity of this step, (vx, vy, vz, 0)
     P2GTile<T, kBlk + 2> p;
     DevParams<T> par;        // the item's scene (batches)
+    uint64_t tbar;           // mbarrier of the tile copy
 };
+// Dynamic shared memory of k_g2p2g: the struct plus room to align it to the
+// 128 bytes a TMA destination needs.
+template <typename T> constexpr size_t fused_smem_bytes() { return sizeof(FusedShared<T>) + 128; }
+
+// Polls of a tile copy's mbarrier before the kernel gives up (RD_FLAG_WAIT_TIMEOUT).
+constexpr int kTileWaitTries = 1 << 16;
+
+// The tile-copy wait on an mbarrier that no copy and no thread arrives at:
+// it must give up after `tries` polls and report it.
+__global__ void k_wait_probe(int tries, uint32_t* flags, int* gave_up) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar);
+    __syncthreads();
+    const bool arrived = mbar_wait(&bar, 0u, tries);
+    if (__syncthreads_or(!arrived)) {
+        if (threadIdx.x == 0) {
+            raise_flag(flags, 8u);
+            *gave_up = 1;
+        }
+    }
+}
+
+// One thread: the grid tile of work item `it` (the kTile^3 nodes from its
+// tile origin) into S.graw by TMA.  P is the item's scene.
+template <typename T>
+__device__ __forceinline__ void issue_tile(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S, int4 it,
+                                           int scene) {
+    int org[3];
+    tile_origin(P, it.x, org);
+    tma_load_4d(S.graw, static_cast<const char*>(D.tmaps) + 128 * (size_t)scene, &S.tbar,
+                (uint32_t)(kTileCells * sizeof(vec4<T>)), org[2], org[1], org[0]);
+}
 
 // G2P of one particle from the velocity tile (updateParticleVelocities,
 // material_point_method.cpp:332-342): v_p = sum w v_i and
@@ -1155,11 +1192,10 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
 // gathered.
 template <typename T, bool TRACK_FP, bool LAGGED>
 __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
-                                           const int4 it) {
+                                           const int4 it, bool has_next, int4 nit, const DevParams<T>* nscene) {
     constexpr int CA = kBlk + 2;
     const vec4<T>* __restrict__ pin = static_cast<const vec4<T>*>(D.pin);
     vec4<T>* __restrict__ pout = static_cast<vec4<T>*>(D.pout);
-    const vec4<T>* __restrict__ grid = static_cast<const vec4<T>*>(D.grid) + P.goff;
     vec4<T>* __restrict__ gnext = static_cast<vec4<T>*>(D.grid_next) + P.goff;
     const size_t n = (size_t)P.n;
     {
@@ -1177,23 +1213,22 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             load_particle(pin, n, src, p);
             if (TRACK_FP) load_fp(pin, n, src, FP);
         }
+        // the (m, p) tile arrived by TMA (nodes outside the grid read as
+        // zero): the grid update, walls and colliders into velocities
         for (int c = threadIdx.x; c < kTileCells; c += blockDim.x) {
-            size_t lin;
             T v0 = T(0), v1 = T(0), v2 = T(0);
-            if (cell_of_tile(P, org, c, lin)) {
-                const vec4<T> g4 = grid[lin];
-                if (g4.x != T(0)) {
-                    v0 = g4.y / g4.x + P.dt * P.g[0];
-                    v1 = g4.z / g4.x + P.dt * P.g[1];
-                    v2 = g4.w / g4.x + P.dt * P.g[2];
-                    const int ix = c / (kTile * kTile), iy = (c / kTile) % kTile, iz = c % kTile;
-                    if (P.bc == 1 && wall_node(P, org[0] + ix, org[1] + iy, org[2] + iz)) v0 = v1 = v2 = T(0);
-                    if (P.ncol) {
-                        T vv[3] = {v0, v1, v2};
-                        collide_node(P, static_cast<const Collider<T>*>(D.colliders), (T)(org[0] + ix) * P.h,
-                                     (T)(org[1] + iy) * P.h, (T)(org[2] + iz) * P.h, vv);
-                        v0 = vv[0]; v1 = vv[1]; v2 = vv[2];
-                    }
+            const vec4<T> g4 = S.graw[c];
+            if (g4.x != T(0)) {
+                v0 = g4.y / g4.x + P.dt * P.g[0];
+                v1 = g4.z / g4.x + P.dt * P.g[1];
+                v2 = g4.w / g4.x + P.dt * P.g[2];
+                const int ix = c / (kTile * kTile), iy = (c / kTile) % kTile, iz = c % kTile;
+                if (P.bc == 1 && wall_node(P, org[0] + ix, org[1] + iy, org[2] + iz)) v0 = v1 = v2 = T(0);
+                if (P.ncol) {
+                    T vv[3] = {v0, v1, v2};
+                    collide_node(P, static_cast<const Collider<T>*>(D.colliders), (T)(org[0] + ix) * P.h,
+                                 (T)(org[1] + iy) * P.h, (T)(org[2] + iz) * P.h, vv);
+                    v0 = vv[0]; v1 = vv[1]; v2 = vv[2];
                 }
             }
             S.gv[c] = mk4<T>(v0, v1, v2, T(0));
@@ -1201,6 +1236,9 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         zero_tile(S.p);
         for (int c = threadIdx.x; c < P2GTile<T, CA>::NC; c += blockDim.x) S.p.cnt[c] = 0;
         __syncthreads();
+        // S.graw is free again: copy the next item's tile while this one runs
+        // (nscene: the next item's scene in a batch, else this item's)
+        if (threadIdx.x == 0 && has_next) issue_tile(nscene ? *nscene : P, D, S, nit, nscene ? nit.w : 0);
         int rcell = 0xff, rrank = 0;  // this thread's record: cell and rank within it
         if (j < count) {
             const int s = it.y + j;
@@ -1271,18 +1309,42 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
 template <typename T, bool TRACK_FP, bool BATCH, bool LAGGED>
 __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlocks : 1)
     k_g2p2g(DevParams<T> P0, DevBufs D) {
-    extern __shared__ __align__(32) unsigned char smem_raw[];
-    FusedShared<T>& S = *reinterpret_cast<FusedShared<T>*>(smem_raw);
+    extern __shared__ __align__(128) unsigned char smem_fused[];
+    FusedShared<T>& S =
+        *reinterpret_cast<FusedShared<T>*>(smem_fused + ((128u - (smem_addr(smem_fused) & 127u)) & 127u));
+    const DevParams<T>* scenes = static_cast<const DevParams<T>*>(D.scenes);
     const uint32_t nw = min(*D.nwork, D.work_cap);
-    for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
+    if (threadIdx.x == 0) mbar_init(&S.tbar);
+    __syncthreads();
+    uint32_t wi = blockIdx.x;
+    if (threadIdx.x == 0 && wi < nw) {
+        const int4 it0 = D.work[wi];
+        if constexpr (BATCH) issue_tile(scenes[it0.w], D, S, it0, it0.w);
+        else issue_tile(P0, D, S, it0, 0);
+    }
+    // the tile of item k completes phase k & 1 of the mbarrier; the next
+    // item's copy is issued inside g2p2g_item once this tile is converted
+    uint32_t parity = 0u;
+    for (; wi < nw; wi += gridDim.x) {
         const int4 it = D.work[wi];
-        if constexpr (BATCH) {
-            copy_scene(S.par, D.scenes, it.w);
-            __syncthreads();
-            g2p2g_item<T, TRACK_FP, LAGGED>(S.par, D, S, it);
-        } else {
-            g2p2g_item<T, TRACK_FP, LAGGED>(P0, D, S, it);
+        if constexpr (BATCH) copy_scene(S.par, D.scenes, it.w);
+        const bool arrived = mbar_wait(&S.tbar, parity, kTileWaitTries);
+        parity ^= 1u;
+        // every thread decides together (this barrier also publishes S.par)
+        if (__syncthreads_or(!arrived)) {
+            if (threadIdx.x == 0) {
+                raise_flag(D.flags, 8u);
+                mbar_wait(&S.tbar, parity ^ 1u, kTileWaitTries);  // the copy in flight, bounded again
+            }
+            return;
         }
+        const uint32_t wn = wi + gridDim.x;
+        const bool has_next = wn < nw;
+        const int4 nit = has_next ? D.work[wn] : make_int4(0, 0, 0, 0);
+        if constexpr (BATCH)
+            g2p2g_item<T, TRACK_FP, LAGGED>(S.par, D, S, it, has_next, nit, has_next ? &scenes[nit.w] : nullptr);
+        else
+            g2p2g_item<T, TRACK_FP, LAGGED>(P0, D, S, it, has_next, nit, nullptr);
     }
 }
 

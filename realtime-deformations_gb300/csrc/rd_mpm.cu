@@ -1,7 +1,9 @@
 // Host side of the C ABI declared in include/rd_mpm.h: the handle, its device
 // buffers (allocated once in rd_create), parameter preparation and the launch
 // sequences for the fused step and for the reference's individual stages.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder is fetched from the driver at run time)
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -197,6 +199,7 @@ struct rd_handle {
     int col_mode = RD_COLLIDE_REFERENCE;
     double col_mu = 0.5;
     void* d_col = nullptr;          // Collider<T>[RD_MAX_COLLIDERS]
+    void* d_tmaps = nullptr;        // CUtensorMap per grid buffer and scene, [2][nscenes]
     int wp = 0;         // particles per work item (<= WorkP)
     int grid_mult = 0;  // persistent CTAs per SM of the step kernels (0: occupancy)
     cudaStream_t stream = nullptr;
@@ -375,6 +378,7 @@ template <typename T> DevBufs bufs(rd_handle* h) {
     D.spoff = h->d_spoff;
     D.nscenes = (int)h->scenes.size();
     D.colliders = h->d_col;
+    D.tmaps = static_cast<const char*>(h->d_tmaps) + (size_t)h->g * h->scenes.size() * sizeof(CUtensorMap);
     return D;
 }
 
@@ -549,7 +553,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
     DevBufs D = bufs<T>(h);
     t = tmark_begin(h, RD_KERNEL_G2P2G);
     const unsigned fg = persistent_grid<T>(h, h->occ_g2p);
-    fused_kernel<T>(h)<<<fg, kFusedThreads, sizeof(FusedShared<T>), h->stream>>>(P, D);
+    fused_kernel<T>(h)<<<fg, kFusedThreads, fused_smem_bytes<T>(), h->stream>>>(P, D);
     tmark_end(h, t);
     RD_TRY(launched(h, "k_g2p2g"));
     h->cur ^= 1;
@@ -803,7 +807,7 @@ template <typename T> rd_status occupancy(rd_handle* h) {
         RD_TRY(check_cuda(h, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
     RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true, false>, kThreads, sm), "occ"));
     h->occ_p2g = std::max(1, o);
-    const int fsm = (int)sizeof(FusedShared<T>);
+    const int fsm = (int)fused_smem_bytes<T>();
     const void* used = (const void*)fused_kernel<T>(h);
     RD_TRY(check_cuda(h, cudaFuncSetAttribute(used, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm), "smem attr"));
     RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, used, kFusedThreads, fsm), "occ"));
@@ -845,7 +849,7 @@ void release(rd_handle* h) {
     void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->bcount, h->gmark[0],
                     h->gmark[1], h->cursor, h->work,
                     h->nwork2, h->tile_sums, h->tile_list, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
-                    h->d_col, h->rgba, h->zid, h->img,
+                    h->d_col, h->d_tmaps, h->rgba, h->zid, h->img,
                     h->d_scenes, h->d_sblock, h->d_spoff};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -891,6 +895,49 @@ bool valid_scene(const rd_params& p) {
 // [poff_s, poff_s + n_s) of the shared particle planes (in every step's
 // sorted order too, since the block keys of scene s precede those of s + 1),
 // its grid nodes [goff_s, goff_s + cells_s) of each grid buffer.
+// Tensor maps of both grid buffers for the fused kernel's tile copies: per
+// scene, its grid region as a 4-D tensor (channel, z, y, x) of the element
+// type, box 4 x kTile^3; nodes outside the region read as zero.  The encoder
+// is the driver's cuTensorMapEncodeTiled, fetched through the runtime.
+rd_status encode_tile_maps(rd_handle* h) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::mutex mu;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!encode) {
+            cudaDriverEntryPointQueryResult q{};
+            void* fn = nullptr;
+            if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                    cudaSuccess ||
+                q != cudaDriverEntryPointSuccess || !fn)
+                return fail(h, RD_CUDA_ERROR, "cuTensorMapEncodeTiled is not available");
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        }
+    }
+    const size_t ns = h->scenes.size();
+    std::vector<CUtensorMap> maps(2 * ns);
+    const cuuint64_t es = (cuuint64_t)h->esize;
+    for (int b = 0; b < 2; ++b)
+        for (size_t s = 0; s < ns; ++s) {
+            const rd_scene_info& sc = h->scenes[s];
+            const cuuint64_t M0 = (cuuint64_t)sc.prm.max_i, M1 = (cuuint64_t)sc.prm.max_j, M2 = (cuuint64_t)sc.prm.max_k;
+            const cuuint64_t dims[4] = {4, M2, M1, M0};
+            const cuuint64_t strides[3] = {4 * es, 4 * es * M2, 4 * es * M2 * M1};
+            const cuuint32_t box[4] = {4, (cuuint32_t)kTile, (cuuint32_t)kTile, (cuuint32_t)kTile};
+            const cuuint32_t estr[4] = {1, 1, 1, 1};
+            void* base = static_cast<char*>(h->grid[b]) + sc.goff * 4 * es;
+            const CUresult r = encode(&maps[b * ns + s],
+                                      es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base,
+                                      dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return fail(h, RD_CUDA_ERROR, "tensor map of a grid tile");
+        }
+    RD_TRY(check_cuda(h, cudaMalloc(&h->d_tmaps, maps.size() * sizeof(CUtensorMap)), "tensor maps"));
+    return check_cuda(h, cudaMemcpy(h->d_tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice),
+                      "tensor maps");
+}
+
 rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
     if (!params || !out || nscenes < 1) return RD_INVALID_ARG;
     *out = nullptr;
@@ -1010,7 +1057,8 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
     cudaMemsetAsync(h->flags, 0, 4, h->stream);
     cudaMemsetAsync(h->nwork2, 0, 8, h->stream);
     cudaMemsetAsync(h->rgba, 0xff, n * sizeof(uint32_t), h->stream);  // white
-    rd_status st = p.precision == RD_FP64 ? occupancy<double>(h) : occupancy<float>(h);
+    rd_status st = encode_tile_maps(h);
+    if (st == RD_OK) st = p.precision == RD_FP64 ? occupancy<double>(h) : occupancy<float>(h);
     if (st != RD_OK) return bail(st);
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(RD_CUDA_ERROR);
     *out = h;
@@ -2003,6 +2051,24 @@ rd_status rd_last_error(rd_handle* h, char* buf, size_t len) {
     if (!h || !buf || len == 0) return RD_INVALID_ARG;
     std::snprintf(buf, len, "%s", h->err.c_str());
     return RD_OK;
+}
+
+rd_status rd_debug_wait_timeout(rd_handle* h, int32_t tries, int32_t* gave_up) {
+    if (!h || !gave_up || tries < 1 || tries > kTileWaitTries) return RD_INVALID_ARG;
+    cudaSetDevice(h->prm.device);
+    int* d = nullptr;
+    RD_TRY(check_cuda(h, cudaMalloc((void**)&d, sizeof(int)), "probe"));
+    rd_status st = check_cuda(h, cudaMemsetAsync(d, 0, sizeof(int), h->stream), "probe");
+    if (st == RD_OK) {
+        k_wait_probe<<<1, 64, 0, h->stream>>>(tries, h->flags, d);
+        st = launched(h, "k_wait_probe");
+    }
+    int g = 0;
+    if (st == RD_OK) st = check_cuda(h, cudaMemcpyAsync(&g, d, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "probe");
+    if (st == RD_OK) st = check_cuda(h, cudaStreamSynchronize(h->stream), "probe");
+    cudaFree(d);
+    *gave_up = g;
+    return st;
 }
 
 rd_status rd_debug_sort(rd_handle* h, uint32_t* keys, uint32_t* order, int where) {

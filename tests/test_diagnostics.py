@@ -71,3 +71,21 @@ def test_nan_injection_is_flagged_and_the_handle_recovers(built_pkg):
     sim.step(sc.dt, 5)
     assert sim.flags() == 0
     assert np.all(np.isfinite(sim.get_particles(("x",))["x"]))
+
+
+@pytest.mark.gpu
+def test_tile_copy_wait_gives_up_and_the_handle_keeps_working(built_pkg):
+    """The fused kernel's wait for a TMA tile copy is bounded: against an
+    mbarrier that nothing arrives at it gives up, raises the flag and the
+    context stays usable (the next steps run and are flag-free)."""
+    from rd_gb300 import scenes
+    sc = scenes.snowball(seed=7, n=2000, grid=32)
+    sim = built_pkg.Simulation(built_pkg.make_params(*sc.grid, sc.n, sc.h, **sc.params()))
+    sim.set_particles(sc.x, sc.v, sc.mass)
+    sim.init_volumes()
+    assert sim.debug_wait_timeout(tries=32)
+    assert sim.flags() & built_pkg.FLAG_WAIT_TIMEOUT
+    sim.clear_flags()
+    sim.step(sc.dt, 4)
+    assert sim.flags() == 0
+    assert np.all(np.isfinite(sim.get_particles(("x",))["x"]))
