@@ -38,6 +38,16 @@
 
 namespace rd {
 
+// v / h, exactly: a product where h is a power of two, else the division.
+template <typename T>
+__device__ __forceinline__ T over_h(const DevParams<T>& P, T v) {
+    return P.hinv_pow2 != T(0) ? v * P.hinv_pow2 : v / P.h;
+}
+template <typename T>
+__device__ __forceinline__ T x_over_h(const DevParams<T>& P, T x) {
+    return P.hinv_pow2 != T(0) ? x * P.hinv_pow2 : div_rn(x, P.h);
+}
+
 // d w / d t of bspline4's four weights (t = x / h, f = t - base, g = 1 - f).
 template <typename T>
 __device__ __forceinline__ void bspline4_dt(T t, int base, T dw[4]) {
@@ -283,6 +293,7 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
     for (int c = threadIdx.x; c < P2GTile<T, kBlk>::NC; c += blockDim.x) S.p.cnt[c] = 0;
     __syncthreads();
     const int j = threadIdx.x;
+    int rcell = 0xff, rrank = 0;  // this thread's record: cell and rank within it
     if (j < count) {
         const uint32_t sp = (uint32_t)(it.y + j);  // sorted position: slot of this particle in state n + 1
         const uint32_t idx = D.perm[sp];
@@ -297,9 +308,9 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
             T dw[3][4];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                bspline4_dt(div_rn(p.x[a], P.h), St.b[a], dw[a]);
+                bspline4_dt(x_over_h(P, p.x[a]), St.b[a], dw[a]);
 #pragma unroll
-                for (int o = 0; o < 4; ++o) dw[a][o] = dw[a][o] / P.h;
+                for (int o = 0; o < 4; ++o) dw[a][o] = over_h(P, dw[a][o]);
             }
             T vn[3], Bn[9];
             g2p_gather(S.gv, St, vn, Bn);
@@ -336,9 +347,9 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
                 }
             // the vh_b scatter as a record: q' = v'_b + B'_b e, A = B'_b
             write_record<T, false>(&S.p.rec[j * kRecV4], St, p.x, Bb, vb, T(0), P.h);
-            const int cell = (St.rel[0] * kBlk + St.rel[1]) * kBlk + St.rel[2];
-            S.p.cellof[j] = (uint8_t)cell;
-            atomicAdd(&S.p.cnt[cell], 1);
+            rcell = (St.rel[0] * kBlk + St.rel[1]) * kBlk + St.rel[2];
+            S.p.cellof[j] = (uint8_t)rcell;
+            rrank = atomicAdd(&S.p.cnt[rcell], 1);
             // plastic split of F* = (I + dt D B) F (lagged B)
             T A[9];
 #pragma unroll
@@ -370,7 +381,7 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
             pacc[(size_t)kAccPerScene * sp + 3] += (double)ths_b;
         }
     }
-    sort_records<T, kBlk>(S.p, count);
+    sort_ranked<T, kBlk>(S.p, j, rcell, rrank);
     p2g_tasks<T, false, kBlk>(S.p, count);
     __syncthreads();
     p2g_flush<T, kBlk>(P, S.p, org, agrid);
@@ -445,9 +456,9 @@ __device__ __forceinline__ void adj_p2g_item(const DevParams<T>& P, const DevBuf
             T dw[3][4];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                bspline4_dt(div_rn(p.x[a], P.h), St.b[a], dw[a]);
+                bspline4_dt(x_over_h(P, p.x[a]), St.b[a], dw[a]);
 #pragma unroll
-                for (int o = 0; o < 4; ++o) dw[a][o] = dw[a][o] / P.h;
+                for (int o = 0; o < 4; ++o) dw[a][o] = over_h(P, dw[a][o]);
             }
             T U[9], sv[3], svm1[3], tau[9], A[9], mv[3];
             {
