@@ -274,7 +274,7 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
                                              const int4 it, const vec4<T>* __restrict__ st,
                                              const vec4<T>* __restrict__ grid0, vec4<T>* __restrict__ agrid0,
                                              const AdjState<T>& nxt, const AdjState<T>& part,
-                                             double* __restrict__ pacc) {
+                                             double* __restrict__ pacc, const vec4<T>* __restrict__ split) {
     const vec4<T>* grid = grid0 + P.goff;
     vec4<T>* agrid = agrid0 + P.goff;
     int org[3];
@@ -355,10 +355,10 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
 #pragma unroll
             for (int e = 0; e < 9; ++e) A[e] = p.B[e] * P.dinv * P.dt;
             A[0] += T(1); A[4] += T(1); A[8] += T(1);
-            T Fs[9];
-            matmul3(Fs, A, p.F);
-            T U[9], s[3], sm1[3], V[9];
-            svd3_near(Fs, U, s, sm1, V);
+            // the SVD of F* = A F the forward made in this step (the recompute
+            // keeps it per sorted slot): no second SVD here
+            T U[9], s[3], V[9];
+            load_split(split, (size_t)P.n, sp, U, s, V);
             T Fb1[9];
 #pragma unroll
             for (int e = 0; e < 9; ++e) Fb1[e] = nxt.F[9 * sp + e];
@@ -392,7 +392,8 @@ template <typename T, bool BATCH>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_g2p(DevParams<T> P0, DevBufs D, const vec4<T>* __restrict__ st,
                                                         const vec4<T>* __restrict__ grid0,
                                                         vec4<T>* __restrict__ agrid0, AdjState<T> nxt,
-                                                        AdjState<T> part, double* __restrict__ pacc) {
+                                                        AdjState<T> part, double* __restrict__ pacc,
+                                                        const vec4<T>* __restrict__ split) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
     AdjG2PShared<T>& S = *reinterpret_cast<AdjG2PShared<T>*>(smem_raw);
     const uint32_t nw = min(*D.nwork, D.work_cap);
@@ -401,9 +402,9 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_g2p(DevParams<T> P0, DevBuf
         if constexpr (BATCH) {
             copy_scene(S.par, D.scenes, it.w);
             __syncthreads();
-            adj_g2p_item<T>(S.par, D, S, it, st, grid0, agrid0, nxt, part, pacc);
+            adj_g2p_item<T>(S.par, D, S, it, st, grid0, agrid0, nxt, part, pacc, split);
         } else {
-            adj_g2p_item<T>(P0, D, S, it, st, grid0, agrid0, nxt, part, pacc);
+            adj_g2p_item<T>(P0, D, S, it, st, grid0, agrid0, nxt, part, pacc, split);
         }
     }
 }

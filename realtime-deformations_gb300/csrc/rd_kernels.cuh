@@ -53,6 +53,9 @@ struct DevBufs {
     void* grid_next;   // vec4 per cell: P2G of the next step (fused kernel)
     void* gforce;      // vec4 per cell (stage mode forces)
     uint32_t* flags;
+    // fused kernel, adjoint segments: U, singular values and V of each
+    // particle's plastic split, 6 vec4 planes by sorted slot (null: not kept)
+    void* split_out;
     uint32_t* bcount;  // particles per 4x4x4 block (the block sums of counts)
     uint8_t* gmark;       // blocks of grid that hold data (set by every writer)
     uint8_t* gmark_next;  // the same for grid_next
@@ -491,7 +494,7 @@ template <typename T> struct Split {
 // from svd3_near without cancellation.
 template <typename T, bool TRACK_FP>
 __device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T F[9], T& Jp, T FP[9],
-                                         Split<T>& sp) {
+                                         Split<T>& sp, T* s_out = nullptr, T* V_out = nullptr) {
     T A[9];
 #pragma unroll
     for (int e = 0; e < 9; ++e) A[e] = Bm[e] * P.dinv * P.dt;
@@ -500,6 +503,12 @@ __device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T
     matmul3(Fs, A, F);
     T s[3], sm1[3], V[9];
     svd3_near(Fs, sp.U, s, sm1, V);
+    if (s_out) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) s_out[c] = s[c];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) V_out[e] = V[e];
+    }
     T ratio = T(1);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -1176,9 +1185,11 @@ __device__ __forceinline__ void g2p_gather(const vec4<T>* __restrict__ gv, const
 template <typename T, bool TRACK_FP>
 __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T>& p, T FP[9], const T Bm[9],
                                                vec4<T>* __restrict__ pout, size_t n, size_t s, T G6[6],
-                                               bool& finite) {
+                                               bool& finite, void* split_out) {
     Split<T> sp;
-    update_F<T, TRACK_FP>(P, Bm, p.F, p.Jp, FP, sp);
+    T sv[3], V[9];
+    update_F<T, TRACK_FP>(P, Bm, p.F, p.Jp, FP, sp, sv, V);
+    if (split_out) store_split(static_cast<vec4<T>*>(split_out), n, s, sp.U, sv, V);
     stress_from_split(P, sp, p.Jp, P.fscale * (p.vol * P.dinv), G6);
     store_particle_back(pout, n, s, p);
     if (TRACK_FP) store_fp(pout, n, s, FP);
@@ -1247,7 +1258,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             // split is live across the gather
             T G6[6];
             bool finite = true;
-            if constexpr (LAGGED) split_particle<T, TRACK_FP>(P, p, FP, p.B, pout, n, s, G6, finite);
+            if constexpr (LAGGED) split_particle<T, TRACK_FP>(P, p, FP, p.B, pout, n, s, G6, finite, D.split_out);
             Stencil<T> St;
             const bool ok = make_stencil(P, p.x, org, St);
             if (!ok) raise_flag(D.flags, 4u);
@@ -1256,7 +1267,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
 #pragma unroll
             for (int e = 0; e < 9; ++e) Bp[e] = T(0);
             if (ok) g2p_gather(S.gv, St, vp, Bp);
-            if constexpr (!LAGGED) split_particle<T, TRACK_FP>(P, p, FP, Bp, pout, n, s, G6, finite);
+            if constexpr (!LAGGED) split_particle<T, TRACK_FP>(P, p, FP, Bp, pout, n, s, G6, finite, D.split_out);
 #pragma unroll
             for (int a = 0; a < 3; ++a) p.v[a] = vp[a];
 #pragma unroll

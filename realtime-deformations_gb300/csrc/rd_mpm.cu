@@ -143,7 +143,7 @@ struct rd_adjoint_data {
     uint64_t version = 0;  // handle version the record belongs to
     double dt = 0.0;
     int steps = 0, every = 0;
-    size_t state_bytes = 0, grid_bytes = 0;
+    size_t state_bytes = 0, grid_bytes = 0, split_bytes = 0;
     size_t nckpt = 0, nseg = 0;         // capacities (states)
     void* ckpt = nullptr;               // nckpt states
     // two segment stores, so that the recomputation of one segment runs
@@ -153,6 +153,7 @@ struct rd_adjoint_data {
     uint32_t* sperm[2] = {nullptr, nullptr}; // nseg sorted permutations of those states
     int4* swork[2] = {nullptr, nullptr};     // nseg work lists
     uint32_t* snwork[2] = {nullptr, nullptr};// nseg work-item counts
+    void* ssplit[2] = {nullptr, nullptr};    // nseg plastic splits (U, s, V per sorted slot)
     int tail_store = 0;                 // the store the record's last segment is in
     cudaStream_t stream2 = nullptr;     // the reverse kernels
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_rec[2] = {nullptr, nullptr}, ev_rev[2] = {nullptr, nullptr};
@@ -243,6 +244,7 @@ struct rd_handle {
     int grid_mode = GRID_NONE;
     double last_dt = 0.0;
     uint64_t launches = 0, graph_replays = 0;
+    void* split_out = nullptr;  // the fused kernel keeps each particle's plastic split here (adjoint segments)
     int occ_p2g = 1, occ_g2p = 1;
     std::string err;
     // per-kernel event timing (rd_set_kernel_timing)
@@ -370,6 +372,7 @@ template <typename T> DevBufs bufs(rd_handle* h) {
     D.grid_next = h->grid[h->g ^ 1];
     D.gforce = h->gforce;
     D.flags = h->flags;
+    D.split_out = h->split_out;
     D.bcount = h->bcount;
     D.gmark = h->gmark[h->g];
     D.gmark_next = h->gmark[h->g ^ 1];
@@ -834,7 +837,7 @@ void release(rd_handle* h) {
     drop_graphs(h);
     rd_adjoint_data& a = h->adj;
     for (int b = 0; b < 2; ++b) {
-        void* sp[] = {a.sstore[b], a.gstore[b], a.sperm[b], a.swork[b], a.snwork[b]};
+        void* sp[] = {a.sstore[b], a.gstore[b], a.sperm[b], a.swork[b], a.snwork[b], a.ssplit[b]};
         for (void* p : sp)
             if (p) cudaFree(p);
     }
@@ -1220,6 +1223,7 @@ rd_status adj_alloc(rd_handle* h, int steps, int every) {
     const size_t n = std::max<size_t>(1, (size_t)h->n);
     a.state_bytes = (size_t)h->planes * n * 4 * h->esize;
     a.grid_bytes = h->ncells * 4 * h->esize;
+    a.split_bytes = (size_t)kSplitPlanes * n * 4 * h->esize;
     const size_t nckpt = (size_t)((steps + every - 1) / every), nseg = (size_t)every;
     auto grow = [&](void** ptr, size_t bytes) -> rd_status {
         drop_graphs(h);  // a captured sweep holds the old pointers
@@ -1238,6 +1242,7 @@ rd_status adj_alloc(rd_handle* h, int steps, int every) {
             RD_TRY(grow((void**)&a.sperm[b], nseg * n * sizeof(uint32_t)));
             RD_TRY(grow((void**)&a.swork[b], nseg * h->work_cap * sizeof(int4)));
             RD_TRY(grow((void**)&a.snwork[b], nseg * sizeof(uint32_t)));
+            RD_TRY(grow(&a.ssplit[b], nseg * a.split_bytes));
         }
         a.nseg = nseg;
     }
@@ -1278,6 +1283,7 @@ template <typename T> rd_status stored_segment(rd_handle* h, double dt, int len,
         h->pl[h->cur ^ 1] = at(a.sstore[b], (size_t)j + 1, a.state_bytes);
         h->perm = a.sperm[b] + (size_t)j * n;
         h->work = a.swork[b] + (size_t)j * h->work_cap;
+        h->split_out = at(a.ssplit[b], (size_t)j, a.split_bytes);
         st = step_fused<T>(h, dt);
         if (st == RD_OK)
             st = check_cuda(h, cudaMemcpyAsync(at(a.gstore[b], (size_t)j, a.grid_bytes), h->grid[h->g ^ 1], a.grid_bytes,
@@ -1292,6 +1298,7 @@ template <typename T> rd_status stored_segment(rd_handle* h, double dt, int len,
     h->pl[1] = pl1;
     h->perm = perm0;
     h->work = work0;
+    h->split_out = nullptr;
     return st;
 }
 
@@ -1481,6 +1488,7 @@ template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
             const int cur = nxt ^ 1;
             const vec4<T>* st = reinterpret_cast<const vec4<T>*>(at(a.sstore[b], (size_t)j, a.state_bytes));
             const vec4<T>* gr = reinterpret_cast<const vec4<T>*>(at(a.gstore[b], (size_t)j, a.grid_bytes));
+            const vec4<T>* spl = reinterpret_cast<const vec4<T>*>(at(a.ssplit[b], (size_t)j, a.split_bytes));
             vec4<T>* ag = static_cast<vec4<T>*>(a.agrid);
             DevBufs D = bufs<T>(h);
             D.perm = a.sperm[b] + (size_t)j * n;
@@ -1490,9 +1498,9 @@ template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
             const AdjState<T> An = adj_view<T>(h, nxt), Ap = adj_view<T>(h, 2), Ac = adj_view<T>(h, cur);
             long t = tmark_begin(h, RD_KERNEL_ADJ_G2P);
             if (batch)
-                k_adj_g2p<T, true><<<gg, kAdjThreads, sg, rs>>>(P, D, st, gr, ag, An, Ap, a.pacc);
+                k_adj_g2p<T, true><<<gg, kAdjThreads, sg, rs>>>(P, D, st, gr, ag, An, Ap, a.pacc, spl);
             else
-                k_adj_g2p<T, false><<<gg, kAdjThreads, sg, rs>>>(P, D, st, gr, ag, An, Ap, a.pacc);
+                k_adj_g2p<T, false><<<gg, kAdjThreads, sg, rs>>>(P, D, st, gr, ag, An, Ap, a.pacc, spl);
             tmark_end(h, t);
             t = tmark_begin(h, RD_KERNEL_ADJ_P2G);
             if (batch)
