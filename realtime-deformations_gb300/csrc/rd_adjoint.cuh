@@ -358,7 +358,10 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
             // the SVD of F* = A F the forward made in this step (the recompute
             // keeps it per sorted slot): no second SVD here
             T U[9], s[3], V[9];
-            load_split(split, (size_t)P.n, sp, U, s, V);
+            {
+                T sm1[3];
+                load_split(split, (size_t)P.n, sp, U, s, sm1, V);
+            }
             T Fb1[9];
 #pragma unroll
             for (int e = 0; e < 9; ++e) Fb1[e] = nxt.F[9 * sp + e];
@@ -422,7 +425,7 @@ __device__ __forceinline__ void adj_p2g_item(const DevParams<T>& P, const DevBuf
                                              const int4 it, const vec4<T>* __restrict__ st,
                                              const vec4<T>* __restrict__ grid0, const vec4<T>* __restrict__ agrid0,
                                              const AdjState<T>& part, const AdjState<T>& cur,
-                                             double* __restrict__ pacc) {
+                                             double* __restrict__ pacc, const vec4<T>* __restrict__ prev_split) {
     const vec4<T>* grid = grid0 + P.goff;
     const vec4<T>* agrid = agrid0 + P.goff;
     int org[3];
@@ -462,7 +465,17 @@ __device__ __forceinline__ void adj_p2g_item(const DevParams<T>& P, const DevBuf
                 for (int o = 0; o < 4; ++o) dw[a][o] = over_h(P, dw[a][o]);
             }
             T U[9], sv[3], svm1[3], tau[9], A[9], mv[3];
-            {
+            if (prev_split) {
+                // F of this state is U clamp(S) V^T of the previous step's split
+                // (kept at this state's slot by the recompute): its SVD as is
+                T V[9];
+                load_split(prev_split, (size_t)P.n, idx, U, sv, svm1, V);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (sv[k] < P.lo) { sv[k] = P.lo; svm1[k] = P.lo - T(1); }
+                    else if (sv[k] > P.hi) { sv[k] = P.hi; svm1[k] = P.hi - T(1); }
+                }
+            } else {
                 T V[9];
                 svd3_near(p.F, U, sv, svm1, V);
             }
@@ -535,7 +548,8 @@ template <typename T, bool BATCH>
 __global__ void __launch_bounds__(kAdjThreads) k_adj_p2g(DevParams<T> P0, DevBufs D, const vec4<T>* __restrict__ st,
                                                         const vec4<T>* __restrict__ grid0,
                                                         const vec4<T>* __restrict__ agrid0, AdjState<T> part,
-                                                        AdjState<T> cur, double* __restrict__ pacc) {
+                                                        AdjState<T> cur, double* __restrict__ pacc,
+                                                        const vec4<T>* __restrict__ prev_split) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
     AdjP2GShared<T>& S = *reinterpret_cast<AdjP2GShared<T>*>(smem_raw);
     const uint32_t nw = min(*D.nwork, D.work_cap);
@@ -544,9 +558,9 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_p2g(DevParams<T> P0, DevBuf
         if constexpr (BATCH) {
             copy_scene(S.par, D.scenes, it.w);
             __syncthreads();
-            adj_p2g_item<T>(S.par, D, S, it, st, grid0, agrid0, part, cur, pacc);
+            adj_p2g_item<T>(S.par, D, S, it, st, grid0, agrid0, part, cur, pacc, prev_split);
         } else {
-            adj_p2g_item<T>(P0, D, S, it, st, grid0, agrid0, part, cur, pacc);
+            adj_p2g_item<T>(P0, D, S, it, st, grid0, agrid0, part, cur, pacc, prev_split);
         }
     }
 }

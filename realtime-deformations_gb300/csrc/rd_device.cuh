@@ -94,25 +94,28 @@ __device__ __forceinline__ void store_particle(vec4<T>* __restrict__ pl, size_t 
     store_particle_back(pl, n, i, p);
 }
 
-// The plastic split F* = U diag(s) V^T of one particle (U, V row-major), as
-// 6 vec4 planes: U0..U3 | U4..U7 | U8 s0 s1 s2 | V0..V3 | V4..V7 | V8 - - -.
+// The plastic split F* = U diag(s) V^T of one particle (U, V row-major) and
+// s - 1 (formed without cancellation), as 6 vec4 planes:
+// U0..U3 | U4..U7 | U8 s0 s1 s2 | V0..V3 | V4..V7 | V8 (s-1)0 (s-1)1 (s-1)2.
 template <typename T>
 __device__ __forceinline__ void store_split(vec4<T>* __restrict__ pl, size_t n, size_t i, const T U[9], const T s[3],
-                                            const T V[9]) {
+                                            const T sm1[3], const T V[9]) {
     st_stream(pl + 0 * n + i, mk4<T>(U[0], U[1], U[2], U[3]));
     st_stream(pl + 1 * n + i, mk4<T>(U[4], U[5], U[6], U[7]));
     st_stream(pl + 2 * n + i, mk4<T>(U[8], s[0], s[1], s[2]));
     st_stream(pl + 3 * n + i, mk4<T>(V[0], V[1], V[2], V[3]));
     st_stream(pl + 4 * n + i, mk4<T>(V[4], V[5], V[6], V[7]));
-    st_stream(pl + 5 * n + i, mk4<T>(V[8], T(0), T(0), T(0)));
+    st_stream(pl + 5 * n + i, mk4<T>(V[8], sm1[0], sm1[1], sm1[2]));
 }
 template <typename T>
-__device__ __forceinline__ void load_split(const vec4<T>* __restrict__ pl, size_t n, size_t i, T U[9], T s[3], T V[9]) {
+__device__ __forceinline__ void load_split(const vec4<T>* __restrict__ pl, size_t n, size_t i, T U[9], T s[3], T sm1[3],
+                                           T V[9]) {
     const vec4<T> a = ld_stream(pl + 0 * n + i), b = ld_stream(pl + 1 * n + i), c = ld_stream(pl + 2 * n + i),
                   d = ld_stream(pl + 3 * n + i), e = ld_stream(pl + 4 * n + i), f = ld_stream(pl + 5 * n + i);
     U[0] = a.x; U[1] = a.y; U[2] = a.z; U[3] = a.w; U[4] = b.x; U[5] = b.y; U[6] = b.z; U[7] = b.w; U[8] = c.x;
     s[0] = c.y; s[1] = c.z; s[2] = c.w;
     V[0] = d.x; V[1] = d.y; V[2] = d.z; V[3] = d.w; V[4] = e.x; V[5] = e.y; V[6] = e.z; V[7] = e.w; V[8] = f.x;
+    sm1[0] = f.y; sm1[1] = f.z; sm1[2] = f.w;
 }
 constexpr int kSplitPlanes = 6;
 

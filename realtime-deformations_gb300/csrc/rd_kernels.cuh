@@ -494,7 +494,8 @@ template <typename T> struct Split {
 // from svd3_near without cancellation.
 template <typename T, bool TRACK_FP>
 __device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T F[9], T& Jp, T FP[9],
-                                         Split<T>& sp, T* s_out = nullptr, T* V_out = nullptr) {
+                                         Split<T>& sp, T* s_out = nullptr, T* sm1_out = nullptr,
+                                         T* V_out = nullptr) {
     T A[9];
 #pragma unroll
     for (int e = 0; e < 9; ++e) A[e] = Bm[e] * P.dinv * P.dt;
@@ -505,7 +506,7 @@ __device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T
     svd3_near(Fs, sp.U, s, sm1, V);
     if (s_out) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) s_out[c] = s[c];
+        for (int c = 0; c < 3; ++c) { s_out[c] = s[c]; sm1_out[c] = sm1[c]; }
 #pragma unroll
         for (int e = 0; e < 9; ++e) V_out[e] = V[e];
     }
@@ -1187,9 +1188,9 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
                                                vec4<T>* __restrict__ pout, size_t n, size_t s, T G6[6],
                                                bool& finite, void* split_out) {
     Split<T> sp;
-    T sv[3], V[9];
-    update_F<T, TRACK_FP>(P, Bm, p.F, p.Jp, FP, sp, sv, V);
-    if (split_out) store_split(static_cast<vec4<T>*>(split_out), n, s, sp.U, sv, V);
+    T sv[3], svm1[3], V[9];
+    update_F<T, TRACK_FP>(P, Bm, p.F, p.Jp, FP, sp, sv, svm1, V);
+    if (split_out) store_split(static_cast<vec4<T>*>(split_out), n, s, sp.U, sv, svm1, V);
     stress_from_split(P, sp, p.Jp, P.fscale * (p.vol * P.dinv), G6);
     store_particle_back(pout, n, s, p);
     if (TRACK_FP) store_fp(pout, n, s, FP);

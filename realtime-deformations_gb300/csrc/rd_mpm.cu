@@ -1489,6 +1489,9 @@ template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
             const vec4<T>* st = reinterpret_cast<const vec4<T>*>(at(a.sstore[b], (size_t)j, a.state_bytes));
             const vec4<T>* gr = reinterpret_cast<const vec4<T>*>(at(a.gstore[b], (size_t)j, a.grid_bytes));
             const vec4<T>* spl = reinterpret_cast<const vec4<T>*>(at(a.ssplit[b], (size_t)j, a.split_bytes));
+            // the split of step j - 1 is F of state j (none kept for a segment's first step)
+            const vec4<T>* spl_prev =
+                j > 0 ? reinterpret_cast<const vec4<T>*>(at(a.ssplit[b], (size_t)j - 1, a.split_bytes)) : nullptr;
             vec4<T>* ag = static_cast<vec4<T>*>(a.agrid);
             DevBufs D = bufs<T>(h);
             D.perm = a.sperm[b] + (size_t)j * n;
@@ -1504,9 +1507,9 @@ template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
             tmark_end(h, t);
             t = tmark_begin(h, RD_KERNEL_ADJ_P2G);
             if (batch)
-                k_adj_p2g<T, true><<<gp, kAdjThreads, sp, rs>>>(P, D, st, gr, ag, Ap, Ac, a.pacc);
+                k_adj_p2g<T, true><<<gp, kAdjThreads, sp, rs>>>(P, D, st, gr, ag, Ap, Ac, a.pacc, spl_prev);
             else
-                k_adj_p2g<T, false><<<gp, kAdjThreads, sp, rs>>>(P, D, st, gr, ag, Ap, Ac, a.pacc);
+                k_adj_p2g<T, false><<<gp, kAdjThreads, sp, rs>>>(P, D, st, gr, ag, Ap, Ac, a.pacc, spl_prev);
             tmark_end(h, t);
             RD_TRY(launched(h, "adjoint step", 2));
             nxt = cur;
