@@ -73,14 +73,46 @@ __device__ __forceinline__ bool node_velocity(const DevParams<T>& P, const vec4<
     return true;
 }
 
-// Adjoint state of all particles, structure of arrays in slot order.
+// Adjoint state of all particles in slot order: kAdjPlanes vec4 planes of n
+// entries, so a thread moves its particle's 25 values with 8 coalesced
+// 16-byte accesses: 0: x0 x1 x2 J_P | 1: v0 v1 v2 - | 2-4: B row-major |
+// 5-7: F row-major (the last entry of each matrix's third plane is spare).
+constexpr int kAdjPlanes = 8;
+constexpr int kAdjB = 2, kAdjF = 5;
 template <typename T> struct AdjState {
-    T* x;   // n x 3
-    T* v;   // n x 3
-    T* B;   // n x 9
-    T* F;   // n x 9
-    T* Jp;  // n
+    vec4<T>* p;
+    size_t n;
 };
+
+template <typename T>
+__device__ __forceinline__ void adj_load_xj(const AdjState<T>& A, size_t i, T x[3], T& Jp) {
+    const vec4<T> a = A.p[i];
+    x[0] = a.x; x[1] = a.y; x[2] = a.z; Jp = a.w;
+}
+template <typename T>
+__device__ __forceinline__ void adj_load_v(const AdjState<T>& A, size_t i, T v[3]) {
+    const vec4<T> a = A.p[A.n + i];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z;
+}
+template <typename T>
+__device__ __forceinline__ void adj_load_mat(const AdjState<T>& A, int plane, size_t i, T M[9]) {
+    const vec4<T> a = A.p[plane * A.n + i], b = A.p[(plane + 1) * A.n + i], c = A.p[(plane + 2) * A.n + i];
+    M[0] = a.x; M[1] = a.y; M[2] = a.z; M[3] = a.w; M[4] = b.x; M[5] = b.y; M[6] = b.z; M[7] = b.w; M[8] = c.x;
+}
+template <typename T>
+__device__ __forceinline__ void adj_store_xj(const AdjState<T>& A, size_t i, const T x[3], T Jp) {
+    A.p[i] = mk4<T>(x[0], x[1], x[2], Jp);
+}
+template <typename T>
+__device__ __forceinline__ void adj_store_v(const AdjState<T>& A, size_t i, const T v[3]) {
+    A.p[A.n + i] = mk4<T>(v[0], v[1], v[2], T(0));
+}
+template <typename T>
+__device__ __forceinline__ void adj_store_mat(const AdjState<T>& A, int plane, size_t i, const T M[9]) {
+    A.p[plane * A.n + i] = mk4<T>(M[0], M[1], M[2], M[3]);
+    A.p[(plane + 1) * A.n + i] = mk4<T>(M[4], M[5], M[6], M[7]);
+    A.p[(plane + 2) * A.n + i] = mk4<T>(M[8], T(0), T(0), T(0));
+}
 
 // Per scene: sums of mu0_b, lambda0_b, theta_c_b, theta_s_b.
 constexpr int kAccPerScene = 4;
@@ -315,16 +347,17 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
             T vn[3], Bn[9];
             g2p_gather(S.gv, St, vn, Bn);
             // advection x' = clamp(x + dt v')
-            T xb[3], vb[3], Bb[9];
+            T xb[3], vb[3], Bb[9], Jpb1;
+            adj_load_xj(nxt, sp, xb, Jpb1);
+            adj_load_v(nxt, sp, vb);
+            adj_load_mat(nxt, kAdjB, sp, Bb);
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const T xn = p.x[a] + vn[a] * P.dt;
                 const T mask = (xn >= P.xlo && xn <= P.xhi[a]) ? T(1) : T(0);
-                xb[a] = nxt.x[3 * sp + a] * mask;
-                vb[a] = nxt.v[3 * sp + a] + P.dt * xb[a];
+                xb[a] *= mask;
+                vb[a] += P.dt * xb[a];
             }
-#pragma unroll
-            for (int e = 0; e < 9; ++e) Bb[e] = nxt.B[9 * sp + e];
 #pragma unroll
             for (int c = 0; c < 3; ++c) xb[c] -= Bb[c] * vn[0] + Bb[3 + c] * vn[1] + Bb[6 + c] * vn[2];
             // x_b += sum grad w_i (vh_i . (v'_b + B'_b d_i))
@@ -363,23 +396,22 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
                 load_split(split, (size_t)P.n, sp, U, s, sm1, V);
             }
             T Fb1[9];
-#pragma unroll
-            for (int e = 0; e < 9; ++e) Fb1[e] = nxt.F[9 * sp + e];
-            const T Jpb1 = nxt.Jp[sp];
+            adj_load_mat(nxt, kAdjF, sp, Fb1);
             T Fsb[9], g_ratio, thc_b, ths_b;
             split_backward(P, U, s, V, Fb1, Jpb1, p.Jp, Fsb, g_ratio, thc_b, ths_b);
+            T pF[9], pB[9];
 #pragma unroll
             for (int r = 0; r < 3; ++r)
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    part.F[9 * sp + 3 * r + c] = A[r] * Fsb[c] + A[3 + r] * Fsb[3 + c] + A[6 + r] * Fsb[6 + c];
-                    part.B[9 * sp + 3 * r + c] =
+                    pF[3 * r + c] = A[r] * Fsb[c] + A[3 + r] * Fsb[3 + c] + A[6 + r] * Fsb[6 + c];
+                    pB[3 * r + c] =
                         P.dt * P.dinv *
                         (Fsb[3 * r] * p.F[3 * c] + Fsb[3 * r + 1] * p.F[3 * c + 1] + Fsb[3 * r + 2] * p.F[3 * c + 2]);
                 }
-#pragma unroll
-            for (int a = 0; a < 3; ++a) part.x[3 * sp + a] = xb[a];
-            part.Jp[sp] = Jpb1 * g_ratio;
+            adj_store_mat(part, kAdjF, sp, pF);
+            adj_store_mat(part, kAdjB, sp, pB);
+            adj_store_xj(part, sp, xb, Jpb1 * g_ratio);
             pacc[(size_t)kAccPerScene * sp + 2] += (double)thc_b;
             pacc[(size_t)kAccPerScene * sp + 3] += (double)ths_b;
         }
@@ -524,17 +556,25 @@ __device__ __forceinline__ void adj_p2g_item(const DevParams<T>& P, const DevBuf
             for (int e = 0; e < 9; ++e) { tb[e] = -fs * Ab[e]; Fb[e] = T(0); }
             T Jpb = T(0), mu0b = T(0), lam0b = T(0);
             stress_backward(P, p.F, p.Jp, U, sv, svm1, tb, Fb, Jpb, mu0b, lam0b);
+            {
+                T px[3], pJp, vo[3];
+                adj_load_xj(part, sp, px, pJp);
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                cur.x[3 * idx + a] = part.x[3 * sp + a] + xb[a];
-                cur.v[3 * idx + a] = p.m * swq[a];
+                for (int a = 0; a < 3; ++a) { px[a] += xb[a]; vo[a] = p.m * swq[a]; }
+                adj_store_xj(cur, idx, px, pJp + Jpb);
+                adj_store_v(cur, idx, vo);
             }
+            {
+                T M[9];
+                adj_load_mat(part, kAdjB, sp, M);
 #pragma unroll
-            for (int e = 0; e < 9; ++e) {
-                cur.B[9 * idx + e] = part.B[9 * sp + e] + p.m * P.dinv * Ab[e];
-                cur.F[9 * idx + e] = part.F[9 * sp + e] + Fb[e];
+                for (int e = 0; e < 9; ++e) M[e] += p.m * P.dinv * Ab[e];
+                adj_store_mat(cur, kAdjB, idx, M);
+                adj_load_mat(part, kAdjF, sp, M);
+#pragma unroll
+                for (int e = 0; e < 9; ++e) M[e] += Fb[e];
+                adj_store_mat(cur, kAdjF, idx, M);
             }
-            cur.Jp[idx] = part.Jp[sp] + Jpb;
             pacc[(size_t)kAccPerScene * sp + 0] += (double)mu0b;
             pacc[(size_t)kAccPerScene * sp + 1] += (double)lam0b;
         } else {
@@ -573,14 +613,18 @@ __global__ void k_adj_seed(int n, const vec4<T>* __restrict__ st, const T* __res
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t id = real_to_id<T>(st[6 * (size_t)n + i].w);
+    T x[3], v[3], Z[9];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        A.x[3 * i + a] = (gx && id < (uint32_t)n) ? gx[3 * id + a] : T(0);
-        A.v[3 * i + a] = (gv && id < (uint32_t)n) ? gv[3 * id + a] : T(0);
+        x[a] = (gx && id < (uint32_t)n) ? gx[3 * id + a] : T(0);
+        v[a] = (gv && id < (uint32_t)n) ? gv[3 * id + a] : T(0);
     }
 #pragma unroll
-    for (int e = 0; e < 9; ++e) { A.B[9 * i + e] = T(0); A.F[9 * i + e] = T(0); }
-    A.Jp[i] = T(0);
+    for (int e = 0; e < 9; ++e) Z[e] = T(0);
+    adj_store_xj(A, i, x, T(0));
+    adj_store_v(A, i, v);
+    adj_store_mat(A, kAdjB, i, Z);
+    adj_store_mat(A, kAdjF, i, Z);
 }
 
 // Slot order -> particle id order (into a scratch adjoint) and back, for the
@@ -593,10 +637,7 @@ __global__ void k_adj_to_id(int n, const vec4<T>* __restrict__ st, AdjState<T> f
     const uint32_t id = real_to_id<T>(st[6 * (size_t)n + i].w);
     if (id >= (uint32_t)n) return;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) { by_id.x[3 * id + a] = from.x[3 * i + a]; by_id.v[3 * id + a] = from.v[3 * i + a]; }
-#pragma unroll
-    for (int e = 0; e < 9; ++e) { by_id.B[9 * id + e] = from.B[9 * i + e]; by_id.F[9 * id + e] = from.F[9 * i + e]; }
-    by_id.Jp[id] = from.Jp[i];
+    for (int k = 0; k < kAdjPlanes; ++k) by_id.p[k * by_id.n + id] = from.p[k * from.n + i];
 }
 
 template <typename T>
@@ -606,10 +647,7 @@ __global__ void k_adj_from_id(int n, const vec4<T>* __restrict__ st, AdjState<T>
     const uint32_t id = real_to_id<T>(st[6 * (size_t)n + i].w);
     if (id >= (uint32_t)n) return;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) { to.x[3 * i + a] = by_id.x[3 * id + a]; to.v[3 * i + a] = by_id.v[3 * id + a]; }
-#pragma unroll
-    for (int e = 0; e < 9; ++e) { to.B[9 * i + e] = by_id.B[9 * id + e]; to.F[9 * i + e] = by_id.F[9 * id + e]; }
-    to.Jp[i] = by_id.Jp[id];
+    for (int k = 0; k < kAdjPlanes; ++k) to.p[k * to.n + i] = by_id.p[k * by_id.n + id];
 }
 
 // dL/dv of the start state, from its slot order to particle id order.
@@ -619,8 +657,10 @@ __global__ void k_adj_out(int n, const vec4<T>* __restrict__ st, AdjState<T> A, 
     if (i >= n) return;
     const uint32_t id = real_to_id<T>(st[6 * (size_t)n + i].w);
     if (id >= (uint32_t)n) return;
+    T v[3];
+    adj_load_v(A, i, v);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) v0[3 * id + a] = A.v[3 * i + a];
+    for (int a = 0; a < 3; ++a) v0[3 * id + a] = v[a];
 }
 
 }  // namespace rd

@@ -1252,7 +1252,8 @@ rd_status adj_alloc(rd_handle* h, int steps, int every) {
         for (cudaEvent_t* e : evs)
             RD_TRY(check_cuda(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "adjoint events"));
         RD_TRY(check_cuda(h, cudaMalloc(&a.final_state, a.state_bytes), "adjoint buffers"));
-        for (int k = 0; k < 3; ++k) RD_TRY(check_cuda(h, cudaMalloc(&a.adj[k], 25 * n * h->esize), "adjoint buffers"));
+        for (int k = 0; k < 3; ++k)
+            RD_TRY(check_cuda(h, cudaMalloc(&a.adj[k], (size_t)kAdjPlanes * 4 * n * h->esize), "adjoint buffers"));
         RD_TRY(check_cuda(h, cudaMalloc(&a.agrid, a.grid_bytes), "adjoint buffers"));
         RD_TRY(check_cuda(h, cudaMalloc((void**)&a.pacc, kAccPerScene * n * sizeof(double)), "adjoint buffers"));
         RD_TRY(check_cuda(h, cudaMalloc((void**)&a.acc, kAccPerScene * h->scenes.size() * sizeof(double)),
@@ -1419,9 +1420,7 @@ template <typename T> rd_status adjoint_record_impl(rd_handle* h, double dt, int
 }
 
 template <typename T> AdjState<T> adj_view(rd_handle* h, int k) {
-    T* base = static_cast<T*>(h->adj.adj[k]);
-    const size_t n = (size_t)h->n;
-    return AdjState<T>{base, base + 3 * n, base + 6 * n, base + 15 * n, base + 24 * n};
+    return AdjState<T>{static_cast<vec4<T>*>(h->adj.adj[k]), (size_t)h->n};
 }
 
 // Puts the handle's state back to `src` (a stored state) for the next step.
@@ -1470,8 +1469,8 @@ template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
         const vec4<T>* after = reinterpret_cast<const vec4<T>*>(at(a.sstore[b], (size_t)len, a.state_bytes));
         const unsigned nb256 = blocks_for(n, 256);
         if (seg == nseg - 1) {  // dL/dx, dL/dv of the final state (staged in adj[2] by id)
-            const AdjState<T> S = adj_view<T>(h, 2);
-            k_adj_seed<T><<<nb256, 256, 0, rs>>>((int)n, after, S.x, S.v, adj_view<T>(h, nxt));
+            const T* gx = static_cast<const T*>(a.adj[2]);  // staged by particle id (adjoint_backward_impl)
+            k_adj_seed<T><<<nb256, 256, 0, rs>>>((int)n, after, gx, gx + 3 * n, adj_view<T>(h, nxt));
             RD_TRY(launched(h, "k_adj_seed"));
         } else {  // from the order of the next segment's checkpoint
             const vec4<T>* ck = reinterpret_cast<const vec4<T>*>(at(a.ckpt, (size_t)seg + 1, a.state_bytes));
@@ -1577,12 +1576,14 @@ rd_status adjoint_backward_impl(rd_handle* h, const void* grad_x, const void* gr
     const bool batch = batched(h);
     const cudaMemcpyKind kin = where == RD_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
     int nxt = 1;
-    if (n) {  // dL/dx, dL/dv of the final state by particle id, staged for the sweep's seed
-        const AdjState<T> S = adj_view<T>(h, 2);
-        if (grad_x) RD_TRY(check_cuda(h, cudaMemcpyAsync(S.x, grad_x, 3 * n * sizeof(T), kin, h->stream), "adjoint seed"));
-        else RD_TRY(check_cuda(h, cudaMemsetAsync(S.x, 0, 3 * n * sizeof(T), h->stream), "adjoint seed"));
-        if (grad_v) RD_TRY(check_cuda(h, cudaMemcpyAsync(S.v, grad_v, 3 * n * sizeof(T), kin, h->stream), "adjoint seed"));
-        else RD_TRY(check_cuda(h, cudaMemsetAsync(S.v, 0, 3 * n * sizeof(T), h->stream), "adjoint seed"));
+    if (n) {  // dL/dx, dL/dv of the final state by particle id (n x 3 each), staged in the
+              // scratch adjoint for the sweep's seed
+        T* sx = static_cast<T*>(a.adj[2]);
+        T* sv = sx + 3 * n;
+        if (grad_x) RD_TRY(check_cuda(h, cudaMemcpyAsync(sx, grad_x, 3 * n * sizeof(T), kin, h->stream), "adjoint seed"));
+        else RD_TRY(check_cuda(h, cudaMemsetAsync(sx, 0, 3 * n * sizeof(T), h->stream), "adjoint seed"));
+        if (grad_v) RD_TRY(check_cuda(h, cudaMemcpyAsync(sv, grad_v, 3 * n * sizeof(T), kin, h->stream), "adjoint seed"));
+        else RD_TRY(check_cuda(h, cudaMemsetAsync(sv, 0, 3 * n * sizeof(T), h->stream), "adjoint seed"));
     }
     RD_TRY(check_cuda(h, cudaMemsetAsync(a.pacc, 0, kAccPerScene * std::max<size_t>(n, 1) * sizeof(double), h->stream),
                       "adjoint acc"));
@@ -1599,7 +1600,7 @@ rd_status adjoint_backward_impl(rd_handle* h, const void* grad_x, const void* gr
                                                                    (int)h->scenes.size(), h->n, a.acc);
     RD_TRY(launched(h, "k_reduce_acc"));
     if (out && out->v0 && n) {  // dL/dv of the start state (checkpoint 0) in particle id order
-        T* dst = where == RD_HOST ? adj_view<T>(h, 2).v : static_cast<T*>(out->v0);
+        T* dst = where == RD_HOST ? static_cast<T*>(a.adj[2]) : static_cast<T*>(out->v0);
         k_adj_out<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, static_cast<const vec4<T>*>(a.ckpt),
                                                                  adj_view<T>(h, nxt), dst);
         RD_TRY(launched(h, "k_adj_out"));
