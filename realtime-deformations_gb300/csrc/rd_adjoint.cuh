@@ -119,7 +119,15 @@ constexpr int kAccPerScene = 4;
 
 // Per-scene parameter adjoints are summed per sorted position over all steps
 // (position s belongs to the same scene in every step) and reduced per scene
-// at the end: pacc[4 s + k], k = mu0, lambda0, theta_c, theta_s.
+// at the end.  pacc holds two double2 planes of n: (mu0, lambda0) at s and
+// (theta_c, theta_s) at n + s, so each reverse kernel adds its pair with one
+// coalesced 16-byte read-modify-write.
+__device__ __forceinline__ void acc_add2(double* pacc, size_t plane_off, double a, double b) {
+    double2* q = reinterpret_cast<double2*>(pacc) + plane_off;
+    const double2 o = *q;
+    *q = make_double2(o.x + a, o.y + b);
+}
+
 __global__ void __launch_bounds__(256) k_reduce_acc(const double* __restrict__ pacc,
                                                     const uint32_t* __restrict__ spoff, int nscenes, int n,
                                                     double* __restrict__ acc) {
@@ -128,9 +136,11 @@ __global__ void __launch_bounds__(256) k_reduce_acc(const double* __restrict__ p
     if (s >= nscenes) return;
     const int lo = spoff ? (int)spoff[s] : 0, hi = spoff ? (int)spoff[s + 1] : n;
     double sum[kAccPerScene] = {0.0, 0.0, 0.0, 0.0};
-    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x)
-#pragma unroll
-        for (int k = 0; k < kAccPerScene; ++k) sum[k] += pacc[(size_t)kAccPerScene * i + k];
+    const double2* pp = reinterpret_cast<const double2*>(pacc);
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const double2 ml = pp[i], th = pp[(size_t)n + i];
+        sum[0] += ml.x; sum[1] += ml.y; sum[2] += th.x; sum[3] += th.y;
+    }
 #pragma unroll
     for (int k = 0; k < kAccPerScene; ++k) {
         double v = sum[k];
@@ -412,8 +422,7 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
             adj_store_mat(part, kAdjF, sp, pF);
             adj_store_mat(part, kAdjB, sp, pB);
             adj_store_xj(part, sp, xb, Jpb1 * g_ratio);
-            pacc[(size_t)kAccPerScene * sp + 2] += (double)thc_b;
-            pacc[(size_t)kAccPerScene * sp + 3] += (double)ths_b;
+            acc_add2(pacc, (size_t)P.n + sp, (double)thc_b, (double)ths_b);
         }
     }
     sort_ranked<T, kBlk>(S.p, j, rcell, rrank);
@@ -575,8 +584,7 @@ __device__ __forceinline__ void adj_p2g_item(const DevParams<T>& P, const DevBuf
                 for (int e = 0; e < 9; ++e) M[e] += Fb[e];
                 adj_store_mat(cur, kAdjF, idx, M);
             }
-            pacc[(size_t)kAccPerScene * sp + 0] += (double)mu0b;
-            pacc[(size_t)kAccPerScene * sp + 1] += (double)lam0b;
+            acc_add2(pacc, sp, (double)mu0b, (double)lam0b);
         } else {
             raise_flag(D.flags, 4u);
         }
