@@ -888,6 +888,9 @@ void rd_default_params(rd_params* p) {
 
 namespace {
 
+// At least 8 nodes per axis: the stencil needs them, and the fused kernel's
+// TMA box (kTile nodes per axis) then never exceeds a grid axis.
+static_assert(kTile <= 8, "tile copies assume grids of at least kTile nodes per axis");
 bool valid_scene(const rd_params& p) {
     return p.max_i >= 8 && p.max_j >= 8 && p.max_k >= 8 && p.num_particles >= 0 && p.h > 0 &&
            (p.precision == RD_FP32 || p.precision == RD_FP64) && p.bc_width >= 0 &&
