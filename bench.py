@@ -292,7 +292,8 @@ def measure_adjoint(pkg, local, reps=3):
     checkpoint every 10, loss ||centroid(x_T) - (0.55, 0.3, 0.5)||^2, gradients
     with respect to v0 (per particle), E and nu; against the plain forward of
     the same 50 steps, both timed on the host clock around synchronised calls
-    (best of `reps`)."""
+    (best of `reps`): the record and the backward are the timed library calls,
+    the loss and dL/dx_T are computed on the host between them, untimed."""
     graft.load_package()
     from rd_gb300 import scenes
     sc = scenes.cube(seed=0)
@@ -315,11 +316,13 @@ def measure_adjoint(pkg, local, reps=3):
         start()
         t0 = time.perf_counter()
         sim.adjoint_record(sc.dt, steps, every)
-        xT = sim.get_particles(("x",))["x"].astype(np.float64)
+        sim.synchronize()
         t1 = time.perf_counter()
+        xT = sim.get_particles(("x",))["x"].astype(np.float64)  # the loss, on the host, untimed
         gx = np.tile(2.0 * (xT.mean(0) - target) / sc.n, (sc.n, 1)).astype(np.float32)
+        t2 = time.perf_counter()
         g = sim.adjoint_backward(gx)
-        t_fa.append(time.perf_counter() - t0)
+        t_fa.append((t1 - t0) + (time.perf_counter() - t2))
         t_rec.append(t1 - t0)
     # per-kernel split of one forward + adjoint (events around each launch)
     start()
@@ -345,8 +348,9 @@ def measure_batched_adjoint(pkg, local):
     on 64^3-96^3 grids, 100 steps, checkpoint every 10; per-scene loss = mean
     squared position error against a target rollout run at E = 2e5,
     theta = (2e-2, 5e-3); gradients w.r.t. each scene's E, theta_c, theta_s.
-    Host-clock time of record + backward against the batched forward of the
-    same steps."""
+    Host-clock time of the two library calls, the record and the backward
+    (the loss and its gradient dL/dx_T are computed on the host between them,
+    untimed), against the batched forward of the same steps."""
     graft.load_package()
     from rd_gb300 import scenes
     batch = scenes.uneven_snowballs(seed=1, nscenes=32, n_lo=16384, n_hi=131072, g_lo=64, g_hi=96, steps=100)
@@ -386,13 +390,17 @@ def measure_batched_adjoint(pkg, local):
         b.synchronize()
         t0 = time.perf_counter()
         b.adjoint_record(dt, steps, every)
+        b.synchronize()
+        t_rec = time.perf_counter() - t0
         gx, loss = [], []
         for i, s in enumerate(batch):
             x = b.get_particles(i, ("x",))["x"].astype(np.float64)
             loss.append(float(np.mean(np.sum((x - xt[i]) ** 2, axis=1))))
             gx.append((2.0 * (x - xt[i]) / s.n).astype(np.float32))
-        g = b.adjoint_backward(np.concatenate(gx))
-        t_fa.append(time.perf_counter() - t0)
+        gxa = np.concatenate(gx)
+        t0 = time.perf_counter()
+        g = b.adjoint_backward(gxa)
+        t_fa.append(t_rec + time.perf_counter() - t0)
     n = b.n
     b.close()
     fwd, fa = min(t_fwd[1:]), min(t_fa[1:])
