@@ -370,24 +370,36 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
             }
 #pragma unroll
             for (int c = 0; c < 3; ++c) xb[c] -= Bb[c] * vn[0] + Bb[3 + c] * vn[1] + Bb[6 + c] * vn[2];
-            // x_b += sum grad w_i (vh_i . (v'_b + B'_b d_i))
-            for (int ox = 0; ox < 4; ++ox)
+            // x_b += sum_i grad w_i s_i with s_i = vh_i . u_i, u_i = v'_b + B'_b d_i.
+            // Separably: for each (ox, oy) column u = (v'_b + B'_b[:,0] d_x +
+            // B'_b[:,1] d_y) + B'_b[:,2] d_z, and the z sums c0 = sum w_z s,
+            // c1 = sum dw_z s come first, then the y sums, then the x sums.
+            for (int ox = 0; ox < 4; ++ox) {
+                T ax = T(0), ay = T(0), az = T(0);
                 for (int oy = 0; oy < 4; ++oy) {
                     const int rowc = ((St.rel[0] + ox) * kTile + (St.rel[1] + oy)) * kTile + St.rel[2];
+                    T ucol[3];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+                        ucol[r] = vb[r] + Bb[3 * r] * St.d[0][ox] + Bb[3 * r + 1] * St.d[1][oy];
+                    T c0 = T(0), c1 = T(0);
 #pragma unroll
                     for (int oz = 0; oz < 4; ++oz) {
                         const vec4<T> v4 = S.gv[rowc + oz];
-                        const T d[3] = {St.d[0][ox], St.d[1][oy], St.d[2][oz]};
-                        T u[3];
-#pragma unroll
-                        for (int r = 0; r < 3; ++r)
-                            u[r] = vb[r] + (Bb[3 * r] * d[0] + Bb[3 * r + 1] * d[1] + Bb[3 * r + 2] * d[2]);
-                        const T sdot = v4.x * u[0] + v4.y * u[1] + v4.z * u[2];
-                        xb[0] += sdot * (dw[0][ox] * St.w[1][oy] * St.w[2][oz]);
-                        xb[1] += sdot * (St.w[0][ox] * dw[1][oy] * St.w[2][oz]);
-                        xb[2] += sdot * (St.w[0][ox] * St.w[1][oy] * dw[2][oz]);
+                        const T dz = St.d[2][oz];
+                        const T sdot = v4.x * (ucol[0] + Bb[2] * dz) + v4.y * (ucol[1] + Bb[5] * dz) +
+                                       v4.z * (ucol[2] + Bb[8] * dz);
+                        c0 += St.w[2][oz] * sdot;
+                        c1 += dw[2][oz] * sdot;
                     }
+                    ax += St.w[1][oy] * c0;
+                    ay += dw[1][oy] * c0;
+                    az += St.w[1][oy] * c1;
                 }
+                xb[0] += dw[0][ox] * ax;
+                xb[1] += St.w[0][ox] * ay;
+                xb[2] += St.w[0][ox] * az;
+            }
             // the vh_b scatter as a record: q' = v'_b + B'_b e, A = B'_b
             write_record<T, false>(&S.p.rec[j * kRecV4], St, p.x, Bb, vb, T(0), P.h);
             rcell = (St.rel[0] * kBlk + St.rel[1]) * kBlk + St.rel[2];
