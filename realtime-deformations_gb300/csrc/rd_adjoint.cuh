@@ -298,6 +298,10 @@ __device__ __forceinline__ void stress_backward(const DevParams<T>& P, const T F
 // Both reverse kernels walk the work items of the sort of the step-n state
 // (kept from the recompute): a CTA per item, one particle per thread.
 constexpr int kAdjThreads = 256;
+// Two resident CTAs per SM in FP32 (at most 128 registers a thread; the batch
+// instantiations would otherwise take more and run one CTA, half the warps);
+// FP64 needs over 200 registers a thread and runs one.
+template <typename T> constexpr int kAdjMinBlocks = sizeof(T) == 4 ? 2 : 1;
 static_assert(WorkP<float>::value <= kAdjThreads && WorkP<double>::value <= kAdjThreads,
               "one particle per thread");
 
@@ -445,7 +449,7 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
 }
 
 template <typename T, bool BATCH>
-__global__ void __launch_bounds__(kAdjThreads) k_adj_g2p(DevParams<T> P0, DevBufs D, const vec4<T>* __restrict__ st,
+__global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks<T>) k_adj_g2p(DevParams<T> P0, DevBufs D, const vec4<T>* __restrict__ st,
                                                         const vec4<T>* __restrict__ grid0,
                                                         vec4<T>* __restrict__ agrid0, AdjState<T> nxt,
                                                         AdjState<T> part, double* __restrict__ pacc,
@@ -605,7 +609,7 @@ __device__ __forceinline__ void adj_p2g_item(const DevParams<T>& P, const DevBuf
 }
 
 template <typename T, bool BATCH>
-__global__ void __launch_bounds__(kAdjThreads) k_adj_p2g(DevParams<T> P0, DevBufs D, const vec4<T>* __restrict__ st,
+__global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks<T>) k_adj_p2g(DevParams<T> P0, DevBufs D, const vec4<T>* __restrict__ st,
                                                         const vec4<T>* __restrict__ grid0,
                                                         const vec4<T>* __restrict__ agrid0, AdjState<T> part,
                                                         AdjState<T> cur, double* __restrict__ pacc,
