@@ -56,6 +56,12 @@ struct DevBufs {
     // fused kernel, adjoint segments: U, singular values and V of each
     // particle's plastic split, 6 vec4 planes by sorted slot (null: not kept)
     void* split_out;
+    // k_p2g of a step whose particles are not in sorted order (after an
+    // upload): the particles copied to these planes at their sorted
+    // positions, and perm_reset[s] = s, so the fused kernel then reads them
+    // in order (null: no copy)
+    void* reorder_out;
+    uint32_t* perm_reset;
     uint32_t* bcount;  // particles per 4x4x4 block (the block sums of counts)
     uint8_t* gmark;       // blocks of grid that hold data (set by every writer)
     uint8_t* gmark_next;  // the same for grid_next
@@ -1008,6 +1014,10 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         Particle<T> p;
         load_particle(pl, n, D.perm[it.y + j], p);
+        if (D.reorder_out) {  // the particle to its sorted position
+            store_particle(static_cast<vec4<T>*>(D.reorder_out), n, (size_t)(it.y + j), p);
+            D.perm_reset[it.y + j] = (uint32_t)(it.y + j);
+        }
         Stencil<T> St;
         if (!make_stencil(P, p.x, org, St)) {
             raise_flag(D.flags, 4u);

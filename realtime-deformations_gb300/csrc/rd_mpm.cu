@@ -541,6 +541,16 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
         RD_TRY(clear_grid<T>(h, h->g));
         tmark_end(h, t);
         DevBufs D = bufs<T>(h);
+        // particles not yet in sorted order (an upload): k_p2g, which reads
+        // them all through the permutation, also writes them to the other
+        // plane buffer in order, so the fused kernel reads them sequentially.
+        // Not in the adjoint's stored segments, whose plane buffers are the
+        // store's slots.
+        const bool reorder = !h->split_out && !h->prm.track_fp;
+        if (reorder) {
+            D.reorder_out = h->pl[h->cur ^ 1];
+            D.perm_reset = h->perm;
+        }
         t = tmark_begin(h, RD_KERNEL_P2G);
         const unsigned pg = persistent_grid<T>(h, h->occ_p2g);
         if (batch)
@@ -549,6 +559,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
             k_p2g<T, true, true, false><<<pg, kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
         tmark_end(h, t);
         RD_TRY(launched(h, "k_p2g"));
+        if (reorder) h->cur ^= 1;  // the ordered copy is the state now; perm is the identity
     }
     t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
     RD_TRY(clear_grid<T>(h, h->g ^ 1));
