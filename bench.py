@@ -65,8 +65,10 @@ def parse_args():
     ap.add_argument("--adjoint", type=int, default=1, help="measure forward + adjoint on the 65,536-particle cube")
     ap.add_argument("--only", choices=("batched", "adjoint", "batched_adjoint"), default=None,
                     help="run one secondary measurement alone and print its JSON (profiling runs)")
-    ap.add_argument("--batch-steps", type=int, default=300,
-                    help="timed steps of the batched-forward workload (64 uneven scenes); 0 skips it")
+    ap.add_argument("--batch-steps", type=int, default=-1,
+                    help="timed steps of the batched-forward workload (64 uneven scenes); -1: as many as "
+                         "--steps, so the batch and the plain forward it is compared with run equally long; "
+                         "0 skips it")
     return ap.parse_args()
 
 
@@ -544,8 +546,9 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
-    if args.batch_steps > 0:
-        out["batched_forward"] = measure_batched(pkg, local, args.batch_steps, max(args.warmup, 3), value)
+    batch_steps = args.steps if args.batch_steps < 0 else args.batch_steps
+    if batch_steps > 0:
+        out["batched_forward"] = measure_batched(pkg, local, batch_steps, max(args.warmup, 3), value)
     if args.adjoint:
         out["forward_adjoint"] = measure_adjoint(pkg, local)
         out["batched_forward_adjoint"] = measure_batched_adjoint(pkg, local)
