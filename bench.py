@@ -488,20 +488,22 @@ def run_ours(args):
     fields = ("x", "v", "B", "FE", "Jp", "mass", "volume")
     shapes = {"x": (sc.n, 3), "v": (sc.n, 3), "B": (sc.n, 9), "FE": (sc.n, 9), "Jp": (sc.n,), "mass": (sc.n,),
               "volume": (sc.n,)}
-    host = {k: torch.empty(shapes[k], dtype=torch.float32, pin_memory=True).numpy() for k in fields}
+    pinned = {k: torch.empty(shapes[k], dtype=torch.float32, pin_memory=True).numpy() for k in fields}
     reset()
     sim.step(sc.dt, args.warmup)
-    sim.get_particles(fields, out=host)
+    sim.get_particles(fields, out=pinned)
+    pageable = {k: a.copy() for k, a in pinned.items()}
     e2e_steps = max(1, args.e2e_steps)
 
-    def e2e_pass(mapped):
-        """Every step: the whole state in from pinned host memory, one step, the
-        whole state back out, then the host waits for it.  Staged: rd_*_particles
-        with RD_HOST (copies to and from a device buffer around the pack and
-        unpack kernels); mapped: the same pinned buffers passed as RD_DEVICE, so
-        the pack and unpack kernels read and write host memory directly."""
+    def e2e_pass(host, mapped):
+        """Every step: the whole state in from host memory, one step, the whole
+        state back out, then the host waits for it.  RD_HOST on page-locked
+        arrays: the pack and unpack kernels read and write them in place over
+        the CPU-GPU link; on pageable arrays: copies through the device staging
+        buffer; mapped: the page-locked arrays passed as RD_DEVICE pointers."""
         sim.synchronize()
         barrier(ws)
+        io0 = sim.io_bytes()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             sim.set_particles(host["x"], host["v"], host["mass"], B=host["B"], FE=host["FE"], Jp=host["Jp"],
@@ -511,13 +513,17 @@ def run_ours(args):
             if mapped:
                 sim.synchronize()
         el = time.perf_counter() - t0
-        return max_over_ranks(ws, el, device=torch.device("cuda", local))
+        io1 = sim.io_bytes()
+        moved = ((io1[0] - io0[0]) // e2e_steps, (io1[1] - io0[1]) // e2e_steps)
+        return max_over_ranks(ws, el, device=torch.device("cuda", local)), moved
 
-    e2e_s = e2e_pass(False)
-    e2e_mapped_s = e2e_pass(True)
+    e2e_s, e2e_moved = e2e_pass(pinned, False)
+    e2e_mapped_s, _ = e2e_pass(pinned, True)
+    e2e_pageable_s, pageable_moved = e2e_pass(pageable, False)
     io_bytes = sum(int(np.prod(shapes[k])) * 4 for k in fields)
     e2e_value = ws * sc.n * e2e_steps / e2e_s
     e2e_mapped = ws * sc.n * e2e_steps / e2e_mapped_s
+    e2e_pageable = ws * sc.n * e2e_steps / e2e_pageable_s
 
     out = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
@@ -529,11 +535,15 @@ def run_ours(args):
                    "l2": f"inputs larger than L2: {2 * 7 * 16 * sc.n / 1e6:.0f} MB of particle planes per step"},
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes, "steps": e2e_steps,
-                "path": "rd_set_particles(host) + rd_step + rd_get_particles(host), pinned buffers "
-                        "(cudaMemcpyAsync to and from a device staging buffer around the pack / unpack kernels)",
+                "path": "rd_set_particles(RD_HOST) + rd_step + rd_get_particles(RD_HOST) on page-locked host "
+                        "arrays: the pack / unpack kernels read and write them in place over NVLink-C2C",
+                "bytes_in_place_per_step": e2e_moved[0], "bytes_staged_per_step": e2e_moved[1],
                 "mapped_value": e2e_mapped,
-                "mapped_path": "the same pinned buffers passed as device-accessible pointers: the pack / unpack "
-                               "kernels read and write host memory directly (slower: strided small transfers)"},
+                "mapped_path": "the same page-locked arrays passed as RD_DEVICE pointers (same kernels)",
+                "pageable_value": e2e_pageable,
+                "pageable_path": "pageable host arrays: cudaMemcpyAsync to and from the device staging buffer "
+                                 "around the pack / unpack kernels",
+                "pageable_bytes_staged_per_step": pageable_moved[1]},
         "roofline": {"bound": "hbm", "kernel": {"p2g": "k_p2g", "g2p2g": "k_g2p2g"}[dom],
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src,

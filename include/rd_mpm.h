@@ -112,10 +112,17 @@ rd_status rd_create(const rd_params* params, rd_handle** out);
 rd_status rd_destroy(rd_handle* h);
 
 /* Writes particle state (initializeParticles / writes through getParticles(),
- * material_point_method.cpp:18-63, .hpp:181-183).  where = RD_HOST or RD_DEVICE. */
+ * material_point_method.cpp:18-63, .hpp:181-183).  where = RD_HOST or RD_DEVICE.
+ * RD_HOST: a field in page-locked host memory (cudaHostAlloc, cudaHostRegister)
+ * is read in place by the packing kernel over the CPU-GPU link; other host
+ * fields are copied to a device staging buffer first.  Either way the call
+ * returns once the work is queued: the arrays stay untouched until the
+ * handle's stream reaches it (rd_synchronize). */
 rd_status rd_set_particles(rd_handle* h, const rd_particles* in, int where);
 /* Reads particle state in the caller's original particle order (getParticles()).
- * Fields left NULL are skipped. */
+ * Fields left NULL are skipped.  RD_HOST: page-locked fields are written in
+ * place by the unpacking kernel, the others through a staging buffer; the
+ * call returns when the data is there.  RD_DEVICE: returns once queued. */
 rd_status rd_get_particles(rd_handle* h, rd_particles* out, int where);
 
 /* rasterizeParticlesToGrid + computeParticleVolumesAndDensities, main.cpp:53-54. */
@@ -220,6 +227,10 @@ rd_status rd_kernel_timing(rd_handle* h, int kernel, uint64_t* launches, double*
 rd_status rd_launch_count(rd_handle* h, uint64_t* count);
 /* Number of two-step CUDA graphs this handle has replayed (rd_set_graphs). */
 rd_status rd_graph_replays(rd_handle* h, uint64_t* count);
+/* Bytes of particle state moved by rd_set_particles / rd_get_particles with
+ * RD_HOST so far: read or written in place in page-locked host memory, and
+ * through the device staging buffer. */
+rd_status rd_io_bytes(rd_handle* h, uint64_t* in_place, uint64_t* staged);
 
 /* initializeParticles (material_point_method.cpp:18-63) on the device: the cells
  * within radius / h of the origin, 8 points per cell at quarter offsets, each

@@ -45,7 +45,7 @@ STAGES = {"rasterize": 0, "forces": 1, "grid_velocities": 2, "collisions": 3,
 EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "rd_get_particles",
            "rd_init_volumes", "rd_step", "rd_stage", "rd_get_grid", "rd_device_xyzs", "rd_get_flags",
            "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort", "rd_debug_wait_timeout",
-           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_graph_replays", "rd_batch_create",
+           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_graph_replays", "rd_io_bytes", "rd_batch_create",
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
            "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
@@ -195,6 +195,7 @@ def lib():
             L.rd_debug_wait_timeout.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
             L.rd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
             L.rd_graph_replays.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+            L.rd_io_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
             L.rd_rasterize_noalloc.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(_Particles), vp, vp]
             L.rd_batch_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int32, ctypes.POINTER(vp)]
             L.rd_batch_num_scenes.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
@@ -315,12 +316,13 @@ class Simulation:
 
     def set_particles(self, x, v, mass, B=None, FE=None, FP=None, Jp=None, volume=None, sync=True,
                       mapped=False):
-        """Copies host arrays in (rd_set_particles).  With sync=False the call
-        returns once the copies are queued; the arrays must stay alive and
+        """Copies host arrays in (rd_set_particles).  Arrays in page-locked
+        memory (torch ``pin_memory``) are read in place by the packing kernel,
+        the others go through a device staging buffer.  With sync=False the
+        call returns once the work is queued; the arrays must stay alive and
         unchanged until the handle's stream reaches them.  mapped=True passes
-        the arrays as device-accessible pointers (RD_DEVICE): for pinned host
-        memory the packing kernel then reads them directly, with no staging
-        copy (unified addressing)."""
+        the arrays as device-accessible pointers (RD_DEVICE) without the
+        page-locked check."""
         ps, self._pending = self._particles_in(self.n, x, v, mass, B, FE, FP, Jp, volume)
         self._check(lib().rd_set_particles(self._h, ctypes.byref(ps), RD_DEVICE if mapped else RD_HOST),
                     "rd_set_particles")
@@ -329,10 +331,10 @@ class Simulation:
 
     def get_particles(self, fields=("x", "v", "B", "FE", "FP", "Jp", "mass", "volume"), out=None, mapped=False):
         """Copies the particle state out in the original particle order
-        (rd_get_particles).  ``out`` may supply the destination arrays.  With
-        mapped=True (``out`` in pinned host memory) the unpacking kernel writes
-        them directly and the call returns without waiting: synchronize()
-        before reading."""
+        (rd_get_particles).  ``out`` may supply the destination arrays;
+        page-locked ones are written in place by the unpacking kernel.  With
+        mapped=True (``out`` device-accessible, e.g. pinned host memory) the
+        call returns without waiting: synchronize() before reading."""
         ps, out = self._particles_out(self.n, fields, out)
         self._check(lib().rd_get_particles(self._h, ctypes.byref(ps), RD_DEVICE if mapped else RD_HOST),
                     "rd_get_particles")
@@ -417,6 +419,14 @@ class Simulation:
         c = ctypes.c_uint64()
         self._check(lib().rd_graph_replays(self._h, ctypes.byref(c)), "rd_graph_replays")
         return c.value
+
+    def io_bytes(self):
+        """(in place, staged): particle bytes that set_particles / get_particles
+        moved straight from and to page-locked host arrays, and through the
+        device staging buffer (rd_io_bytes)."""
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(lib().rd_io_bytes(self._h, ctypes.byref(a), ctypes.byref(b)), "rd_io_bytes")
+        return a.value, b.value
 
     @property
     def num_scenes(self) -> int:

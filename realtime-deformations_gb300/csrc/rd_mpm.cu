@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -34,65 +35,122 @@ struct NvtxRange {
 
 enum GridMode { GRID_NONE = 0, GRID_FUSED = 1, GRID_MV = 2, GRID_V = 3 };
 
-// Particles off .. off + n - 1 of planes holding ntot particles (one scene of
-// a batch, or all of a single scene), from structure-of-arrays input.
-template <typename T>
-__global__ void k_pack(int n, int off, int ntot, const T* __restrict__ x, const T* __restrict__ v, const T* __restrict__ B,
-                       const T* __restrict__ FE, const T* __restrict__ FP, const T* __restrict__ Jp,
-                       const T* __restrict__ mass, const T* __restrict__ vol, vec4<T>* __restrict__ pl,
-                       int track_fp) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    Particle<T> p;
-    T P[9];
+// Rows of K reals per particle (x, v: K = 3; B, F_E, F_P: K = 9) of the
+// caller's structure-of-arrays buffers move through shared memory, so that
+// consecutive threads touch consecutive words of the K-strided row array.
+// Called by every thread of a 256-thread block; rows r0 .. r0 + cnt - 1 are
+// the block's, thread t's row is r0 + t.
+constexpr int kIoThreads = 256;
+template <typename T, int K>
+__device__ __forceinline__ void load_rows(const T* __restrict__ src, int r0, int cnt, T (&val)[K], T* sh) {
+    __syncthreads();  // the previous use of sh is done
+    const T* s = src + (size_t)r0 * K;
+    for (int e = threadIdx.x; e < cnt * K; e += blockDim.x) sh[e] = s[e];
+    __syncthreads();
 #pragma unroll
-    for (int a = 0; a < 3; ++a) { p.x[a] = x[3 * i + a]; p.v[a] = v[3 * i + a]; }
+    for (int k = 0; k < K; ++k) val[k] = sh[threadIdx.x * K + k];  // rows past cnt: not used
+}
+template <typename T, int K>
+__device__ __forceinline__ void store_rows(T* __restrict__ dst, int r0, int cnt, const T (&val)[K], T* sh) {
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) sh[threadIdx.x * K + k] = val[k];
+    __syncthreads();
+    T* d = dst + (size_t)r0 * K;
+    for (int e = threadIdx.x; e < cnt * K; e += blockDim.x) d[e] = sh[e];
+}
+
+// Particles off .. off + n - 1 of planes holding ntot particles (one scene of
+// a batch, or all of a single scene), from structure-of-arrays input in
+// particle id order; particle i goes to slot off + i.
+template <typename T>
+__global__ void __launch_bounds__(kIoThreads)
+    k_pack(int n, int off, int ntot, const T* __restrict__ x, const T* __restrict__ v, const T* __restrict__ B,
+           const T* __restrict__ FE, const T* __restrict__ FP, const T* __restrict__ Jp, const T* __restrict__ mass,
+           const T* __restrict__ vol, vec4<T>* __restrict__ pl, int track_fp) {
+    __shared__ T sh[9 * kIoThreads];
+    const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
+    const int cnt = min((int)blockDim.x, n - r0);
+    Particle<T> p;
+    T P[9], t3[3];
+    load_rows(x, r0, cnt, t3, sh);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) p.x[a] = t3[a];
+    load_rows(v, r0, cnt, t3, sh);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) p.v[a] = t3[a];
+    if (B) {
+        load_rows(B, r0, cnt, p.B, sh);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 9; ++e) p.B[e] = T(0);
+    }
+    if (FE) {
+        load_rows(FE, r0, cnt, p.F, sh);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 9; ++e) p.F[e] = (e % 4 == 0) ? T(1) : T(0);
+    }
+    if (FP) {
+        load_rows(FP, r0, cnt, P, sh);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 9; ++e) P[e] = (e % 4 == 0) ? T(1) : T(0);
+    }
+    if (i >= n) return;
     p.m = mass[i];
     p.vol = vol ? vol[i] : T(0);
-#pragma unroll
-    for (int e = 0; e < 9; ++e) {
-        p.B[e] = B ? B[9 * i + e] : T(0);
-        p.F[e] = FE ? FE[9 * i + e] : ((e % 4 == 0) ? T(1) : T(0));
-        P[e] = FP ? FP[9 * i + e] : ((e % 4 == 0) ? T(1) : T(0));
-    }
     p.Jp = Jp ? Jp[i] : (FP ? det3(P) : T(1));
     p.id = (uint32_t)(off + i);
     store_particle(pl, (size_t)ntot, (size_t)(off + i), p);
     if (track_fp) store_fp(pl, (size_t)ntot, (size_t)(off + i), P);
 }
 
+// The slot of each particle of a scene (particles off .. off + n - 1 in
+// slots off .. off + n - 1, in any order): slot[id - off].
 template <typename T>
-__global__ void k_unpack(int n, int off, int ntot, const vec4<T>* __restrict__ pl, T* __restrict__ x, T* __restrict__ v,
-                         T* __restrict__ B, T* __restrict__ FE, T* __restrict__ FP, T* __restrict__ Jp,
-                         T* __restrict__ mass, T* __restrict__ vol, int track_fp) {
+__global__ void k_slot_of_id(int n, int off, int ntot, const vec4<T>* __restrict__ pl, uint32_t* __restrict__ slot) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const uint32_t o = real_to_id<T>(pl[6 * (size_t)ntot + off + i].w) - (uint32_t)off;
+    if (o < (uint32_t)n) slot[o] = (uint32_t)(off + i);
+}
+
+// The scene's particles in id order: thread o gathers particle id off + o
+// from its slot and the rows go out coalesced (a slot outside the scene's,
+// which a consistent state never holds, gives a zero row).
+template <typename T>
+__global__ void __launch_bounds__(kIoThreads)
+    k_unpack(int n, int off, int ntot, const vec4<T>* __restrict__ pl, const uint32_t* __restrict__ slot,
+             T* __restrict__ x, T* __restrict__ v, T* __restrict__ B, T* __restrict__ FE, T* __restrict__ FP,
+             T* __restrict__ Jp, T* __restrict__ mass, T* __restrict__ vol, int track_fp) {
+    __shared__ T sh[9 * kIoThreads];
+    const int r0 = blockIdx.x * blockDim.x, o = r0 + threadIdx.x;
+    const int cnt = min((int)blockDim.x, n - r0);
     Particle<T> p;
-    load_particle(pl, (size_t)ntot, (size_t)(off + i), p);
-    const uint32_t o = p.id - (uint32_t)off;
-    if (o >= (uint32_t)n) return;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        if (x) x[3 * o + a] = p.x[a];
-        if (v) v[3 * o + a] = p.v[a];
-    }
-#pragma unroll
-    for (int e = 0; e < 9; ++e) {
-        if (B) B[9 * o + e] = p.B[e];
-        if (FE) FE[9 * o + e] = p.F[e];
-    }
-    if (FP) {
-        T P[9];
+    T P[9];
+    const uint32_t s = o < n ? slot[o] : 0xffffffffu;
+    const bool ok = s - (uint32_t)off < (uint32_t)n;
+    if (ok) {
+        load_particle(pl, (size_t)ntot, (size_t)s, p);
         if (track_fp) {
-            load_fp(pl, (size_t)ntot, (size_t)(off + i), P);
+            load_fp(pl, (size_t)ntot, (size_t)s, P);
         } else {  // only det F_P is carried: report the isotropic F_P with that det
             const T c = cbrt(p.Jp);
 #pragma unroll
             for (int e = 0; e < 9; ++e) P[e] = (e % 4 == 0) ? c : T(0);
         }
+    } else {
+        p.x[0] = p.x[1] = p.x[2] = p.v[0] = p.v[1] = p.v[2] = p.m = p.vol = p.Jp = T(0);
 #pragma unroll
-        for (int e = 0; e < 9; ++e) FP[9 * o + e] = P[e];
+        for (int e = 0; e < 9; ++e) p.B[e] = p.F[e] = P[e] = T(0);
     }
+    if (x) store_rows(x, r0, cnt, p.x, sh);
+    if (v) store_rows(v, r0, cnt, p.v, sh);
+    if (B) store_rows(B, r0, cnt, p.B, sh);
+    if (FE) store_rows(FE, r0, cnt, p.F, sh);
+    if (FP) store_rows(FP, r0, cnt, P, sh);
+    if (o >= n) return;
     if (Jp) Jp[o] = p.Jp;
     if (mass) mass[o] = p.m;
     if (vol) vol[o] = p.vol;
@@ -216,6 +274,7 @@ struct rd_handle {
     int cur = 0;
     uint32_t* keys[2] = {nullptr, nullptr};
     uint32_t* perm = nullptr;
+    uint32_t* slot_of = nullptr;  // slot of each particle id (rd_get_particles)
     uint32_t* counts = nullptr;
     uint32_t* bcount = nullptr;   // particles per block
     uint8_t* gmark[2] = {nullptr, nullptr};  // blocks of grid[0] / grid[1] holding data
@@ -244,6 +303,7 @@ struct rd_handle {
     int grid_mode = GRID_NONE;
     double last_dt = 0.0;
     uint64_t launches = 0, graph_replays = 0;
+    uint64_t io_direct = 0, io_staged = 0;  // particle bytes set / got in place in host memory, through staging
     void* split_out = nullptr;  // the fused kernel keeps each particle's plastic split here (adjoint segments)
     int occ_p2g = 1, occ_g2p = 1;
     std::string err;
@@ -659,6 +719,38 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
     }
 }
 
+// True when the kernels can read and write [p, p + bytes) in place: the range
+// lies inside one page-locked host allocation mapped at the same address on
+// the device (cudaHostAlloc / cudaHostRegister under unified addressing).
+// The pack and unpack kernels then move the particle state over the
+// CPU-GPU link themselves, with no staging copy through device memory; on a
+// Grace-Blackwell node that is faster than copying in and packing apart.
+bool host_in_place(const void* p, size_t bytes) {
+    using PtrAttr = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+    static PtrAttr attr = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q{};
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            attr = reinterpret_cast<PtrAttr>(fn);
+    });
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // an unknown pointer is not an error here
+        return false;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer != p || !attr) return false;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    if (attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, (CUdeviceptr)p) != CUDA_SUCCESS ||
+        attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, (CUdeviceptr)p) != CUDA_SUCCESS)
+        return false;
+    return (uintptr_t)p >= (uintptr_t)start && (uintptr_t)p + bytes <= (uintptr_t)start + size;
+}
+
 template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, const rd_particles* in, int where) {
     rd_scene_info& sc = h->scenes[scene];
     const size_t n = (size_t)sc.n;
@@ -671,16 +763,19 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, cons
     const T* ptr[8];
     for (int k = 0; k < 8; ++k) {
         if (!src[k] || n == 0) { ptr[k] = nullptr; continue; }
-        if (where == RD_HOST) {
+        if (where == RD_HOST && !host_in_place(src[k], cnt[k] * sizeof(T))) {
             RD_TRY(check_cuda(h, cudaMemcpyAsync(d[k], src[k], cnt[k] * sizeof(T), cudaMemcpyHostToDevice, h->stream),
                               "upload"));
             ptr[k] = d[k];
+            h->io_staged += cnt[k] * sizeof(T);
         } else {
             ptr[k] = static_cast<const T*>(src[k]);
+            if (where == RD_HOST) h->io_direct += cnt[k] * sizeof(T);
         }
     }
     if (n > 0) {
-        k_pack<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, (int)sc.poff, h->n, ptr[0], ptr[1], ptr[2], ptr[3],
+        k_pack<T><<<blocks_for(n, kIoThreads), kIoThreads, 0, h->stream>>>((int)n, (int)sc.poff, h->n, ptr[0], ptr[1],
+                                                                           ptr[2], ptr[3],
                                                              ptr[4], ptr[5], ptr[6], ptr[7],
                                                              static_cast<vec4<T>*>(h->pl[h->cur]), h->prm.track_fp);
         RD_TRY(launched(h, "k_pack"));
@@ -702,15 +797,21 @@ template <typename T> rd_status get_particles_impl(rd_handle* h, int scene, rd_p
     void* dst[8] = {out->x, out->v, out->B, out->FE, out->FP, out->Jp, out->mass, out->volume};
     const size_t cnt[8] = {3 * n, 3 * n, 9 * n, 9 * n, 9 * n, n, n, n};
     T* tgt[8];
-    for (int k = 0; k < 8; ++k) tgt[k] = dst[k] ? (where == RD_HOST ? d[k] : static_cast<T*>(dst[k])) : nullptr;
-    k_unpack<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, (int)sc.poff, h->n,
-                                                           static_cast<const vec4<T>*>(h->pl[h->cur]), tgt[0], tgt[1],
-                                                           tgt[2], tgt[3], tgt[4], tgt[5], tgt[6], tgt[7],
-                                                           h->prm.track_fp);
-    RD_TRY(launched(h, "k_unpack"));
+    bool staged[8];
+    for (int k = 0; k < 8; ++k) {
+        staged[k] = dst[k] && where == RD_HOST && !host_in_place(dst[k], cnt[k] * sizeof(T));
+        tgt[k] = dst[k] ? (staged[k] ? d[k] : static_cast<T*>(dst[k])) : nullptr;
+        if (dst[k] && where == RD_HOST) (staged[k] ? h->io_staged : h->io_direct) += cnt[k] * sizeof(T);
+    }
+    const vec4<T>* pl = static_cast<const vec4<T>*>(h->pl[h->cur]);
+    k_slot_of_id<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, (int)sc.poff, h->n, pl, h->slot_of);
+    k_unpack<T><<<blocks_for(n, kIoThreads), kIoThreads, 0, h->stream>>>((int)n, (int)sc.poff, h->n, pl, h->slot_of,
+                                                                         tgt[0], tgt[1], tgt[2], tgt[3], tgt[4],
+                                                                         tgt[5], tgt[6], tgt[7], h->prm.track_fp);
+    RD_TRY(launched(h, "k_unpack", 2));
     if (where == RD_HOST) {
         for (int k = 0; k < 8; ++k)
-            if (dst[k])
+            if (staged[k])
                 RD_TRY(check_cuda(h, cudaMemcpyAsync(dst[k], d[k], cnt[k] * sizeof(T), cudaMemcpyDeviceToHost, h->stream),
                                   "download"));
         RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "sync"));
@@ -860,7 +961,7 @@ void release(rd_handle* h) {
                      a.agrid, a.pacc, a.acc};
     for (void* p : aptrs)
         if (p) cudaFree(p);
-    void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->counts, h->bcount, h->gmark[0],
+    void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->slot_of, h->counts, h->bcount, h->gmark[0],
                     h->gmark[1], h->cursor, h->work,
                     h->nwork2, h->tile_sums, h->tile_list, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
                     h->d_col, h->d_tmaps, h->rgba, h->zid, h->img,
@@ -1023,6 +1124,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
         {(void**)&h->keys[0], n * 4, true},
         {(void**)&h->keys[1], n * 4, true},
         {(void**)&h->perm, n * 4, true},
+        {(void**)&h->slot_of, n * 4, true},
         {(void**)&h->counts, (size_t)h->nkeys * 4, true},
         {(void**)&h->bcount, (size_t)h->nblocks * 4, true},
         {(void**)&h->gmark[0], (size_t)h->nblocks, true},
@@ -2136,6 +2238,13 @@ rd_status rd_launch_count(rd_handle* h, uint64_t* count) {
 rd_status rd_graph_replays(rd_handle* h, uint64_t* count) {
     if (!h || !count) return RD_INVALID_ARG;
     *count = h->graph_replays;
+    return RD_OK;
+}
+
+rd_status rd_io_bytes(rd_handle* h, uint64_t* in_place, uint64_t* staged) {
+    if (!h || !in_place || !staged) return RD_INVALID_ARG;
+    *in_place = h->io_direct;
+    *staged = h->io_staged;
     return RD_OK;
 }
 

@@ -175,25 +175,41 @@ def test_batch_rejects_single_scene_calls_and_unset_scenes(built_pkg):
     assert b.flags() == 0
 
 
-def test_mapped_pinned_host_buffers_match_staged_copies(built_pkg):
-    """rd_set_particles / rd_get_particles on pinned host buffers passed as
-    device-accessible pointers (the pack and unpack kernels read and write host
-    memory directly) give the same state as the staged copies."""
+def test_pinned_host_buffers_are_used_in_place_and_match_staged_copies(built_pkg):
+    """rd_set_particles / rd_get_particles with pageable host arrays (copied
+    through the device staging buffer), with page-locked ones under RD_HOST
+    (read and written in place by the pack and unpack kernels) and with
+    page-locked ones passed as device-accessible pointers (RD_DEVICE) give
+    the same state; rd_io_bytes tells the first two routes apart."""
     import torch
     from rd_gb300 import scenes
     sc = scenes.snowball(seed=12, n=4000, grid=32)
-    pinned = {k: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
-              for k, a in (("x", sc.x), ("v", sc.v), ("mass", sc.mass))}
+    src = {"x": sc.x, "v": sc.v, "mass": sc.mass}
+    shapes = {"x": (sc.n, 3), "v": (sc.n, 3), "FE": (sc.n, 9)}
+    state_bytes = sum(a.size * 4 for a in src.values())
+    out_bytes = sum(int(np.prod(s)) * 4 for s in shapes.values())
     out = []
-    for mapped in (False, True):
+    for route in ("pageable", "pinned", "mapped"):
+        pin = route != "pageable"
+        arr = {k: (torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy() if pin else np.array(a))
+               for k, a in src.items()}
+        res = {k: (torch.empty(s, dtype=torch.float32).pin_memory().numpy() if pin else np.empty(s, np.float32))
+               for k, s in shapes.items()}
         s = built_pkg.Simulation(scene_params(built_pkg, sc))
-        s.set_particles(pinned["x"], pinned["v"], pinned["mass"], mapped=mapped)
+        s.set_particles(arr["x"], arr["v"], arr["mass"], mapped=route == "mapped")
         s.init_volumes()
         s.step(sc.dt, 3)
-        res = {k: torch.empty(shape, dtype=torch.float32).pin_memory().numpy()
-               for k, shape in (("x", (sc.n, 3)), ("v", (sc.n, 3)), ("FE", (sc.n, 9)))}
-        s.get_particles(("x", "v", "FE"), out=res, mapped=mapped)
+        s.get_particles(("x", "v", "FE"), out=res, mapped=route == "mapped")
         s.synchronize()
+        in_place, staged = s.io_bytes()
+        if route == "pageable":
+            assert (in_place, staged) == (0, state_bytes + out_bytes)
+        elif route == "pinned":
+            assert (in_place, staged) == (state_bytes + out_bytes, 0)
+        else:  # RD_DEVICE: not host I/O
+            assert (in_place, staged) == (0, 0)
         out.append({k: a.copy() for k, a in res.items()})
-    for k in ("x", "v", "FE"):
-        assert rel(out[1][k], out[0][k]) < 1e-6, k
+        assert s.flags() == 0
+    for o in out[1:]:
+        for k in shapes:
+            assert rel(o[k], out[0][k]) < 1e-6, k
