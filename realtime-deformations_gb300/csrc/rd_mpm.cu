@@ -62,17 +62,22 @@ __device__ __forceinline__ void store_rows(T* __restrict__ dst, int r0, int cnt,
 
 // Particles off .. off + n - 1 of planes holding ntot particles (one scene of
 // a batch, or all of a single scene), from structure-of-arrays input in
-// particle id order; particle i goes to slot off + i.
+// particle id order; particle i goes to slot off + i.  With keys (a single
+// scene, P its parameters) it also writes the first sort's keys and
+// histogram, as k_keys would: the loads from host memory bound this kernel,
+// so the keys cost nothing here.
 template <typename T>
 __global__ void __launch_bounds__(kIoThreads)
     k_pack(int n, int off, int ntot, const T* __restrict__ x, const T* __restrict__ v, const T* __restrict__ B,
            const T* __restrict__ FE, const T* __restrict__ FP, const T* __restrict__ Jp, const T* __restrict__ mass,
-           const T* __restrict__ vol, vec4<T>* __restrict__ pl, int track_fp) {
+           const T* __restrict__ vol, vec4<T>* __restrict__ pl, int track_fp, DevParams<T> P,
+           uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, uint32_t* __restrict__ bcount,
+           uint32_t* __restrict__ flags) {
     __shared__ T sh[9 * kIoThreads];
     const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
     const int cnt = min((int)blockDim.x, n - r0);
     Particle<T> p;
-    T P[9], t3[3];
+    T FPm[9], t3[3];
     load_rows(x, r0, cnt, t3, sh);
 #pragma unroll
     for (int a = 0; a < 3; ++a) p.x[a] = t3[a];
@@ -92,18 +97,25 @@ __global__ void __launch_bounds__(kIoThreads)
         for (int e = 0; e < 9; ++e) p.F[e] = (e % 4 == 0) ? T(1) : T(0);
     }
     if (FP) {
-        load_rows(FP, r0, cnt, P, sh);
+        load_rows(FP, r0, cnt, FPm, sh);
     } else {
 #pragma unroll
-        for (int e = 0; e < 9; ++e) P[e] = (e % 4 == 0) ? T(1) : T(0);
+        for (int e = 0; e < 9; ++e) FPm[e] = (e % 4 == 0) ? T(1) : T(0);
     }
     if (i >= n) return;
     p.m = mass[i];
     p.vol = vol ? vol[i] : T(0);
-    p.Jp = Jp ? Jp[i] : (FP ? det3(P) : T(1));
+    p.Jp = Jp ? Jp[i] : (FP ? det3(FPm) : T(1));
     p.id = (uint32_t)(off + i);
     store_particle(pl, (size_t)ntot, (size_t)(off + i), p);
-    if (track_fp) store_fp(pl, (size_t)ntot, (size_t)(off + i), P);
+    if (track_fp) store_fp(pl, (size_t)ntot, (size_t)(off + i), FPm);
+    if (keys) {
+        const int b[3] = {base_of(p.x[0], P.h), base_of(p.x[1], P.h), base_of(p.x[2], P.h)};
+        if (!stencil_in_grid(P, b)) raise_flag(flags, 1u);
+        const uint32_t key = sort_key(P, b);
+        keys[off + i] = key;
+        count_key(counts, bcount, key);
+    }
 }
 
 // The slot of each particle of a scene (particles off .. off + n - 1 in
@@ -773,15 +785,21 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, cons
             if (where == RD_HOST) h->io_direct += cnt[k] * sizeof(T);
         }
     }
+    // a single scene's first sort reads its keys and histogram from the pack
+    const bool keys = !batched(h) && n > 0;
+    if (keys) {
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->counts, 0, sizeof(uint32_t) * h->nkeys, h->stream), "memset counts"));
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->bcount, 0, sizeof(uint32_t) * h->nblocks, h->stream), "memset counts"));
+    }
     if (n > 0) {
-        k_pack<T><<<blocks_for(n, kIoThreads), kIoThreads, 0, h->stream>>>((int)n, (int)sc.poff, h->n, ptr[0], ptr[1],
-                                                                           ptr[2], ptr[3],
-                                                             ptr[4], ptr[5], ptr[6], ptr[7],
-                                                             static_cast<vec4<T>*>(h->pl[h->cur]), h->prm.track_fp);
+        k_pack<T><<<blocks_for(n, kIoThreads), kIoThreads, 0, h->stream>>>(
+            (int)n, (int)sc.poff, h->n, ptr[0], ptr[1], ptr[2], ptr[3], ptr[4], ptr[5], ptr[6], ptr[7],
+            static_cast<vec4<T>*>(h->pl[h->cur]), h->prm.track_fp, make_params<T>(h, 0.0, T(0)),
+            keys ? h->keys[h->cur] : nullptr, h->counts, h->bcount, h->flags);
         RD_TRY(launched(h, "k_pack"));
     }
     sc.set = true;
-    h->keys_valid = false;
+    h->keys_valid = keys;
     h->sorted = false;
     h->fgrid_valid = false;
     h->grid_mode = GRID_NONE;
