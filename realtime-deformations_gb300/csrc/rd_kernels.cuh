@@ -881,13 +881,19 @@ __device__ __forceinline__ void sort_ranked(P2GTile<T, CA>& S, int j, int cell, 
     __syncthreads();
 }
 
+// Sorted slots holding a record after sort_records / sort_ranked (records of
+// cell 0xff are not placed).
+template <typename T, int CA> __device__ __forceinline__ int sorted_total(const P2GTile<T, CA>& S) {
+    return S.off[P2GTile<T, CA>::NC - 1] + S.cnt[P2GTile<T, CA>::NC - 1];
+}
+
+// total: the slots 0 .. total - 1 of S.order / S.scell hold the records, the
+// records of one cell contiguous.
 template <typename T, bool MOM, int CA>
-__device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int count) {
+__device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int ox = lane >> 3, oy = (lane >> 1) & 3, oz0 = lane & 1;
     const T fx = (T)ox, fy = (T)oy, fz = (T)oz0;
-    // sorted slots holding a record: the records of cells 0xff were skipped
-    const int total = S.off[P2GTile<T, CA>::NC - 1] + S.cnt[P2GTile<T, CA>::NC - 1];
     const int k0 = (int)(((long long)total * warp) / nwarps), k1 = (int)(((long long)total * (warp + 1)) / nwarps);
     const T* recs = reinterpret_cast<const T*>(S.rec);
     int cur = -1;
@@ -934,7 +940,7 @@ __device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int count) {
         T am[2] = {T(0), T(0)}, aq[2][3] = {{T(0), T(0), T(0)}, {T(0), T(0), T(0)}};
         for (int k = k0; k < k1; ++k) {
             const int j = S.order[k];
-            const int c = S.cellof[j];
+            const int c = S.scell[k];
             if (c != cur) {
                 if (cur >= 0) p2g_flush_lane<T, CA>(S, cur, ox, oy, oz0, am, aq, MOM);
                 cur = c;
@@ -1010,6 +1016,7 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
     tile_origin(P, it.x, org);
     const int count = min(it.z, min(WorkP<T>::value, P.n - it.y));
     __syncthreads();
+    bool stray = false;  // a record outside the cell space
     // phase 1: a record per particle
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         Particle<T> p;
@@ -1022,6 +1029,7 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
         if (!make_stencil(P, p.x, org, St)) {
             raise_flag(D.flags, 4u);
             S.cellof[j] = 0xff;
+            stray = true;
             continue;
         }
         if (!stencil_in_grid(P, St.b)) raise_flag(D.flags, 1u);
@@ -1045,10 +1053,20 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
         write_record<T, MOM>(&S.rec[j * kRecV4], St, p.x, A, mv, p.m, P.h);
         const int cell = (St.rel[0] * kBlk + St.rel[1]) * kBlk + St.rel[2];
         S.cellof[j] = (uint8_t)cell;
-        atomicAdd(&S.cnt[cell], 1);
+        S.order[j] = (uint16_t)j;
+        S.scell[j] = (uint8_t)cell;
     }
-    sort_records<T, kBlk>(S, count);
-    p2g_tasks<T, MOM, kBlk>(S, count);
+    // The item is a run of the global sort by cell key and nothing has moved
+    // since, so its records are grouped by cell already, in item order; only
+    // a particle outside the cell space (flagged above) needs the record sort.
+    int total = count;
+    if (__syncthreads_or(stray)) {
+        for (int j = threadIdx.x; j < count; j += blockDim.x)
+            if (S.cellof[j] != 0xff) atomicAdd(&S.cnt[S.cellof[j]], 1);
+        sort_records<T, kBlk>(S, count);
+        total = sorted_total(S);
+    }
+    p2g_tasks<T, MOM, kBlk>(S, total);
     __syncthreads();
     p2g_flush<T, kBlk>(P, S, org, grid);
     if (MOM) mark_around(P, D.gmark, it.x);
@@ -1318,7 +1336,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             }
         }
         sort_ranked<T, CA>(S.p, j, rcell, rrank);
-        p2g_tasks<T, true, CA>(S.p, count);
+        p2g_tasks<T, true, CA>(S.p, sorted_total(S.p));
         __syncthreads();
         p2g_flush<T, CA>(P, S.p, porg, gnext);
         mark_around(P, D.gmark_next, it.x);

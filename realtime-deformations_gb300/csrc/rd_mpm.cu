@@ -2344,7 +2344,7 @@ __global__ void __launch_bounds__(kThreads) k_na_p2g(DevParams<float> P, const f
             atomicAdd(&S.cnt[cell], 1);
         }
         sort_records<float, kBlk>(S, count);
-        p2g_tasks<float, true, kBlk>(S, count);
+        p2g_tasks<float, true, kBlk>(S, sorted_total(S));
         __syncthreads();
         p2g_flush<float, kBlk>(P, S, org, grid);
         __syncthreads();
