@@ -1073,6 +1073,11 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
     __syncthreads();
 }
 
+// k_p2g runs one particle per thread, three CTAs per SM in FP32: a work
+// item's particle loads (through the sort permutation, scattered when the
+// state was just uploaded) are all in flight at once.
+template <typename T> constexpr int kP2GThreads = WorkP<T>::value;
+
 template <typename T> struct P2GShared {
     P2GTile<T, kBlk> t;
     DevParams<T> par;  // the item's scene (batches)
@@ -1081,7 +1086,7 @@ template <typename T> struct P2GShared {
 // BATCH: the work items belong to different scenes (D.scenes); otherwise all
 // to the scene P0.
 template <typename T, bool MOM, bool FORCE, bool BATCH>
-__global__ void __launch_bounds__(kThreads) k_p2g(DevParams<T> P0, DevBufs D) {
+__global__ void __launch_bounds__(kP2GThreads<T>, sizeof(T) == 4 ? 3 : 1) k_p2g(DevParams<T> P0, DevBufs D) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
     P2GShared<T>& S = *reinterpret_cast<P2GShared<T>*>(smem_raw);
     const uint32_t nw = min(*D.nwork, D.work_cap);

@@ -626,9 +626,9 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
         t = tmark_begin(h, RD_KERNEL_P2G);
         const unsigned pg = persistent_grid<T>(h, h->occ_p2g);
         if (batch)
-            k_p2g<T, true, true, true><<<pg, kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+            k_p2g<T, true, true, true><<<pg, kP2GThreads<T>, sizeof(P2GShared<T>), h->stream>>>(P, D);
         else
-            k_p2g<T, true, true, false><<<pg, kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+            k_p2g<T, true, true, false><<<pg, kP2GThreads<T>, sizeof(P2GShared<T>), h->stream>>>(P, D);
         tmark_end(h, t);
         RD_TRY(launched(h, "k_p2g"));
         if (reorder) h->cur ^= 1;  // the ordered copy is the state now; perm is the identity
@@ -666,7 +666,7 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
             RD_TRY(check_cuda(h, cudaMemsetAsync(h->gforce, 0, nc * sizeof(vec4<T>), h->stream), "memset force"));
             if (h->n > 0) {
                 DevBufs D = bufs<T>(h);
-                k_p2g<T, true, false, false><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+                k_p2g<T, true, false, false><<<persistent_grid<T>(h, h->occ_p2g), kP2GThreads<T>, sizeof(P2GShared<T>), h->stream>>>(P, D);
                 RD_TRY(launched(h, "k_p2g<rasterize>"));
             }
             k_grid_normalize<T><<<cb, 256, 0, h->stream>>>(static_cast<vec4<T>*>(h->grid[h->g]), nc);
@@ -679,7 +679,7 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
             if (!h->sorted) RD_TRY(sort_particles<T>(h));
             if (h->n > 0) {
                 DevBufs D = bufs<T>(h);
-                k_p2g<T, false, true, false><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+                k_p2g<T, false, true, false><<<persistent_grid<T>(h, h->occ_p2g), kP2GThreads<T>, sizeof(P2GShared<T>), h->stream>>>(P, D);
                 RD_TRY(launched(h, "k_p2g<forces>"));
             }
             return RD_OK;
@@ -921,7 +921,7 @@ template <typename T> rd_status init_volumes_impl(rd_handle* h) {
     RD_TRY(clear_grid<T>(h, h->g));
     const DevParams<T> P = make_params<T>(h, 0.0, T(1));
     const DevBufs D = bufs<T>(h);
-    k_p2g<T, true, false, true><<<persistent_grid<T>(h, h->occ_p2g), kThreads, sizeof(P2GShared<T>), h->stream>>>(P, D);
+    k_p2g<T, true, false, true><<<persistent_grid<T>(h, h->occ_p2g), kP2GThreads<T>, sizeof(P2GShared<T>), h->stream>>>(P, D);
     RD_TRY(launched(h, "k_p2g<rasterize>"));
     k_volumes<T, true><<<blocks_for(h->n, 256), 256, 0, h->stream>>>(P, D, static_cast<vec4<T>*>(h->pl[h->cur]),
                                                                       static_cast<const vec4<T>*>(h->grid[h->g]));
@@ -938,7 +938,7 @@ template <typename T> rd_status occupancy(rd_handle* h) {
                          (const void*)k_p2g<T, true, false, true>};
     for (const void* f : p2g)
         RD_TRY(check_cuda(h, cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sm), "smem attr"));
-    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true, false>, kThreads, sm), "occ"));
+    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true, false>, kP2GThreads<T>, sm), "occ"));
     h->occ_p2g = std::max(1, o);
     const int fsm = (int)fused_smem_bytes<T>();
     const void* used = (const void*)fused_kernel<T>(h);
