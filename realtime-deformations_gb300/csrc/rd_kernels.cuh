@@ -1,6 +1,7 @@
 // sm_103a kernels of the MPM step.  One step of rd_step is
-//   k_keys (only when positions changed outside a step) -> k_scan -> k_scatter
-//   -> memset(next grid) -> k_g2p2g (k_p2g first when the grid must be rebuilt)
+//   k_keys (only when positions changed outside a step and the upload did not
+//   count them) -> k_tile_sums -> k_tile_prefix -> k_scan -> k_scatter
+//   -> k_grid_clear -> k_g2p2g (k_p2g first when the grid must be rebuilt)
 // and the stage kernels serve rd_stage, which runs the reference's seven
 // stages one by one (material_point_method.cpp:94-350).
 #pragma once
