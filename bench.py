@@ -11,7 +11,9 @@ The metric is particle-steps per second.  Prints one JSON line (rank 0).
 * ours (default): the CUDA path through the C ABI.  ``value`` is timed with
   CUDA events on the handle's stream with the particle state resident in HBM;
   ``e2e`` times the same steps through the C ABI with the whole particle state
-  copied in from pinned host memory and back out every step; ``roofline``
+  moved in from page-locked host memory and back out every step (the pack and
+  unpack kernels read and write it in place; pageable arrays, copied through
+  a staging buffer, are reported beside it); ``roofline``
   comes from a second pass of the same steps with per-kernel CUDA events.
   Multi-GPU (torchrun): one independent replica per GPU (the step has no
   exchange between scenes), barrier-bracketed, max over ranks.
