@@ -142,9 +142,20 @@ public:
         p.track_fp = 1;
         h_ = p.h;
         check(rd_create(&p, &sim_), "rd_create");
-        host_.resize(static_cast<size_t>(n_) * 36);
+        // page-locked, so rd_set_particles / rd_get_particles move it in place
+        void* buf = nullptr;
+        const rd_status s = rd_host_alloc(static_cast<size_t>(n_) * 36 * sizeof(float), &buf);
+        if (s != RD_OK) {
+            rd_destroy(sim_);
+            sim_ = nullptr;
+            throw rd::Error(s, "rd_host_alloc: page-locked exchange arrays");
+        }
+        host_ = static_cast<float*>(buf);
     }
-    ~LagrangeEulerView() { if (sim_) rd_destroy(sim_); }
+    ~LagrangeEulerView() {
+        if (sim_) rd_destroy(sim_);
+        rd_host_free(host_);
+    }
     LagrangeEulerView(const LagrangeEulerView&) = delete;
     LagrangeEulerView& operator=(const LagrangeEulerView&) = delete;
 
@@ -220,7 +231,7 @@ private:
     // host_ holds the SoA exchange arrays: x 3n | v 3n | B 9n | FE 9n | FP 9n | mass n | vol n | Jp n
     float* soa(int k) {
         static const size_t off[] = {0, 3, 6, 15, 24, 33, 34, 35};
-        return host_.data() + off[k] * static_cast<size_t>(n_);
+        return host_ + off[k] * static_cast<size_t>(n_);
     }
     rd_particles views() {
         rd_particles v;
@@ -268,7 +279,7 @@ private:
     float h_ = 0.05f;
     rd_handle* sim_ = nullptr;
     std::vector<Particle> particles_;
-    std::vector<float> host_;
+    float* host_ = nullptr;  // page-locked (rd_host_alloc), 36 n floats
     std::vector<rd_collider> colliders_;
     bool dirty_host_ = false;
 };

@@ -231,6 +231,14 @@ rd_status rd_graph_replays(rd_handle* h, uint64_t* count);
  * RD_HOST so far: read or written in place in page-locked host memory, and
  * through the device staging buffer. */
 rd_status rd_io_bytes(rd_handle* h, uint64_t* in_place, uint64_t* staged);
+/* Page-locked host memory (cudaHostAlloc) for the particle arrays of
+ * rd_set_particles / rd_get_particles, which the pack and unpack kernels then
+ * read and write in place: the host side of the reference's particle buffer
+ * (material_point_method.hpp:181-183) for callers without CUDA headers.
+ * bytes = 0 gives NULL.  RD_OOM when the allocation fails. */
+rd_status rd_host_alloc(size_t bytes, void** out);
+/* Releases memory from rd_host_alloc (NULL: nothing). */
+rd_status rd_host_free(void* p);
 
 /* initializeParticles (material_point_method.cpp:18-63) on the device: the cells
  * within radius / h of the origin, 8 points per cell at quarter offsets, each

@@ -45,7 +45,7 @@ STAGES = {"rasterize": 0, "forces": 1, "grid_velocities": 2, "collisions": 3,
 EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "rd_get_particles",
            "rd_init_volumes", "rd_step", "rd_stage", "rd_get_grid", "rd_device_xyzs", "rd_get_flags",
            "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort", "rd_debug_wait_timeout",
-           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_graph_replays", "rd_io_bytes", "rd_batch_create",
+           "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_graph_replays", "rd_io_bytes", "rd_host_alloc", "rd_host_free", "rd_batch_create",
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
            "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
@@ -196,6 +196,8 @@ def lib():
             L.rd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
             L.rd_graph_replays.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
             L.rd_io_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+            L.rd_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]
+            L.rd_host_free.argtypes = [vp]
             L.rd_rasterize_noalloc.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(_Particles), vp, vp]
             L.rd_batch_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int32, ctypes.POINTER(vp)]
             L.rd_batch_num_scenes.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]

@@ -2266,6 +2266,26 @@ rd_status rd_io_bytes(rd_handle* h, uint64_t* in_place, uint64_t* staged) {
     return RD_OK;
 }
 
+rd_status rd_host_alloc(size_t bytes, void** out) {
+    if (!out) return RD_INVALID_ARG;
+    *out = nullptr;
+    if (bytes == 0) return RD_OK;
+    if (cudaHostAlloc(out, bytes, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return RD_OOM;
+    }
+    return RD_OK;
+}
+
+rd_status rd_host_free(void* p) {
+    if (p && cudaFreeHost(p) != cudaSuccess) {
+        cudaGetLastError();
+        return RD_CUDA_ERROR;
+    }
+    return RD_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------

@@ -55,5 +55,8 @@ int main(int argc, char** argv) {
         std::fwrite(rec, sizeof(float), 34, f);
     }
     std::fclose(f);
+    // the drop-in's exchange arrays are page-locked: no byte went through staging
+    uint64_t in_place = 0, staged = 0;
+    if (rd_io_bytes(MPM.handle(), &in_place, &staged) != RD_OK || staged != 0 || in_place == 0) return 4;
     return 0;
 }
