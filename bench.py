@@ -47,12 +47,13 @@ import __graft_entry__ as graft  # noqa: E402
 STEP_BYTES_PER_PARTICLE = 208
 STEP_BYTES_PER_CELL = 44
 # Per kernel (FP32, what each kernel must move per particle / per active cell):
-#   k_p2g (first step only) reads x, m, v, V, B, F_E, J_P (108 B) and adds
-#     (m, p) into its cells (16 B);
+#   k_p2g (first step only) reads x, m, v, V, B, F_E, J_P (108 B), writes the
+#     particle to its sorted slot for the fused kernel (108 B and its id, 4 B)
+#     and adds (m, p) into its cells (16 B);
 #   k_g2p2g reads x, m, V, B, F_E, J_P (96 B), writes the particle at its sorted
 #     slot (x, m, v, V, B, F_E, J_P: 108 B) and its next block key (4 B); it
 #     reads this step's cell (m, p) (16 B) and adds the next step's (16 B).
-KERNEL_BYTES = {"p2g": (108, 16), "g2p2g": (96 + 108 + 4, 32)}
+KERNEL_BYTES = {"p2g": (108 + 112, 16), "g2p2g": (96 + 108 + 4, 32)}
 
 
 def parse_args():
