@@ -22,6 +22,16 @@ def test_header_declares_exactly_the_exports(pkg):
     assert declared_functions() == set(pkg.EXPORTS)
 
 
+def test_missing_library_fails_loudly(pkg, monkeypatch):
+    """No CPU fallback: without the built CUDA library every call raises."""
+    monkeypatch.setattr(pkg, "_LIB", None)
+    monkeypatch.setattr(pkg, "LIB_PATH", os.path.join(REPO, "no_such_dir", "librd_mpm.so"))
+    with pytest.raises(RuntimeError, match="not built"):
+        pkg.lib()
+    with pytest.raises(RuntimeError, match="not built"):
+        pkg.Simulation(pkg.make_params(16, 16, 16, 8, 1.0 / 16))
+
+
 def test_library_loads_and_exports_every_declared_symbol(built_pkg):
     L = built_pkg.lib()
     for name in declared_functions():
