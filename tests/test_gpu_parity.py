@@ -460,3 +460,47 @@ def test_large_host_transfers_round_trip(built_pkg):
     for k in fields:
         assert np.array_equal(chunked[k], pinned[k]), k
     assert sim.flags() == 0
+
+
+# ----------------------------------------------------------------- full size
+def test_full_size_two_ball_workload_properties(built_pkg):
+    """The benchmark's 1.1M-particle two-ball workload (128^3) at full size,
+    10 fused steps, checked through properties that hold at any size: every
+    particle comes back with its own mass; total grid mass equals particle
+    mass; linear momentum changes by the gravity impulse only (the MLS force
+    and the APIC affine term sum to zero over each particle's stencil, and no
+    particle is near a wall yet), within FP32 rounding; the block keys of the
+    final positions equal a CPU computation bit for bit and the sort is a
+    permutation in key order; no status flag."""
+    from rd_gb300 import scenes
+    sc = scenes.two_balls_1m()
+    steps = 10
+    sim = make_sim(built_pkg, sc.grid, sc.n, sc.h, **sc.params())
+    sim.set_particles(sc.x, sc.v, sc.mass)
+    sim.init_volumes()
+    sim.step(sc.dt, steps)
+    out = sim.get_particles(("x", "v", "FE", "Jp", "mass"))
+    assert sim.flags() == 0
+    assert np.array_equal(out["mass"], sc.mass)
+    for k in ("x", "v", "FE", "Jp"):
+        assert np.all(np.isfinite(out[k])), k
+    m = sc.mass.astype(np.float64)
+    total = float(m.sum())
+    gm = sim.get_grid()["mass"]
+    assert abs(float(np.sum(gm, dtype=np.float64)) - total) / total < 1e-6
+    v = out["v"].astype(np.float64)
+    p0 = (m[:, None] * sc.v.astype(np.float64)).sum(0)
+    p = (m[:, None] * v).sum(0)
+    want = p0 + total * steps * sc.dt * np.array([0.0, -9.8, 0.0])
+    scale = float((m * np.linalg.norm(v, axis=1)).sum())
+    assert np.abs(p - want).max() < 1e-5 * scale, (p, want)
+    keys, order = sim.debug_sort()
+    h = np.float32(sc.h)
+    nb = (np.array(sc.grid) + 3) // 4
+    base = (out["x"] / h).astype(np.int32)
+    blk = ((base[:, 0] // 4) * nb[1] + base[:, 1] // 4) * nb[2] + base[:, 2] // 4
+    cell = ((base[:, 0] % 4) * 4 + base[:, 1] % 4) * 4 + base[:, 2] % 4
+    cpu = (blk * 64 + cell).astype(np.int64)
+    assert np.array_equal(keys, cpu.astype(np.uint32))
+    assert np.array_equal(np.sort(order), np.arange(sc.n))
+    assert np.all(np.diff(keys[order].astype(np.int64)) >= 0)
