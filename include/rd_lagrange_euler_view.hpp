@@ -22,11 +22,13 @@
 // small stand-ins with the same member access (x/y/z, m[col][row]) are used.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "rd_mpm.h"
@@ -126,6 +128,77 @@ inline int reference_initial_particles(float h, const rd_facade::vec3& origin, c
                 }
     return need_more;
 }
+
+namespace detail {
+// f(begin, end) over [0, n): in one call for small n, else split over the
+// host's cores (at least 32,768 particles a thread).
+template <typename F>
+inline void parallel_ranges(int n, F&& f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nt = static_cast<int>(std::min<unsigned>(hw, static_cast<unsigned>(std::max(1, n / 32768))));
+    if (nt <= 1) {
+        f(0, n);
+        return;
+    }
+    const int per = (n + nt - 1) / nt;
+    std::vector<std::thread> pool;
+    pool.reserve(nt - 1);
+    for (int k = 1; k < nt; ++k) {
+        const int b = k * per, e = std::min(n, b + per);
+        if (b < e) pool.emplace_back([&f, b, e] { f(b, e); });
+    }
+    f(0, std::min(n, per));
+    for (auto& t : pool) t.join();
+}
+
+// The exchange arrays of rd_set_particles / rd_get_particles, structure of
+// arrays of n particles: x 3n | v 3n | B 9n | FE 9n | FP 9n | mass n | vol n
+// (| Jp n, filled by the library); matrices row-major, glm's m[col][row].
+inline size_t soa_offset(int k, int n) {
+    static const size_t off[] = {0, 3, 6, 15, 24, 33, 34, 35};
+    return off[k] * static_cast<size_t>(n);
+}
+
+inline void particles_to_soa(const Particle* ps, int n, float* soa) {
+    parallel_ranges(n, [=](int b, int e) {
+        float *x = soa + soa_offset(0, n), *v = soa + soa_offset(1, n), *B = soa + soa_offset(2, n),
+              *FE = soa + soa_offset(3, n), *FP = soa + soa_offset(4, n), *m = soa + soa_offset(5, n),
+              *vol = soa + soa_offset(6, n);
+        for (int i = b; i < e; ++i) {
+            const Particle& p = ps[i];
+            for (int a = 0; a < 3; ++a) { x[3 * i + a] = p.pos[a]; v[3 * i + a] = p.velocity[a]; }
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) {
+                    B[9 * i + 3 * r + c] = p.B[c][r];
+                    FE[9 * i + 3 * r + c] = p.FElastic[c][r];
+                    FP[9 * i + 3 * r + c] = p.FPlastic[c][r];
+                }
+            m[i] = p.mass;
+            vol[i] = p.volume;
+        }
+    });
+}
+
+inline void soa_to_particles(const float* soa, int n, Particle* ps) {
+    parallel_ranges(n, [=](int b, int e) {
+        const float *x = soa + soa_offset(0, n), *v = soa + soa_offset(1, n), *B = soa + soa_offset(2, n),
+                    *FE = soa + soa_offset(3, n), *FP = soa + soa_offset(4, n), *m = soa + soa_offset(5, n),
+                    *vol = soa + soa_offset(6, n);
+        for (int i = b; i < e; ++i) {
+            Particle& p = ps[i];
+            for (int a = 0; a < 3; ++a) { p.pos[a] = x[3 * i + a]; p.velocity[a] = v[3 * i + a]; }
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) {
+                    p.B[c][r] = B[9 * i + 3 * r + c];
+                    p.FElastic[c][r] = FE[9 * i + 3 * r + c];
+                    p.FPlastic[c][r] = FP[9 * i + 3 * r + c];
+                }
+            p.mass = m[i];
+            p.volume = vol[i];
+        }
+    });
+}
+}  // namespace detail
 
 class LagrangeEulerView {
 public:
@@ -228,11 +301,8 @@ private:
         check(rd_stage(sim_, id, dt), "rd_stage");
         dirty_host_ = true;
     }
-    // host_ holds the SoA exchange arrays: x 3n | v 3n | B 9n | FE 9n | FP 9n | mass n | vol n | Jp n
-    float* soa(int k) {
-        static const size_t off[] = {0, 3, 6, 15, 24, 33, 34, 35};
-        return host_ + off[k] * static_cast<size_t>(n_);
-    }
+    // host_ holds the exchange arrays (detail::soa_offset)
+    float* soa(int k) { return host_ + detail::soa_offset(k, n_); }
     rd_particles views() {
         rd_particles v;
         v.x = soa(0); v.v = soa(1); v.B = soa(2); v.FE = soa(3); v.FP = soa(4); v.mass = soa(5);
@@ -240,18 +310,7 @@ private:
         return v;
     }
     void upload() {
-        for (int i = 0; i < n_; ++i) {
-            const Particle& p = particles_[i];
-            for (int a = 0; a < 3; ++a) { soa(0)[3 * i + a] = p.pos[a]; soa(1)[3 * i + a] = p.velocity[a]; }
-            for (int r = 0; r < 3; ++r)
-                for (int c = 0; c < 3; ++c) {
-                    soa(2)[9 * i + 3 * r + c] = p.B[c][r];
-                    soa(3)[9 * i + 3 * r + c] = p.FElastic[c][r];
-                    soa(4)[9 * i + 3 * r + c] = p.FPlastic[c][r];
-                }
-            soa(5)[i] = p.mass;
-            soa(6)[i] = p.volume;
-        }
+        detail::particles_to_soa(particles_.data(), n_, host_);
         rd_particles v = views();
         v.Jp = nullptr;  // det F_P from FP
         check(rd_set_particles(sim_, &v, RD_HOST), "rd_set_particles");
@@ -260,18 +319,7 @@ private:
     void download() {
         rd_particles v = views();
         check(rd_get_particles(sim_, &v, RD_HOST), "rd_get_particles");
-        for (int i = 0; i < n_; ++i) {
-            Particle& p = particles_[i];
-            for (int a = 0; a < 3; ++a) { p.pos[a] = soa(0)[3 * i + a]; p.velocity[a] = soa(1)[3 * i + a]; }
-            for (int r = 0; r < 3; ++r)
-                for (int c = 0; c < 3; ++c) {
-                    p.B[c][r] = soa(2)[9 * i + 3 * r + c];
-                    p.FElastic[c][r] = soa(3)[9 * i + 3 * r + c];
-                    p.FPlastic[c][r] = soa(4)[9 * i + 3 * r + c];
-                }
-            p.mass = soa(5)[i];
-            p.volume = soa(6)[i];
-        }
+        detail::soa_to_particles(host_, n_, particles_.data());
         dirty_host_ = false;
     }
 

@@ -26,12 +26,22 @@ def test_reference_initialiser_is_bit_exact(tmp_path):
     assert np.array_equal(rec[:, 3], g["m0"])
 
 
+def test_exchange_arrays_round_trip_bit_exact_on_host_threads(tmp_path):
+    """Particle <-> exchange arrays of the drop-in, split over host threads for
+    large counts, against a plain one-thread conversion (no GPU needed)."""
+    exe = tmp_path / "facade_exchange"
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-pthread", "-I", INC,
+                           os.path.join(CPP, "facade_exchange.cpp"), "-o", str(exe)])
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["stages", "fused"])
 def test_cpp_driver_matches_reference_scene(built_pkg, tmp_path, mode):
     exe = tmp_path / "drive"
     libdir = os.path.dirname(built_pkg.LIB_PATH)
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", INC, os.path.join(CPP, "main_reference_scene.cpp"),
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-pthread", "-I", INC, os.path.join(CPP, "main_reference_scene.cpp"),
                            "-L", libdir, "-l:librd_mpm.so", f"-Wl,-rpath,{libdir}", "-o", str(exe)])
     out = tmp_path / "state.bin"
     subprocess.check_call([str(exe), str(out), mode])
