@@ -66,6 +66,18 @@ int main(void) {
     return dict((k, int(v)) for k, v in (line.split() for line in out.strip().splitlines()))
 
 
+def test_c_example_compiles_and_links_as_c99(built_pkg, tmp_path):
+    """The integration guide's C example (tests/cpp/abi_example.c) builds
+    against the header alone, as C99 with warnings as errors, and links
+    against the library."""
+    exe = tmp_path / "abi_example"
+    libdir = os.path.dirname(built_pkg.LIB_PATH)
+    subprocess.check_call(["gcc", "-std=c99", "-O2", "-Wall", "-Wextra", "-Werror", "-I",
+                           os.path.join(REPO, "include"), os.path.join(REPO, "tests", "cpp", "abi_example.c"),
+                           "-L", libdir, "-l:librd_mpm.so", f"-Wl,-rpath,{libdir}", "-o", str(exe)])
+    assert exe.exists()
+
+
 def test_ctypes_structs_match_c_layout(pkg, tmp_path):
     c = _c_layout(tmp_path)
     assert c["rd_params"] == ctypes.sizeof(pkg.Params)
