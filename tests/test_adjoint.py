@@ -69,6 +69,25 @@ def test_gradients_match_central_differences_fp64(built_pkg):
         assert rel_err(fd, ad) < FD_TOL, (name, fd, ad)
 
 
+def test_gradients_from_identity_elastic_F_match_central_differences_fp64(built_pkg):
+    """Every scene starts with F_E = I: all three singular values tie at 1
+    in the first steps, where the split's backward takes its tie branch."""
+    sc = plastic_scene(seed=7)
+    sc["FE"] = np.tile(np.eye(3).reshape(1, 9), (len(sc["m"]), 1))
+    L0, g = run(built_pkg, sc, sc["v"])
+    for k in range(2):
+        e = sc["rng"].normal(size=sc["v"].shape)
+        eps = 1e-6
+        fd = (run(built_pkg, sc, sc["v"] + eps * e, grads=False)[0] - run(built_pkg, sc, sc["v"] - eps * e, grads=False)[0]) / (2 * eps)
+        ad = float(np.sum(g["v0"] * e))
+        assert rel_err(fd, ad) < FD_TOL, (k, fd, ad)
+    for name, base, eps in (("E", 1.4e5, 1.0), ("theta_s", 7.5e-3, 1e-7)):
+        lp = run(built_pkg, sc, sc["v"], grads=False, **{name: base + eps})[0]
+        lm = run(built_pkg, sc, sc["v"], grads=False, **{name: base - eps})[0]
+        fd = (lp - lm) / (2 * eps)
+        assert rel_err(fd, float(g[name][0])) < FD_TOL, (name, fd, float(g[name][0]))
+
+
 def test_checkpoint_interval_does_not_change_gradients(built_pkg):
     sc = plastic_scene(seed=1, n=800, grid=20)
     ref = run(built_pkg, sc, sc["v"], steps=9, every=9)[1]

@@ -1,0 +1,191 @@
+"""Parity on the measured workloads themselves, at their full sizes: the CUDA
+path through the C ABI against the oracle (the C restatement of
+material_point_method.cpp:94-350, pinned to the reference) on identical seeded
+inputs.
+
+* snowball: 8,192 particles, r = 0.1, 64^3, v0 = (0, -2, 0), theta_s = 7.5e-3,
+  sticky walls.  One step against the FP32 oracle at 1e-5 per field, and the
+  200-step rollout with the grid mass conserved to 1e-6 after every step and
+  the final state as close to the FP64 oracle as the FP32 oracle gets.
+* two balls at 128^3: the 1.1M-particle workload the throughput is quoted on,
+  and the stated 8-per-cell geometry (about 4.7e5 particles); one step, every
+  particle field and the grid mass and momentum against the oracle at 1e-5.
+* uneven batch: the largest, the largest-grid and the smallest scenes of the
+  64-scene batch stepped together in one handle, each against its own oracle.
+* cube: the 65,536-particle, 50-step, checkpoint-every-10 rollout of the
+  gradient workload in the FP64 build, reverse-mode dL/dv0 along two random
+  directions and dL/dE, dL/dnu against central finite differences at 1e-4.
+
+Errors are norm-wise, ||gpu - ref|| / ||ref||; B is measured against its
+natural scale ||v|| h because it vanishes for a rigid translation."""
+import numpy as np
+import pytest
+
+from conftest import b_scale, rel, rel_floor
+
+pytestmark = pytest.mark.gpu
+
+TOL1 = 1e-5
+
+
+def oracle_kw(sc):
+    return sc.params()
+
+
+def one_step_against_oracle(pkg, orc, sc, grid_tol=TOL1):
+    kw = oracle_kw(sc)
+    sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, **kw))
+    sim.set_particles(sc.x, sc.v, sc.mass)
+    sim.init_volumes()
+    o = orc.OracleSim(orc.Params(*sc.grid, float(sc.h), **kw), sc.x, sc.v, sc.mass)
+    o.init()
+    assert rel(sim.get_particles(("volume",))["volume"], o.vol) < 1e-6
+    sim.step(sc.dt, 1)
+    o.step(sc.dt, 1)
+    got = sim.get_particles()
+    errs = {k: rel(got[k], getattr(o, k)) for k in ("x", "v", "FE", "Jp")}
+    errs["B"] = rel_floor(got["B"], o.B, b_scale(o.v, sc.h))
+    grd = sim.get_grid()
+    errs["grid_mass"] = rel(grd["mass"], o.gmass)
+    errs["grid_momentum"] = rel(grd["mass"][:, None] * grd["vel"], o.gmass[:, None] * o.gvel)
+    assert sim.flags() == 0
+    sim.close()
+    bad = {k: e for k, e in errs.items() if not e < (1e-6 if k == "grid_mass" else grid_tol if k.startswith("grid") else TOL1)}
+    assert not bad, errs
+    return errs
+
+
+def test_snowball_one_step_matches_oracle(built_pkg, orc):
+    from rd_gb300 import scenes
+    sc = scenes.snowball()
+    assert (sc.n, sc.grid, sc.h) == (8192, (64, 64, 64), 1.0 / 64)
+    assert sc.material["theta_s"] == 7.5e-3 and sc.bc == 1 and sc.bc_width == 3
+    one_step_against_oracle(built_pkg, orc, sc)
+
+
+def test_snowball_200_step_rollout(built_pkg, orc):
+    """Grid mass after every one of the 200 steps equals the particle mass to
+    1e-6; the final particle state is compared with the FP64 oracle, next to
+    the FP32 oracle's own distance from it (the FP32 rounding of 200 steps)."""
+    from rd_gb300 import scenes
+    sc = scenes.snowball()
+    kw = sc.params()
+    sim = built_pkg.Simulation(built_pkg.make_params(*sc.grid, sc.n, sc.h, **kw))
+    sim.set_particles(sc.x, sc.v, sc.mass)
+    sim.init_volumes()
+    total = float(np.sum(sc.mass, dtype=np.float64))
+    worst = 0.0
+    for _ in range(sc.steps):
+        sim.step(sc.dt, 1)
+        gm = sim.get_grid()["mass"]
+        worst = max(worst, abs(float(np.sum(gm, dtype=np.float64)) - total) / total)
+    assert worst < 1e-6, worst
+    assert sim.flags() == 0
+    got = sim.get_particles()
+    P = orc.Params(*sc.grid, float(sc.h), **kw)
+    o64 = orc.OracleSim(P, sc.x, sc.v, sc.mass, dtype=np.float64)
+    o64.init()
+    o64.step(sc.dt, sc.steps)
+    o32 = orc.OracleSim(P, sc.x, sc.v, sc.mass)
+    o32.init()
+    o32.step(sc.dt, sc.steps)
+    for k in ("x", "v", "FE", "Jp"):
+        e_gpu, e_orc = rel(got[k], getattr(o64, k)), rel(getattr(o32, k), getattr(o64, k))
+        # FP32 rounding after 200 steps: x, F_E ~1e-7, v ~1e-5 from FP64
+        assert e_gpu < max(3.0 * e_orc, 1e-6), (k, e_gpu, e_orc)
+    e_gpu = rel_floor(got["B"], o64.B, b_scale(o64.v, sc.h))
+    e_orc = rel_floor(o32.B, o64.B, b_scale(o64.v, sc.h))
+    assert e_gpu < max(3.0 * e_orc, 1e-5), (e_gpu, e_orc)
+    assert rel(got["x"], o32.x) < 1e-5
+
+
+@pytest.mark.parametrize("which", ["two_balls_1m", "two_balls"])
+def test_two_ball_workload_one_step_matches_oracle(built_pkg, orc, which):
+    from rd_gb300 import scenes
+    sc = getattr(scenes, which)()
+    assert sc.grid == (128, 128, 128)
+    if which == "two_balls_1m":
+        assert sc.n == 1_100_000
+    else:
+        assert 4.0e5 < sc.n < 5.5e5
+    one_step_against_oracle(built_pkg, orc, sc)
+
+
+def test_uneven_batch_extremes_match_oracle(built_pkg, orc):
+    """The largest scene (most particles), the scene on the largest grid and the
+    smallest scene of the 64-scene batch, in one batch handle."""
+    from rd_gb300 import scenes
+    allsc = scenes.uneven_snowballs(seed=0)
+    by_n = sorted(range(len(allsc)), key=lambda i: allsc[i].n)
+    by_g = sorted(range(len(allsc)), key=lambda i: allsc[i].grid[0])
+    pick = []
+    for i in (by_n[-1], by_n[-2], by_g[-1], by_n[0]):
+        if i not in pick:
+            pick.append(i)
+    batch = [allsc[i] for i in pick]
+    assert max(s.n for s in batch) > 2.5e5 and max(s.grid[0] for s in batch) >= 120
+    b = built_pkg.Batch([built_pkg.make_params(*s.grid, s.n, s.h, **s.params()) for s in batch])
+    for s, sc in enumerate(batch):
+        b.set_particles(s, sc.x, sc.v, sc.mass)
+    b.init_volumes()
+    b.step(batch[0].dt, 1)
+    assert b.flags() == 0
+    for s, sc in enumerate(batch):
+        o = orc.OracleSim(orc.Params(*sc.grid, float(sc.h), **sc.params()), sc.x, sc.v, sc.mass)
+        o.init()
+        o.step(sc.dt, 1)
+        got = b.get_particles(s)
+        errs = {k: rel(got[k], getattr(o, k)) for k in ("x", "v", "FE", "Jp")}
+        errs["B"] = rel_floor(got["B"], o.B, b_scale(o.v, sc.h))
+        g = b.get_grid(s)
+        errs["grid_mass"] = rel(g["mass"], o.gmass)
+        errs["grid_momentum"] = rel(g["mass"][:, None] * g["vel"], o.gmass[:, None] * o.gvel)
+        assert all(e < (1e-6 if k == "grid_mass" else TOL1) for k, e in errs.items()), (pick[s], sc.n, errs)
+
+
+def cube_loss(pkg, sc, v0, grads, **mat):
+    target = np.array([0.55, 0.3, 0.5])
+    sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, precision=pkg.RD_FP64, **sc.params(**mat)))
+    sim.set_particles(sc.x.astype(np.float64), v0, sc.mass.astype(np.float64))
+    sim.init_volumes()
+    sim.adjoint_record(sc.dt, sc.steps, 10)
+    xT = sim.get_particles(("x",))["x"].astype(np.float64)
+    cen = xT.mean(0)
+    loss = float(np.sum((cen - target) ** 2))
+    g = None
+    if grads:
+        gx = np.tile(2.0 * (cen - target) / sc.n, (sc.n, 1))
+        g = sim.adjoint_backward(gx)
+    assert sim.flags() == 0
+    sim.close()
+    return loss, g
+
+
+def test_cube_rollout_gradient_matches_central_differences_fp64(built_pkg):
+    """The 65,536-particle cube, 64^3, 50 steps, checkpoint every 10, loss
+    ||centroid(x_T) - (0.55, 0.3, 0.5)||^2, in the FP64 build.  The initial
+    velocities carry a random field (the workload starts at rest, where every
+    particle moves alike) so the stress, the plastic split and the grid all
+    carry gradient; F_E starts at the identity, the all-tie case of the
+    singular-value backward."""
+    from rd_gb300 import scenes
+    sc = scenes.cube()
+    assert (sc.n, sc.grid, sc.steps) == (65536, (64, 64, 64), 50)
+    rng = np.random.default_rng(5)
+    v0 = sc.v.astype(np.float64) + rng.normal(0.0, 0.5, (sc.n, 3))
+    L0, g = cube_loss(built_pkg, sc, v0, True)
+    assert np.all(np.isfinite(g["v0"]))
+    for k in range(2):
+        e = rng.normal(size=v0.shape)
+        eps = 1e-6  # small enough that few singular values cross a clamp bound between the two runs
+        fd = (cube_loss(built_pkg, sc, v0 + eps * e, False)[0] - cube_loss(built_pkg, sc, v0 - eps * e, False)[0]) / (2 * eps)
+        ad = float(np.sum(g["v0"] * e))
+        assert abs(fd - ad) <= 1e-4 * max(abs(fd), abs(ad)), (k, fd, ad)
+    for name, eps in (("E", 1.0), ("nu", 1e-6)):
+        base = sc.material[name]
+        lp = cube_loss(built_pkg, sc, v0, False, **{name: base + eps})[0]
+        lm = cube_loss(built_pkg, sc, v0, False, **{name: base - eps})[0]
+        fd = (lp - lm) / (2 * eps)
+        ad = float(g[name][0])
+        assert ad != 0.0, name
+        assert abs(fd - ad) <= 1e-4 * max(abs(fd), abs(ad)), (name, fd, ad)
