@@ -20,14 +20,21 @@
 // With glm on the include path the vector and matrix members are glm::vec3 and
 // glm::mat3 as in the reference (material_point_method.hpp:96-110); otherwise
 // small stand-ins with the same member access (x/y/z, m[col][row]) are used.
+//
+// Logging follows the reference's Logger / Loggable (logger.hpp:7-43): the
+// class derives from Loggable, so MPM.setLevel(MaterialPointMethod::
+// DEFAULT_LOG_LEVEL_MPM) (main.cpp:51) compiles unchanged, and the stage calls
+// print the reference's diagnostics at its levels (see LagrangeEulerView).
 #pragma once
 
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <iostream>
 #include <stdexcept>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -57,6 +64,50 @@ struct mat3 {  // column-major like glm: m[col][row]
 }  // namespace rd_facade
 #endif
 
+// logger.hpp:7-33: messages at or above the level go to std::cout, one per
+// line; "<name> is: <value>" with std::to_string for numbers, vectors as
+// "x y z" and matrices as three lines, one per glm column.
+class Logger {
+public:
+    enum class LogLevel { INFO, WARNING, ERROR };
+    void log(LogLevel level, const std::string& iMessage) {
+        if (level >= level_) std::cout << iMessage << "\n";
+    }
+    void log(LogLevel level, const std::string& iName, float iValue) {
+        log(level, iName + " is: " + std::to_string(iValue));
+    }
+    void log(LogLevel level, const std::string& iName, int iValue) {
+        log(level, iName + " is: " + std::to_string(iValue));
+    }
+    void log(LogLevel level, const std::string& iName, const rd_facade::vec3& v) {
+        log(level, iName + " is: " + std::to_string(v[0]) + " " + std::to_string(v[1]) + " " + std::to_string(v[2]));
+    }
+    void log(LogLevel level, const std::string& iName, const rd_facade::mat3& m) {
+        std::string s;
+        for (int c = 0; c < 3; ++c) {
+            if (c) s += "\n";
+            for (int r = 0; r < 3; ++r) s += (r ? " " : "") + std::to_string(m[c][r]);
+        }
+        log(level, iName + " is: " + s);
+    }
+    void setLevel(LogLevel level) { level_ = level; }
+    // Whether a message at `level` would be printed (lets a caller skip the
+    // work of computing a value nobody sees).
+    bool enabled(LogLevel level) const { return level >= level_; }
+
+private:
+    LogLevel level_ = LogLevel::INFO;
+};
+
+// logger.hpp:36-43.
+class Loggable {
+public:
+    void setLevel(Logger::LogLevel level) { logger.setLevel(level); }
+
+protected:
+    Logger logger;
+};
+
 namespace rd {
 struct Error : std::runtime_error {
     rd_status status;
@@ -65,6 +116,10 @@ struct Error : std::runtime_error {
 }  // namespace rd
 
 namespace MaterialPointMethod {
+
+// material_point_method.hpp:15-16.
+const auto DEFAULT_LOG_LEVEL_OPTIMIZER = Logger::LogLevel::WARNING;
+const auto DEFAULT_LOG_LEVEL_MPM = Logger::LogLevel::WARNING;
 
 namespace WeightCalculator {
 // The reference's global cell size (material_point_method.cpp:17); read when a
@@ -143,12 +198,22 @@ inline void parallel_ranges(int n, F&& f) {
     const int per = (n + nt - 1) / nt;
     std::vector<std::thread> pool;
     pool.reserve(nt - 1);
-    for (int k = 1; k < nt; ++k) {
-        const int b = k * per, e = std::min(n, b + per);
-        if (b < e) pool.emplace_back([&f, b, e] { f(b, e); });
+    int next = 1;  // first range not handed to a thread
+    try {
+        for (; next < nt; ++next) {
+            const int b = next * per, e = std::min(n, b + per);
+            if (b < e) pool.emplace_back([&f, b, e] { f(b, e); });
+        }
+    } catch (const std::system_error&) {
+        // no more threads could be started: the ranges from `next` on run on
+        // this thread below, after the ones already running are joined
     }
     f(0, std::min(n, per));
     for (auto& t : pool) t.join();
+    for (; next < nt; ++next) {
+        const int b = next * per, e = std::min(n, b + per);
+        if (b < e) f(b, e);
+    }
 }
 
 // The exchange arrays of rd_set_particles / rd_get_particles, structure of
@@ -200,7 +265,19 @@ inline void soa_to_particles(const float* soa, int n, Particle* ps) {
 }
 }  // namespace detail
 
-class LagrangeEulerView {
+// Logging (Loggable, material_point_method.hpp:174): at INFO the stage calls
+// print what the reference's print - initializeParticles the particle momentum
+// and the average particles per occupied cell (material_point_method.cpp:61-62),
+// rasterizeParticlesToGrid the particle and grid momentum (:122-125),
+// computeParticleVolumesAndDensities the average cell and particle densities
+// (:140-141), updateDeformationGradient the average of F_E F_P (:329) - and at
+// WARNING (the default level, DEFAULT_LOG_LEVEL_MPM) rasterizeParticlesToGrid
+// warns when the two momenta differ by more than 1% (:126-128).  The values come
+// from device reductions (rd_get_diagnostics), which wait for the stream, so
+// they are computed only at a level that prints them: setLevel(ERROR) skips all
+// of it.  The reference's per-particle "SVD Singular" line (:318) is not
+// printed.  step() logs nothing.
+class LagrangeEulerView : public Loggable {
 public:
     const int MAX_I, MAX_J, MAX_K;
 
@@ -238,6 +315,11 @@ public:
     void initializeParticles(const rd_facade::vec3& origin, const rd_facade::vec3& velocity) {
         reference_initial_particles(h_, origin, velocity, particles_);
         syncParticlesToDevice();
+        if (logger.enabled(Logger::LogLevel::INFO)) {
+            rd_diagnostics d = diagnostics();
+            logger.log(Logger::LogLevel::INFO, "Particles momentum", vec(d.particle_momentum));
+            logger.log(Logger::LogLevel::INFO, "Average PPC", averagePPC());
+        }
     }
 
     // Returns the host copy, synchronised from the device (material_point_method.hpp:181-183).
@@ -248,8 +330,32 @@ public:
     // Uploads the host copy after the caller changed particles through getParticles().
     void syncParticlesToDevice() { upload(); }
 
-    void rasterizeParticlesToGrid() { stage(RD_STAGE_RASTERIZE, 0.0); }
-    void computeParticleVolumesAndDensities() { stage(RD_STAGE_VOLUMES, 0.0); }
+    void rasterizeParticlesToGrid() {
+        stage(RD_STAGE_RASTERIZE, 0.0);
+        if (logger.enabled(Logger::LogLevel::WARNING)) {
+            const rd_diagnostics d = diagnostics();
+            logger.log(Logger::LogLevel::INFO, "ParticlesMomentum", vec(d.particle_momentum));
+            logger.log(Logger::LogLevel::INFO, "GridMomentum", vec(d.grid_momentum));
+            double diff = 0, gn = 0;
+            for (int a = 0; a < 3; ++a) {
+                diff += (d.particle_momentum[a] - d.grid_momentum[a]) * (d.particle_momentum[a] - d.grid_momentum[a]);
+                gn += d.grid_momentum[a] * d.grid_momentum[a];
+            }
+            if (std::sqrt(diff) / std::sqrt(gn) > 1e-2)  // NaN (no grid momentum) does not warn, as in the reference
+                logger.log(Logger::LogLevel::WARNING, "GridMomentum != ParticlesMomentum after rasterization");
+        }
+    }
+    void computeParticleVolumesAndDensities() {
+        stage(RD_STAGE_VOLUMES, 0.0);
+        if (logger.enabled(Logger::LogLevel::INFO)) {
+            const rd_diagnostics d = diagnostics();
+            const double cell = static_cast<double>(h_) * h_ * h_;
+            logger.log(Logger::LogLevel::INFO, "Average cell density",
+                       static_cast<float>(d.grid_mass / static_cast<double>(d.used_cells) / cell));
+            logger.log(Logger::LogLevel::INFO, "Average particle density",
+                       static_cast<float>(d.average_particle_density));
+        }
+    }
     void computeExplicitGridForces() { stage(RD_STAGE_FORCES, 0.0); }
     void gridVelocitiesUpdate(float timeDelta) { stage(RD_STAGE_GRID_VELOCITIES, timeDelta); }
     // material_point_method.cpp:264-304.  The colliders are the reference's
@@ -278,7 +384,16 @@ public:
         }
         stage(RD_STAGE_COLLISIONS, timeDelta);
     }
-    void updateDeformationGradient(float timeDelta) { stage(RD_STAGE_DEFORMATION, timeDelta); }
+    void updateDeformationGradient(float timeDelta) {
+        stage(RD_STAGE_DEFORMATION, timeDelta);
+        if (logger.enabled(Logger::LogLevel::INFO)) {
+            const rd_diagnostics d = diagnostics();
+            rd_facade::mat3 m(0.0f);
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) m[c][r] = static_cast<float>(d.average_deformation_gradient[3 * r + c]);
+            logger.log(Logger::LogLevel::INFO, "Average deformation gradient", m);
+        }
+    }
     void updateParticleVelocities() { stage(RD_STAGE_PARTICLE_VELOCITIES, 0.0); }
     void updateParticlePositions(float timeDelta) { stage(RD_STAGE_POSITIONS, timeDelta); }
 
@@ -300,6 +415,30 @@ private:
     void stage(int id, double dt) {
         check(rd_stage(sim_, id, dt), "rd_stage");
         dirty_host_ = true;
+    }
+    rd_diagnostics diagnostics() {
+        rd_diagnostics d;
+        check(rd_get_diagnostics(sim_, 0, &d), "rd_get_diagnostics");
+        return d;
+    }
+    static rd_facade::vec3 vec(const double* v) {
+        return rd_facade::vec3(static_cast<float>(v[0]), static_cast<float>(v[1]), static_cast<float>(v[2]));
+    }
+    // averagePPC (material_point_method.cpp:396-414): particles per cell
+    // ivec3(pos / h), averaged over the cells holding any, from the host copy.
+    float averagePPC() {
+        const Particle* ps = getParticles();
+        std::vector<int> cnt(static_cast<size_t>(MAX_I) * MAX_J * MAX_K, 0);
+        for (int i = 0; i < n_; ++i) {
+            const int a = static_cast<int>(ps[i].pos[0] / h_), b = static_cast<int>(ps[i].pos[1] / h_),
+                      c = static_cast<int>(ps[i].pos[2] / h_);
+            if (a < 0 || b < 0 || c < 0 || a >= MAX_I || b >= MAX_J || c >= MAX_K) continue;
+            ++cnt[(static_cast<size_t>(a) * MAX_J + b) * MAX_K + c];
+        }
+        long sum = 0, occupied = 0;
+        for (int v : cnt)
+            if (v > 0) { sum += v; ++occupied; }
+        return static_cast<float>(sum) / static_cast<float>(occupied);
     }
     // host_ holds the exchange arrays (detail::soa_offset)
     float* soa(int k) { return host_ + detail::soa_offset(k, n_); }

@@ -1,19 +1,30 @@
 // A headless copy of the reference's driver sequence (main.cpp:48-54 and one
 // pass of main.cpp:192-218 with dt = 1e-5 and no colliders) over the C++
 // drop-in header; writes x, v, B, F_E, F_P (row-major) and volume per particle.
-// argv[2] = "stages" runs the seven stage calls, "fused" calls step(dt).
+// argv[2] = "stages" runs the seven stage calls, "fused" calls step(dt);
+// argv[3] = "info" lowers the log level to INFO after main.cpp's own setLevel.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
 #include "rd_lagrange_euler_view.hpp"
+#if !__has_include(<glm/glm.hpp>)
+namespace glm {
+using vec3 = rd_facade::vec3;  // glm is not on this driver's include path
+}
+#endif
 int main(int argc, char** argv) {
     if (argc < 3) return 2;
     const bool fused = std::strcmp(argv[2], "fused") == 0;
     MaterialPointMethod::WeightCalculator::h = 0.05f;
     std::srand(1);
-    MaterialPointMethod::LagrangeEulerView MPM{20, 20, 20, 270 + 1877};
-    MPM.initializeParticles({0.5f, 0.6f, 0.5f}, {0.0f, -200.0f, 0.0f});
+    // main.cpp:48-54, line for line
+    const auto numParticles = 270 + 1877;
+    const glm::vec3 particlesOrigin(0.5f, 0.6f, 0.5f);
+    MaterialPointMethod::LagrangeEulerView MPM{ 20, 20, 20, numParticles };
+    MPM.setLevel(MaterialPointMethod::DEFAULT_LOG_LEVEL_MPM);
+    if (argc > 3 && std::strcmp(argv[3], "info") == 0) MPM.setLevel(Logger::LogLevel::INFO);
+    MPM.initializeParticles(particlesOrigin, { 0.0f, -200.0f, 0.0f });
     MPM.rasterizeParticlesToGrid();
     MPM.computeParticleVolumesAndDensities();
     const float delta = 1e-5f;

@@ -53,3 +53,38 @@ def test_cpp_driver_matches_reference_scene(built_pkg, tmp_path, mode):
     assert rel(rec[:, 15:24], g["s1_FE"]) < 1e-5
     assert rel(rec[:, 24:33], g["s1_FP"]) < 1e-5
     assert rel(rec[:, 33], g["vol0"]) < 1e-6
+
+
+def test_cpp_driver_compiles_with_the_reference_logging_calls(tmp_path):
+    """main.cpp:51 (MPM.setLevel(MaterialPointMethod::DEFAULT_LOG_LEVEL_MPM))
+    and the rest of main.cpp:48-54 compile against the drop-in header."""
+    obj = tmp_path / "drive.o"
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-c", "-I", INC, os.path.join(CPP, "main_reference_scene.cpp"),
+                           "-o", str(obj)])
+
+
+@pytest.mark.gpu
+def test_cpp_driver_logs_like_the_reference(built_pkg, tmp_path):
+    """At INFO the stage calls print the reference's diagnostics (its
+    material_point_method.cpp:61-62,122-125,140-141,329); at the default
+    WARNING level nothing is printed for this scene."""
+    exe = tmp_path / "drive"
+    libdir = os.path.dirname(built_pkg.LIB_PATH)
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-pthread", "-I", INC, os.path.join(CPP, "main_reference_scene.cpp"),
+                           "-L", libdir, "-l:librd_mpm.so", f"-Wl,-rpath,{libdir}", "-o", str(exe)])
+    quiet = subprocess.run([str(exe), str(tmp_path / "a.bin"), "stages"], capture_output=True, text=True, check=True)
+    assert quiet.stdout == ""
+    loud = subprocess.run([str(exe), str(tmp_path / "b.bin"), "stages", "info"], capture_output=True, text=True,
+                          check=True)
+    lines = loud.stdout.splitlines()
+    heads = [ln.split(" is: ")[0] for ln in lines if " is: " in ln]
+    assert heads[:2] == ["Particles momentum", "Average PPC"]
+    assert heads.count("ParticlesMomentum") == 2 and heads.count("GridMomentum") == 2
+    assert "Average cell density" in heads and "Average particle density" in heads
+    assert "Average deformation gradient" in heads
+    # 2147 particles of mass 6e-5 moving at (0, -200, 0): momentum (0, -25.764, 0)
+    pm = [ln for ln in lines if ln.startswith("Particles momentum is: ")][0].split(": ")[1].split()
+    assert abs(float(pm[1]) + 2147 * 6e-5 * 200) < 1e-3 and abs(float(pm[0])) < 1e-6
+    ppc = float([ln for ln in lines if ln.startswith("Average PPC is: ")][0].split(": ")[1])
+    assert 4.0 < ppc < 8.0
+    assert "GridMomentum != ParticlesMomentum" not in loud.stdout
