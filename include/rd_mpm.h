@@ -388,8 +388,21 @@ rd_status rd_adjoint_backward(rd_handle* h, const void* grad_x, const void* grad
  * calls share the array and it keeps the previous call's contents (the call
  * clears what must start at zero), so calls whose work overlaps on the GPU -
  * on different streams, or from different threads - race and must be
- * serialised by the caller. */
+ * serialised by the caller.
+ *
+ * Status: the call returns RD_CUDA_ERROR when a launch fails, and also, queuing
+ * nothing, when a CUDA error left by earlier work is pending (it is not
+ * consumed).  What the kernels find is recorded in the shared array's flags
+ * word, cleared at the start of every call: RD_FLAG_OUT_OF_DOMAIN when a
+ * particle's stencil reaches past the grid (those nodes are dropped) and
+ * RD_FLAG_BAD_WORK when a particle lies more than a cell outside the grid (the
+ * particle is dropped) or the work list overflowed.  Read it with
+ * rd_rasterize_noalloc_flags once the stream has been synchronised. */
 rd_status rd_rasterize_noalloc(const rd_params* params, const rd_particles* in, float* grid_out, void* stream);
+/* The flags word of the last rd_rasterize_noalloc on the current device (0 if
+ * none ran there): a blocking 4-byte device-to-host copy, made after the
+ * caller has synchronised the stream of that call.  Allocates nothing. */
+rd_status rd_rasterize_noalloc_flags(uint32_t* flags);
 
 #ifdef __cplusplus
 }

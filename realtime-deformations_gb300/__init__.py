@@ -50,7 +50,7 @@ EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
            "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
            "rd_set_colors", "rd_device_colors", "rd_splat", "rd_initialize_particles", "rd_get_diagnostics",
-           "rd_rasterize_noalloc")
+           "rd_rasterize_noalloc", "rd_rasterize_noalloc_flags")
 KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g", "adj_g2p", "adj_p2g")
 
 
@@ -199,6 +199,7 @@ def lib():
             L.rd_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]
             L.rd_host_free.argtypes = [vp]
             L.rd_rasterize_noalloc.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(_Particles), vp, vp]
+            L.rd_rasterize_noalloc_flags.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
             L.rd_batch_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int32, ctypes.POINTER(vp)]
             L.rd_batch_num_scenes.argtypes = [vp, ctypes.POINTER(ctypes.c_int32)]
             L.rd_batch_set_particles.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(_Particles), ctypes.c_int]

@@ -2394,6 +2394,10 @@ extern "C" rd_status rd_rasterize_noalloc(const rd_params* params, const rd_part
                             ((p.max_k + kBlk - 1) / kBlk);
     if (p.num_particles > kNaMaxParticles || cells > kNaMaxKeys || nblocks * kCellsPerBlock > kNaMaxKeys)
         return RD_TOO_LARGE;
+    // an error left pending by earlier, unrelated work stays where it is (peeked,
+    // not consumed) and nothing is queued, so the errors checked below are this
+    // call's own
+    if (cudaPeekAtLastError() != cudaSuccess) return RD_CUDA_ERROR;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return RD_CUDA_ERROR;
     NaDevice nd;
@@ -2438,20 +2442,41 @@ extern "C" rd_status rd_rasterize_noalloc(const rd_params* params, const rd_part
         const uint32_t work_cap = (uint32_t)kNaMaxWork;
         k_na_keys<<<blocks_for(n, 256), 256, 0, st>>>(P, static_cast<const float*>(in->x), sc->keys, sc->counts,
                                                       sc->bcount, &sc->flags);
+        if (cudaGetLastError() != cudaSuccess) return RD_CUDA_ERROR;
         k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, st>>>(sc->bcount, hp.nblocks, ntiles, sc->tile_sums);
+        if (cudaGetLastError() != cudaSuccess) return RD_CUDA_ERROR;
         k_tile_prefix<<<1, 1024, 0, st>>>(sc->tile_sums, ntiles, &sc->nwork[1], (uint32_t)n, &sc->flags,
                                           sc->tile_list);
+        if (cudaGetLastError() != cudaSuccess) return RD_CUDA_ERROR;
         const unsigned scan_grid = (unsigned)std::min<size_t>((size_t)ntiles, (size_t)nd.sms * 2);
         k_scan<<<scan_grid, kScanThreads, 0, st>>>(sc->counts, sc->cursor, sc->bcount, sc->tile_sums, sc->tile_list,
                                                    ntiles, hp.nkeys, sc->work, &sc->nwork[0], work_cap,
                                                    (uint32_t)WorkP<float>::value, &sc->flags, nullptr, 1);
+        if (cudaGetLastError() != cudaSuccess) return RD_CUDA_ERROR;
         k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(n, sc->keys, sc->cursor, sc->perm);
+        if (cudaGetLastError() != cudaSuccess) return RD_CUDA_ERROR;
         const size_t max_items = (size_t)n / WorkP<float>::value + (size_t)std::min<int64_t>(nblocks, n) + 1;
         const unsigned grid = (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)nd.sms * nd.occ));
         k_na_p2g<<<grid, kThreads, sizeof(P2GTile<float, kBlk>), st>>>(
             P, static_cast<const float*>(in->x), static_cast<const float*>(in->v), static_cast<const float*>(in->B),
             static_cast<const float*>(in->mass), sc->perm, sc->work, &sc->nwork[0], work_cap,
             reinterpret_cast<float4*>(grid_out), &sc->flags);
+        if (cudaGetLastError() != cudaSuccess) return RD_CUDA_ERROR;
     }
-    return cudaGetLastError() == cudaSuccess ? RD_OK : RD_CUDA_ERROR;
+    return RD_OK;
+}
+
+extern "C" rd_status rd_rasterize_noalloc_flags(uint32_t* flags) {
+    if (!flags) return RD_INVALID_ARG;
+    *flags = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return RD_CUDA_ERROR;
+    NaScratch* sc = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        sc = g_na[dev].scratch;
+    }
+    if (!sc) return RD_OK;  // no rasterize has run on this device
+    return cudaMemcpy(flags, &sc->flags, sizeof(uint32_t), cudaMemcpyDeviceToHost) == cudaSuccess ? RD_OK
+                                                                                               : RD_CUDA_ERROR;
 }
