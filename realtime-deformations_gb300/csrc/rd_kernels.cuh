@@ -1140,6 +1140,11 @@ template <typename T> constexpr size_t fused_smem_bytes() { return sizeof(FusedS
 
 // Polls of a tile copy's mbarrier before the kernel gives up (RD_FLAG_WAIT_TIMEOUT).
 constexpr int kTileWaitTries = 1 << 16;
+// After giving up, the CTA stays resident until the copy it issued has landed
+// (a bulk copy cannot be cancelled, and it writes this CTA's shared memory):
+// up to this many rounds of kTileWaitTries / 64 polls, each followed by a
+// 64 us sleep - a second or more in all - before it leaves regardless.
+constexpr int kTileDrainRounds = 16384;
 
 // The tile-copy wait on an mbarrier that no copy and no thread arrives at:
 // it must give up after `tries` polls and report it.
@@ -1380,7 +1385,12 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
         if (__syncthreads_or(!arrived)) {
             if (threadIdx.x == 0) {
                 raise_flag(D.flags, 8u);
-                mbar_wait(&S.tbar, parity ^ 1u, kTileWaitTries);  // the copy in flight, bounded again
+                // the copy in flight (this item's) lands in this CTA's shared
+                // memory: wait for it before the CTA exits, bounded
+                for (int r = 0; r < kTileDrainRounds; ++r) {
+                    if (mbar_wait(&S.tbar, parity ^ 1u, kTileWaitTries / 64)) break;
+                    __nanosleep(64000);
+                }
             }
             return;
         }
