@@ -41,12 +41,26 @@ def build_oracle(force: bool = False) -> None:
         os.replace(out + ".tmp", out)
 
 
-def build_ref(reference_root: str = "/root/reference") -> bool:
-    """Build the headless reference if its sources are present.  Returns whether
+def reference_root():
+    """The directory holding the reference's ``realtime-deformations/`` sources:
+    ``$RD_REFERENCE_ROOT`` when set, else ``$RD_REFERENCE_DEFAULT`` as this
+    repository's build recipe exports it for its own checkout; None when neither
+    names a directory that holds them."""
+    for var in ("RD_REFERENCE_ROOT", "RD_REFERENCE_DEFAULT"):
+        root = os.environ.get(var)
+        if root and os.path.isdir(os.path.join(root, "realtime-deformations")):
+            return root
+    return None
+
+
+def build_ref(root=None) -> bool:
+    """Build the headless reference from the sources under ``root`` (default
+    ``reference_root()``) if they are present.  Returns whether
     ``librd_ref.so`` is usable afterwards."""
+    root = root or reference_root()
     script = os.path.join(HERE, "ref", "build_ref.sh")
-    if os.path.isdir(os.path.join(reference_root, "realtime-deformations")):
-        subprocess.check_call(["bash", script, reference_root])
+    if root and os.path.isdir(os.path.join(root, "realtime-deformations")):
+        subprocess.check_call(["bash", script, root])
     return ref_available()
 
 

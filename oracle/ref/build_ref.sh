@@ -3,7 +3,7 @@
 # headless shared library, oracle/_ref/librd_ref.so, for use as the parity
 # oracle and the timed CPU baseline.  Test infrastructure only.
 #
-#   usage: oracle/ref/build_ref.sh [REFERENCE_ROOT]     (default /root/reference)
+#   usage: oracle/ref/build_ref.sh REFERENCE_ROOT   (the directory holding realtime-deformations/)
 #
 # Four first-party files are staged into oracle/_ref/src (git-ignored, deleted
 # again once the library is linked) because three of them are patched; everything else (glm, Eigen, mcloptlib, the polar
@@ -19,7 +19,7 @@
 #       plastic SVD goes through rd_ref_toEigen/rd_ref_toGlm, which reproduce
 #       the reference's transposition unless rd_ref_p4 = 1
 set -euo pipefail
-REF_ROOT="${1:-/root/reference}"
+REF_ROOT="${1:?usage: build_ref.sh REFERENCE_ROOT}"
 RD="$REF_ROOT/realtime-deformations"
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/../_ref"

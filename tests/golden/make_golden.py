@@ -131,9 +131,11 @@ FIXTURES = {"ref_scene_20": ref_scene, "perturbed_16": perturbed, "colliders_32"
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # usage: make_golden.py REFERENCE_ROOT [fixture ...]; REFERENCE_ROOT "-" takes
+    # $RD_REFERENCE_ROOT (oracle.reference_root())
+    root = sys.argv[1] if len(sys.argv) > 1 and sys.argv[1] != "-" else orc.reference_root()
     names = sys.argv[2:] or list(FIXTURES)
-    if not orc.build_ref(root):
+    if not root or not orc.build_ref(root):
         raise SystemExit("headless reference not available")
     for name in names:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **FIXTURES[name]())
