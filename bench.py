@@ -66,8 +66,12 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-baseline", type=int, default=1, help="time the single-core CPU baseline (rank 0, N=1)")
     ap.add_argument("--adjoint", type=int, default=1, help="measure forward + adjoint on the 65,536-particle cube")
-    ap.add_argument("--only", choices=("batched", "adjoint", "batched_adjoint"), default=None,
-                    help="run one secondary measurement alone and print its JSON (profiling runs)")
+    ap.add_argument("--only", choices=("batched", "adjoint", "batched_adjoint", "snowball", "profile"),
+                    default=None,
+                    help="run one secondary measurement alone and print its JSON; 'profile' only initialises "
+                         "the workload and runs --warmup + --steps steps (for ncu captures)")
+    ap.add_argument("--snowball", type=int, default=1, help="measure the 8,192-particle snowball on 64^3")
+    ap.add_argument("--link", type=int, default=1, help="measure the host link (pinned copies each way)")
     ap.add_argument("--batch-steps", type=int, default=-1,
                     help="timed steps of the batched-forward workload (64 uneven scenes); -1: as many as "
                          "--steps, so the batch and the plain forward it is compared with run equally long; "
@@ -187,24 +191,141 @@ def captured_traffic(kernel, workload, particles):
     return None
 
 
+def captured_issue(kernel, workload, particles):
+    """Warp instructions per launch of `kernel` (ncu smsp__inst_executed.sum)
+    from profiles/issue.txt, scaled by particle count to this workload, and the
+    record's source, or (None, None)."""
+    path = os.path.join(REPO, "profiles", "issue.txt")
+    try:
+        for line in open(path):
+            f = line.split()
+            if len(f) >= 5 and not line.startswith("#") and f[0] == kernel and f[1] == workload:
+                return int(f[3]) * particles / int(f[2]), f[4]
+    except OSError:
+        pass
+    return None, None
+
+
+def cpu_model():
+    """The host CPU's model string (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def pin_to_core(core):
+    """Restricts this process to one core (as taskset does); returns the
+    previous affinity to restore, or None where affinity cannot be set."""
+    try:
+        old = os.sched_getaffinity(0)
+        os.sched_setaffinity(0, {core})
+        return old
+    except (AttributeError, OSError):
+        return None
+
+
+def oracle_for(orc, sc):
+    """The reference's CPU step for the workload: its headless build where it is
+    loadable here (it has no grid walls, so it steps without them), else the C
+    restatement (with the workload's walls).  Returns (sim, kind)."""
+    mat = {k: v for k, v in sc.material.items()}
+    if orc.ref_available():
+        return orc.RefSim(orc.Params(*sc.grid, sc.h, **mat), sc.x, sc.v, sc.mass, p4=1), "reference"
+    P = orc.Params(*sc.grid, sc.h, bc=sc.bc, bc_width=sc.bc_width, **mat)
+    return orc.OracleSim(P, sc.x, sc.v, sc.mass), "port"
+
+
 def cpu_baseline_single_core(sc, seconds_hint=20.0):
     """The oracle (the headless reference where loadable, else the C
-    restatement) timed on one core for one full step of the workload after
-    its init; returns (particle-steps/s, kind, sample description)."""
+    restatement) timed on one pinned core for one full step of the workload
+    after its init; returns (particle-steps/s, kind, sample description)."""
     orc = graft.load_oracle()
     orc.build_oracle()
-    P = orc.Params(*sc.grid, sc.h, **{k: v for k, v in sc.material.items()})
-    if orc.ref_available():
-        sim = orc.RefSim(P, sc.x, sc.v, sc.mass, p4=1)
-        kind = "reference"
-    else:
-        sim = orc.OracleSim(P, sc.x, sc.v, sc.mass)
-        kind = "port"
+    sim, kind = oracle_for(orc, sc)
     sim.init()
-    t0 = time.perf_counter()
-    sim.step(sc.dt, 1)
-    dt = time.perf_counter() - t0
-    return sc.n / dt, kind, f"1 step of all {sc.n} particles after init, single thread ({dt:.1f} s)"
+    core = sorted(os.sched_getaffinity(0))[-1] if hasattr(os, "sched_getaffinity") else 0
+    old = pin_to_core(core)
+    try:
+        t0 = time.perf_counter()
+        sim.step(sc.dt, 1)
+        dt = time.perf_counter() - t0
+    finally:
+        if old is not None:
+            os.sched_setaffinity(0, old)
+    pinned = f"pinned to core {core}" if old is not None else "unpinned"
+    return sc.n / dt, kind, (f"1 step of all {sc.n} particles after init, single thread {pinned} "
+                             f"({dt:.1f} s) on {cpu_model()}")
+
+
+def measure_link(local, nbytes=1 << 30, reps=3):
+    """The host link alone: one cudaMemcpyAsync of `nbytes` from page-locked
+    host memory to the device and one back, CUDA events on one stream, best of
+    `reps`; GB/s each way."""
+    import torch
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    dev = torch.empty(nbytes, dtype=torch.uint8, device=torch.device("cuda", local))
+    st = torch.cuda.Stream(device=local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = {"h2d": float("inf"), "d2h": float("inf")}
+    with torch.cuda.stream(st):
+        for _ in range(reps + 1):
+            for way in ("h2d", "d2h"):
+                e0.record(st)
+                if way == "h2d":
+                    dev.copy_(host, non_blocking=True)
+                else:
+                    host.copy_(dev, non_blocking=True)
+                e1.record(st)
+                e1.synchronize()
+                best[way] = min(best[way], e0.elapsed_time(e1))
+    del host, dev
+    return {k: nbytes / (v / 1e3) / 1e9 for k, v in best.items()}
+
+
+def measure_snowball(pkg, local, warmup):
+    """The 8,192-particle snowball on 64^3 for its 200 steps (graph-pair replay):
+    a launch- and latency-bound step; CUDA events on the handle's stream."""
+    import torch
+    graft.load_package()
+    from rd_gb300 import scenes
+    sc = scenes.snowball()
+    sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, device=local, **sc.params()))
+    stream = torch.cuda.ExternalStream(sim.stream(), device=local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for _ in range(3):
+        sim.set_particles(sc.x, sc.v, sc.mass)
+        sim.init_volumes()
+        sim.step(sc.dt, warmup)
+        sim.synchronize()
+        l0, r0 = sim.launch_count(), sim.graph_replays()
+        e0.record(stream)
+        sim.step(sc.dt, sc.steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        if best is None or ms < best[0]:
+            best = (ms, sim.launch_count() - l0, sim.graph_replays() - r0)
+    flags = sim.flags()
+    sim.close()
+    ms, launches, replays = best
+    return {"value": sc.n * sc.steps / (ms / 1e3), "unit": "particle-steps/s", "steps": sc.steps,
+            "warmup": warmup, "ms_per_step": ms / sc.steps, "gpu_launches": launches, "graph_replays": replays,
+            "flags": flags, "timing": "best of 3 passes from the initial state",
+            "workload": "snowball: 8,192 particles uniform in a sphere r = 0.1 at (0.5, 0.6, 0.5), 64^3, "
+                        "v0 = (0, -2, 0), sticky walls, 200 steps, FP32"}
 
 
 def measure_batched(pkg, local, steps, warmup, plain_value):
@@ -421,6 +542,15 @@ def measure_batched_adjoint(pkg, local):
                         "theta = (2e-2, 5e-3), FP32"}
 
 
+def workload_config(sc, ws):
+    """The workload as both arms report it."""
+    return {"workload": sc.name, "particles_per_gpu": sc.n, "grid": list(sc.grid), "dx": sc.h, "dt": sc.dt,
+            "material": {k: v for k, v in sc.material.items()},
+            "bc": f"sticky walls, {sc.bc_width} cells" if sc.bc else "none",
+            "parallelism": f"{ws} independent replica(s)",
+            "l2": f"inputs larger than L2: {2 * 7 * 16 * sc.n / 1e6:.0f} MB of particle planes per step"}
+
+
 def run_ours(args):
     import torch
 
@@ -465,6 +595,7 @@ def run_ours(args):
     ms_max = max_over_ranks(ws, ms, device=torch.device("cuda", local))
     value = ws * sc.n * args.steps / (ms_max / 1e3)
     assert sim.flags() & ~pkg.FLAG_OUT_OF_DOMAIN == 0, f"device flags {sim.flags()}"
+    clock_summary = clocks.summary()
 
     # grid occupancy at the end of the timed steps, for the per-cell byte terms
     grid = sim.get_grid()
@@ -527,17 +658,39 @@ def run_ours(args):
     e2e_value = ws * sc.n * e2e_steps / e2e_s
     e2e_mapped = ws * sc.n * e2e_steps / e2e_mapped_s
     e2e_pageable = ws * sc.n * e2e_steps / e2e_pageable_s
+    del pinned, pageable
+    # the host link's own rate: the floor of an e2e step is its bytes in and out
+    # at that rate (in and out follow each other within a step)
+    link = measure_link(local) if args.link else None
+    e2e_ms = e2e_s / e2e_steps * 1e3
+    link_keys = {}
+    if link:
+        floor_ms = (io_bytes / link["h2d"] + io_bytes / link["d2h"]) / 1e9 * 1e3
+        link_keys = {"link_gbs_h2d": link["h2d"], "link_gbs_d2h": link["d2h"], "link_floor_ms": floor_ms,
+                     "ms_per_step": e2e_ms, "link_frac": floor_ms / e2e_ms,
+                     "link_method": "one cudaMemcpyAsync of 1 GiB each way between page-locked host memory "
+                                    "and the device, CUDA events, best of 3"}
+
+    # instruction ceiling of the dominant kernel: warp instructions per launch
+    # (one ncu capture, scaled by particle count) over what the SMs can issue
+    # in the event-timed launch at the sampled SM clock (4 schedulers per SM)
+    kname = {"p2g": "k_p2g", "g2p2g": "k_g2p2g"}[dom]
+    inst, inst_src = captured_issue(kname, sc.name, sc.n)
+    issue = None
+    if inst is not None:
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clock_summary.get("sm_mhz") or clock_summary.get("sm_max_mhz") or 2070.0
+        slots = sms * 4 * mhz * 1e6 * avg_s
+        issue = {"warp_instructions_per_launch": inst, "per_particle": inst / sc.n, "sms": sms, "sm_mhz": mhz,
+                 "frac": inst / slots, "hbm_frac_at_full_issue": achieved / peak * slots / inst, "source": inst_src}
 
     out = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": sc.name, "particles_per_gpu": sc.n, "grid": list(sc.grid), "dx": sc.h,
-                   "dt": sc.dt, "material": {k: v for k, v in sc.material.items()}, "bc": "sticky walls, 3 cells",
-                   "active_cells": active_cells, "parallelism": f"{ws} independent replica(s)",
-                   "l2": f"inputs larger than L2: {2 * 7 * 16 * sc.n / 1e6:.0f} MB of particle planes per step"},
+        "config": workload_config(sc, ws),
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": io_bytes,
-                "d2h_bytes_per_step": io_bytes, "steps": e2e_steps,
+                "d2h_bytes_per_step": io_bytes, "steps": e2e_steps, **link_keys,
                 "path": "rd_set_particles(RD_HOST) + rd_step + rd_get_particles(RD_HOST) on page-locked host "
                         "arrays: the pack / unpack kernels read and write them in place over NVLink-C2C",
                 "bytes_in_place_per_step": e2e_moved[0], "bytes_staged_per_step": e2e_moved[1],
@@ -551,14 +704,17 @@ def run_ours(args):
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src,
                      "traffic": captured_traffic({"p2g": "k_p2g", "g2p2g": "k_g2p2g"}[dom], sc.name, sc.n),
-                     "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": avg_s * 1e6},
+                     "algorithmic_bytes_per_launch": algo_bytes, "avg_launch_us": avg_s * 1e6,
+                     "active_cells": active_cells, "issue": issue},
         "step_roofline": {"achieved": step_bytes / (step_ms / 1e3) / 1e9, "unit": "GB/s",
                           "frac": step_bytes / (step_ms / 1e3) / 1e9 / peak,
                           "bytes_per_step": step_bytes},
         "kernels_ms_per_step": {k: v[1] / max(v[0], 1) for k, v in kt.items() if v[0]},
         "gpu_launches": launches,
-        "clocks": clocks.summary(),
+        "clocks": clock_summary,
     }
+    if args.snowball:
+        out["snowball"] = measure_snowball(pkg, local, max(args.warmup, 3))
     batch_steps = args.steps if args.batch_steps < 0 else args.batch_steps
     if batch_steps > 0:
         out["batched_forward"] = measure_batched(pkg, local, batch_steps, max(args.warmup, 3), value)
@@ -567,7 +723,8 @@ def run_ours(args):
         out["batched_forward_adjoint"] = measure_batched_adjoint(pkg, local)
     if rank == 0 and ws == 1 and args.cpu_baseline:
         v, kind, sample = cpu_baseline_single_core(sc)
-        out["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": kind, "sample": sample}
+        out["cpu_baseline"] = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": kind, "sample": sample,
+                               "cpu_model": cpu_model()}
     if rank == 0:
         print(json.dumps(out), flush=True)
     sim.close()
@@ -581,14 +738,11 @@ def _reference_worker(args_tuple):
     `warmup` untimed steps, then timed steps until `steps` are done or
     `budget_s` has passed (at least one).  Returns (particle-steps/s, kind,
     steps done, seconds)."""
-    name, seed, steps, warmup, budget_s = args_tuple
+    name, seed, steps, warmup, budget_s, core = args_tuple
+    pinned = pin_to_core(core) is not None
     orc = graft.load_oracle()
     sc = make_scene(name, seed=seed)
-    P = orc.Params(*sc.grid, sc.h, **{k: v for k, v in sc.material.items()})
-    if orc.ref_available():
-        sim, kind = orc.RefSim(P, sc.x, sc.v, sc.mass, p4=1), "reference"
-    else:
-        sim, kind = orc.OracleSim(P, sc.x, sc.v, sc.mass), "port"
+    sim, kind = oracle_for(orc, sc)
     sim.init()
     if warmup:
         sim.step(sc.dt, warmup)
@@ -597,7 +751,7 @@ def _reference_worker(args_tuple):
         sim.step(sc.dt, 1)
         done += 1
     el = time.perf_counter() - t0
-    return sc.n * done / el, kind, done, el
+    return sc.n * done / el, kind, done, el, pinned
 
 
 def run_reference(args):
@@ -613,26 +767,31 @@ def run_reference(args):
     orc = graft.load_oracle()
     orc.build_oracle()
     sc = make_scene(args.workload, seed=0)
-    cores = os.cpu_count() or 1
+    avail = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else list(range(os.cpu_count() or 1))
+    cores = len(avail)
     per_worker = max(1, -(-args.steps // cores))
     warm = min(args.warmup, 1)
     budget_s = 60.0
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        res = pool.map(_reference_worker, [(args.workload, c, per_worker, warm, budget_s) for c in range(cores)])
+        res = pool.map(_reference_worker,
+                       [(args.workload, c, per_worker, warm, budget_s, avail[c]) for c in range(cores)])
     value = float(sum(r[0] for r in res))
     kind = res[0][1]
     steps_done = sum(r[2] for r in res)
+    pinned = "each pinned to its own core" if all(r[4] for r in res) else "unpinned"
+    walls = ("the reference has no grid walls: its step runs without them" if kind == "reference"
+             else "with the workload's walls")
     out = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-        "config": {"workload": sc.name, "particles_per_gpu": sc.n, "grid": list(sc.grid), "dx": sc.h,
-                   "dt": sc.dt, "material": {k: v for k, v in sc.material.items()}},
+        "config": workload_config(sc, ws),
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": kind,
-                         "sample": f"{cores} independent single-threaded instances, each stepping all {sc.n} "
-                                   f"particles of the workload on its {sc.grid[0]}^3 grid after init and "
-                                   f"{warm} untimed step; {steps_done} full steps timed in total "
+                         "cpu_model": cpu_model(),
+                         "sample": f"{cores} independent single-threaded instances ({pinned}), each stepping "
+                                   f"all {sc.n} particles of the workload on its {sc.grid[0]}^3 grid after init "
+                                   f"and {warm} untimed step ({walls}); {steps_done} full steps timed in total "
                                    f"(at most {per_worker} per instance, {budget_s:.0f} s bound)"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -644,7 +803,19 @@ def run_only(args):
     torch.cuda.set_device(0)
     pkg = graft.load_package()
     pkg.build()
-    if args.only == "batched":
+    if args.only == "profile":
+        sc = make_scene(args.workload, seed=0)
+        sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, **sc.params()))
+        sim.set_particles(sc.x, sc.v, sc.mass)
+        sim.init_volumes()
+        sim.step(sc.dt, args.warmup)
+        sim.step(sc.dt, args.steps)
+        sim.synchronize()
+        out = {"workload": sc.name, "particles": sc.n, "steps": args.warmup + args.steps, "flags": sim.flags()}
+        sim.close()
+    elif args.only == "snowball":
+        out = measure_snowball(pkg, 0, max(args.warmup, 3))
+    elif args.only == "batched":
         out = measure_batched(pkg, 0, args.steps, max(args.warmup, 3), float("nan"))
     elif args.only == "adjoint":
         out = measure_adjoint(pkg, 0)
