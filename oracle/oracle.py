@@ -41,26 +41,47 @@ def build_oracle(force: bool = False) -> None:
         os.replace(out + ".tmp", out)
 
 
+# Copy of the reference sources the headless build needs (oracle/ref/stage_tree.sh),
+# for machines without a checkout of the reference; git-ignored.
+TREE = os.path.join(HERE, "_ref", "tree")
+
+
+def _holds_sources(root) -> bool:
+    return bool(root) and os.path.isfile(os.path.join(root, "realtime-deformations", "material_point_method.cpp"))
+
+
 def reference_root():
     """The directory holding the reference's ``realtime-deformations/`` sources:
     ``$RD_REFERENCE_ROOT`` when set, else ``$RD_REFERENCE_DEFAULT`` as this
-    repository's build recipe exports it for its own checkout; None when neither
-    names a directory that holds them."""
-    for var in ("RD_REFERENCE_ROOT", "RD_REFERENCE_DEFAULT"):
-        root = os.environ.get(var)
-        if root and os.path.isdir(os.path.join(root, "realtime-deformations")):
+    repository's build recipe exports it for its own checkout, else the staged
+    copy ``oracle/_ref/tree``; None when none holds them."""
+    for root in (os.environ.get("RD_REFERENCE_ROOT"), os.environ.get("RD_REFERENCE_DEFAULT"), TREE):
+        if _holds_sources(root):
             return root
     return None
+
+
+def start_ref_build(root=None):
+    """Starts building the headless reference from the sources under ``root``
+    (default ``reference_root()``) in the background and returns the process,
+    or None when no sources are found.  Building from a checkout first stages
+    the copy ``oracle/_ref/tree`` that another machine builds from."""
+    root = root or reference_root()
+    if not _holds_sources(root):
+        return None
+    if os.path.realpath(root) != os.path.realpath(TREE):
+        subprocess.check_call(["bash", os.path.join(HERE, "ref", "stage_tree.sh"), root],
+                              stdout=subprocess.DEVNULL)
+    return subprocess.Popen(["bash", os.path.join(HERE, "ref", "build_ref.sh"), root])
 
 
 def build_ref(root=None) -> bool:
     """Build the headless reference from the sources under ``root`` (default
     ``reference_root()``) if they are present.  Returns whether
     ``librd_ref.so`` is usable afterwards."""
-    root = root or reference_root()
-    script = os.path.join(HERE, "ref", "build_ref.sh")
-    if root and os.path.isdir(os.path.join(root, "realtime-deformations")):
-        subprocess.check_call(["bash", script, root])
+    proc = start_ref_build(root)
+    if proc is not None and proc.wait() != 0:
+        raise subprocess.CalledProcessError(proc.returncode, "build_ref.sh")
     return ref_available()
 
 
