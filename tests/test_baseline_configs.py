@@ -177,7 +177,9 @@ def test_cube_rollout_gradient_matches_central_differences_fp64(built_pkg):
     assert np.all(np.isfinite(g["v0"]))
     for k in range(2):
         e = rng.normal(size=v0.shape)
-        eps = 1e-6  # small enough that few singular values cross a clamp bound between the two runs
+        # the loss is smooth to ~1e-7 relative over 1e-4..1e-3 here; below 1e-5 the
+        # rounding of the 50-step rollout dominates the difference quotient
+        eps = 1e-4
         fd = (cube_loss(built_pkg, sc, v0 + eps * e, False)[0] - cube_loss(built_pkg, sc, v0 - eps * e, False)[0]) / (2 * eps)
         ad = float(np.sum(g["v0"] * e))
         assert abs(fd - ad) <= 1e-4 * max(abs(fd), abs(ad)), (k, fd, ad)
