@@ -442,7 +442,7 @@ __device__ __forceinline__ void adj_g2p_item(const DevParams<T>& P, const DevBuf
         }
     }
     sort_ranked<T, kBlk>(S.p, j, rcell, rrank);
-    p2g_tasks<T, false, kBlk>(S.p, sorted_total(S.p));
+    p2g_runs<T, false, kBlk>(S.p, sorted_total(S.p));
     __syncthreads();
     p2g_flush<T, kBlk>(P, S.p, org, agrid);
     __syncthreads();

@@ -966,6 +966,133 @@ __device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int total) {
     }
 }
 
+// p2g_tasks by runs: a warp takes its share of the sorted slots as runs of
+// one cell, each run's end known from the cell's offset and count (S.off,
+// S.cnt after sort_ranked), so the loop over a run carries no per-record cell
+// load or test; a lane accumulates while the run lasts and flushes once.
+template <typename T, bool MOM, int CA>
+__device__ __forceinline__ void p2g_runs(P2GTile<T, CA>& S, int total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int ox = lane >> 3, oy = (lane >> 1) & 3, oz0 = lane & 1;
+    const T fx = (T)ox, fy = (T)oy, fz = (T)oz0;
+    const int k0 = (int)(((long long)total * warp) / nwarps), k1 = (int)(((long long)total * (warp + 1)) / nwarps);
+    const T* recs = reinterpret_cast<const T*>(S.rec);
+    int k = k0;
+    if constexpr (sizeof(T) == 4) {
+        const float2 fzz = make_float2(fz, fz + 2.f);
+        while (k < k1) {
+            const int c = S.scell[k];
+            const int e = min(S.off[c] + S.cnt[c], k1);
+            float2 am2 = make_float2(0.f, 0.f), qx2 = am2, qy2 = am2, qz2 = am2;
+#pragma unroll 1
+            for (; k < e; ++k) {
+                const int j = S.order[k];
+                const T* rs = recs + j * (4 * kRecV4);
+                const float wxy = rs[ox] * rs[4 + oy];
+                const float2 w = __fmul2_rn(make_float2(wxy, wxy), *reinterpret_cast<const float2*>(rs + 8 + 2 * oz0));
+                const vec4<T>* r = &S.rec[j * kRecV4];
+                const vec4<T> qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
+                const float cx = qm.x + a4.x * fx + a4.w * fy;
+                const float cy = qm.y + a4.y * fx + b4.x * fy;
+                const float cz = qm.z + a4.z * fx + b4.y * fy;
+                const float2 px = __ffma2_rn(make_float2(b4.z, b4.z), fzz, make_float2(cx, cx));
+                const float2 py = __ffma2_rn(make_float2(b4.w, b4.w), fzz, make_float2(cy, cy));
+                const float2 pz = __ffma2_rn(make_float2(c4.x, c4.x), fzz, make_float2(cz, cz));
+                if (MOM) am2 = __ffma2_rn(w, make_float2(qm.w, qm.w), am2);
+                qx2 = __ffma2_rn(w, px, qx2);
+                qy2 = __ffma2_rn(w, py, qy2);
+                qz2 = __ffma2_rn(w, pz, qz2);
+            }
+            const T am[2] = {am2.x, am2.y};
+            const T aq[2][3] = {{qx2.x, qy2.x, qz2.x}, {qx2.y, qy2.y, qz2.y}};
+            p2g_flush_lane<T, CA>(S, c, ox, oy, oz0, am, aq, MOM);
+        }
+    } else {
+        while (k < k1) {
+            const int c = S.scell[k];
+            const int e = min(S.off[c] + S.cnt[c], k1);
+            T am[2] = {T(0), T(0)}, aq[2][3] = {{T(0), T(0), T(0)}, {T(0), T(0), T(0)}};
+            for (; k < e; ++k) {
+                const int j = S.order[k];
+                const T* rs = recs + j * (4 * kRecV4);
+                const T wxy = rs[ox] * rs[4 + oy];
+                const T w0 = wxy * rs[8 + 2 * oz0], w1 = wxy * rs[9 + 2 * oz0];
+                const vec4<T>* r = &S.rec[j * kRecV4];
+                const vec4<T> qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
+                const T q0x = qm.x + a4.x * fx + a4.w * fy + b4.z * fz;
+                const T q0y = qm.y + a4.y * fx + b4.x * fy + b4.w * fz;
+                const T q0z = qm.z + a4.z * fx + b4.y * fy + c4.x * fz;
+                const T q1x = q0x + T(2) * b4.z, q1y = q0y + T(2) * b4.w, q1z = q0z + T(2) * c4.x;
+                if (MOM) { am[0] += w0 * qm.w; am[1] += w1 * qm.w; }
+                aq[0][0] += w0 * q0x; aq[0][1] += w0 * q0y; aq[0][2] += w0 * q0z;
+                aq[1][0] += w1 * q1x; aq[1][1] += w1 * q1y; aq[1][2] += w1 * q1z;
+            }
+            p2g_flush_lane<T, CA>(S, c, ox, oy, oz0, am, aq, MOM);
+        }
+    }
+}
+
+// p2g_runs for FP32 with the two half-warps on two records of the same run at
+// once: a lane owns the four nodes of one z column (ox, oy) of the 4 x 4 x 4
+// stencil, so 16 lanes cover a record and each warp instruction serves two
+// records.  A lane keeps two node pairs as float2: its own pair S0 and the
+// pair S1 that its partner lane (lane ^ 16, the same column in the other
+// half) owns - half 0 owns z offsets {0, 2}, half 1 {1, 3} - so at the end of
+// a run each lane sends S1 to its partner with one shuffle per value, adds
+// what it receives to S0 and flushes its two nodes, as p2g_runs does.  A run
+// of odd length gives the last record to half 0; half 1 adds zero weight.
+template <bool MOM, int CA>
+__device__ __forceinline__ void p2g_runs_pairs(P2GTile<float, CA>& S, int total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int hw = lane >> 4, col = lane & 15;
+    const int ox = col >> 2, oy = col & 3;
+    const float fx = (float)ox, fy = (float)oy;
+    // z offsets of the pairs: record z weights are stored in the order 0, 2, 1, 3
+    const float2 fz0 = hw ? make_float2(1.f, 3.f) : make_float2(0.f, 2.f);
+    const float2 fz1 = hw ? make_float2(0.f, 2.f) : make_float2(1.f, 3.f);
+    const int wz0 = 8 + 2 * hw, wz1 = 10 - 2 * hw;
+    const int k0 = (int)(((long long)total * warp) / nwarps), k1 = (int)(((long long)total * (warp + 1)) / nwarps);
+    const float* recs = reinterpret_cast<const float*>(S.rec);
+    int k = k0;
+    while (k < k1) {
+        const int c = S.scell[k];
+        const int e = min(S.off[c] + S.cnt[c], k1);
+        float2 m0 = make_float2(0.f, 0.f), x0 = m0, y0 = m0, z0 = m0, m1 = m0, x1 = m0, y1 = m0, z1 = m0;
+        for (int kb = k; kb < e; kb += 2) {
+            const bool mine = kb + hw < e;
+            const int kk = S.order[mine ? kb + hw : kb];
+            const float* rs = recs + kk * (4 * kRecV4);
+            const float wxy = mine ? rs[ox] * rs[4 + oy] : 0.f;
+            const float2 w0 = __fmul2_rn(make_float2(wxy, wxy), *reinterpret_cast<const float2*>(rs + wz0));
+            const float2 w1 = __fmul2_rn(make_float2(wxy, wxy), *reinterpret_cast<const float2*>(rs + wz1));
+            const float4* r = &S.rec[kk * kRecV4];
+            const float4 qm = r[3], a4 = r[4], b4 = r[5], c4 = r[6];
+            const float cx = qm.x + a4.x * fx + a4.w * fy;
+            const float cy = qm.y + a4.y * fx + b4.x * fy;
+            const float cz = qm.z + a4.z * fx + b4.y * fy;
+            if (MOM) {
+                m0 = __ffma2_rn(w0, make_float2(qm.w, qm.w), m0);
+                m1 = __ffma2_rn(w1, make_float2(qm.w, qm.w), m1);
+            }
+            x0 = __ffma2_rn(w0, __ffma2_rn(make_float2(b4.z, b4.z), fz0, make_float2(cx, cx)), x0);
+            y0 = __ffma2_rn(w0, __ffma2_rn(make_float2(b4.w, b4.w), fz0, make_float2(cy, cy)), y0);
+            z0 = __ffma2_rn(w0, __ffma2_rn(make_float2(c4.x, c4.x), fz0, make_float2(cz, cz)), z0);
+            x1 = __ffma2_rn(w1, __ffma2_rn(make_float2(b4.z, b4.z), fz1, make_float2(cx, cx)), x1);
+            y1 = __ffma2_rn(w1, __ffma2_rn(make_float2(b4.w, b4.w), fz1, make_float2(cy, cy)), y1);
+            z1 = __ffma2_rn(w1, __ffma2_rn(make_float2(c4.x, c4.x), fz1, make_float2(cz, cz)), z1);
+        }
+        k = e;
+        // the partner's pair S1 comes over, this lane's S1 goes to the partner
+        m0.x += __shfl_xor_sync(0xffffffffu, m1.x, 16); m0.y += __shfl_xor_sync(0xffffffffu, m1.y, 16);
+        x0.x += __shfl_xor_sync(0xffffffffu, x1.x, 16); x0.y += __shfl_xor_sync(0xffffffffu, x1.y, 16);
+        y0.x += __shfl_xor_sync(0xffffffffu, y1.x, 16); y0.y += __shfl_xor_sync(0xffffffffu, y1.y, 16);
+        z0.x += __shfl_xor_sync(0xffffffffu, z1.x, 16); z0.y += __shfl_xor_sync(0xffffffffu, z1.y, 16);
+        const float am[2] = {m0.x, m0.y};
+        const float aq[2][3] = {{x0.x, y0.x, z0.x}, {x0.y, y0.y, z0.y}};
+        p2g_flush_lane<float, CA>(S, c, ox, oy, hw, am, aq, MOM);
+    }
+}
+
 // Adds the tile (origin org) to the grid: one vector reduction per node that
 // received anything.
 template <typename T, int CA>
@@ -1241,9 +1368,10 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
 // One work item of k_g2p2g; P is the item's scene.  LAGGED: the F update
 // uses the B of the previous G2P (the reference's order), else the B just
 // gathered.
-template <typename T, bool TRACK_FP, bool LAGGED>
+template <typename T, bool TRACK_FP, bool LAGGED, bool PAIRS>
 __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
                                            const int4 it, bool has_next, int4 nit, const DevParams<T>* nscene) {
+    static_assert(!PAIRS || sizeof(T) == 4, "the record-pairs scatter is FP32");
     constexpr int CA = kBlk + 2;
     const vec4<T>* __restrict__ pin = static_cast<const vec4<T>*>(D.pin);
     vec4<T>* __restrict__ pout = static_cast<vec4<T>*>(D.pout);
@@ -1347,7 +1475,8 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             }
         }
         sort_ranked<T, CA>(S.p, j, rcell, rrank);
-        p2g_tasks<T, true, CA>(S.p, sorted_total(S.p));
+        if constexpr (PAIRS) p2g_runs_pairs<true, CA>(S.p, sorted_total(S.p));
+        else p2g_runs<T, true, CA>(S.p, sorted_total(S.p));
         __syncthreads();
         p2g_flush<T, CA>(P, S.p, porg, gnext);
         mark_around(P, D.gmark_next, it.x);
@@ -1356,8 +1485,9 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
 }
 
 // BATCH: the work items belong to different scenes (D.scenes); otherwise all
-// to the scene P0.
-template <typename T, bool TRACK_FP, bool BATCH, bool LAGGED>
+// to the scene P0.  PAIRS: the scatter's lane layout p2g_runs_pairs (FP32)
+// instead of p2g_runs; the autotuner picks one.
+template <typename T, bool TRACK_FP, bool BATCH, bool LAGGED, bool PAIRS = false>
 __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlocks : 1)
     k_g2p2g(DevParams<T> P0, DevBufs D) {
     extern __shared__ __align__(128) unsigned char smem_fused[];
@@ -1398,9 +1528,10 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
         const bool has_next = wn < nw;
         const int4 nit = has_next ? D.work[wn] : make_int4(0, 0, 0, 0);
         if constexpr (BATCH)
-            g2p2g_item<T, TRACK_FP, LAGGED>(S.par, D, S, it, has_next, nit, has_next ? &scenes[nit.w] : nullptr);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS>(S.par, D, S, it, has_next, nit,
+                                                   has_next ? &scenes[nit.w] : nullptr);
         else
-            g2p2g_item<T, TRACK_FP, LAGGED>(P0, D, S, it, has_next, nit, nullptr);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS>(P0, D, S, it, has_next, nit, nullptr);
     }
 }
 
