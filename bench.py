@@ -346,6 +346,7 @@ def measure_batched(pkg, local, steps, warmup, plain_value):
 
     reset()
     tune = b.autotune(dt, steps=5)
+    tune["candidates"] = b.tune_trials()
     reset()
     b.step(dt, warmup)
     stream = torch.cuda.ExternalStream(b.stream(), device=local)

@@ -321,20 +321,48 @@ rd_status rd_set_graphs(rd_handle* h, int enable);
 
 /* Autotuner: times `steps` steps of the current state (from the same saved
  * state each time) for each work-item size (FP32: 128, 192, 256 particles;
- * FP64: 64, 96, 128) and each persistent grid of 1 .. max resident CTAs per
- * SM of the fused kernel, keeps the fastest and restores the state (the next
- * step re-sorts and rebuilds the grid).  Allocates a copy of the particle
- * state for its duration. */
+ * FP64: 64, 96, 128), each persistent grid of 1 .. max resident CTAs per SM of
+ * the fused kernel and, for FP32 handles with the lagged-B order and without
+ * the full F_P, each scatter layout of its P2G (RD_SCATTER_*: how the 64
+ * stencil nodes of a record map to a warp's lanes); keeps the fastest and
+ * restores the state (the next step re-sorts and rebuilds the grid).
+ * Allocates a copy of the particle state for its duration.
+ * cache_path (may be NULL): a text file of earlier results, one per line
+ * "key<TAB>particles_per_item ctas_per_sm scatter ms_per_step", keyed by
+ * rd_tune_key (device architecture and SM count, precision, step options,
+ * scene count, particle count and grid size).  When the file holds the
+ * handle's key (the last such line counts), that choice is applied without
+ * timing anything (from_cache = 1); otherwise the search runs and its result
+ * is appended to the file. */
+enum { RD_SCATTER_LANE_PAIRS = 0,   /* a lane owns 2 nodes of one record; 32 lanes per record */
+       RD_SCATTER_RECORD_PAIRS = 1  /* a lane owns a 4-node column; the half-warps take 2 records of a run */ };
 typedef struct rd_tune_result {
     int32_t particles_per_item; /* chosen work-item size */
     int32_t ctas_per_sm;        /* chosen persistent CTAs per SM */
-    double ms_per_step;         /* measured for the chosen pair */
-    int32_t trials;             /* pairs timed */
+    double ms_per_step;         /* measured for the chosen point (or as cached) */
+    int32_t trials;             /* points timed (0 from the cache) */
+    int32_t scatter;            /* chosen RD_SCATTER_* */
+    int32_t from_cache;         /* 1: taken from cache_path */
 } rd_tune_result;
-rd_status rd_autotune(rd_handle* h, double dt, int32_t steps, rd_tune_result* result);
-/* Sets the pair by hand (0 = default: the largest item, max resident CTAs). */
-rd_status rd_set_tuning(rd_handle* h, int32_t particles_per_item, int32_t ctas_per_sm);
-rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas_per_sm);
+rd_status rd_autotune(rd_handle* h, double dt, int32_t steps, const char* cache_path, rd_tune_result* result);
+/* Every point the last rd_autotune timed, in the order timed (up to cap);
+ * *count receives how many there were. */
+typedef struct rd_tune_trial {
+    int32_t particles_per_item, ctas_per_sm, scatter;
+    double ms_per_step;
+} rd_tune_trial;
+rd_status rd_tune_trials(rd_handle* h, rd_tune_trial* out, int32_t cap, int32_t* count);
+/* The handle's cache key (NUL-terminated, no tabs or newlines). */
+rd_status rd_tune_key(rd_handle* h, char* buf, size_t len);
+/* The tuning cache file alone, no device involved: the last line of `path`
+ * with this key (*found = 0 when none, or when the file does not exist), and
+ * appending one line.  Malformed lines are skipped. */
+rd_status rd_tune_cache_get(const char* path, const char* key, rd_tune_result* out, int32_t* found);
+rd_status rd_tune_cache_put(const char* path, const char* key, const rd_tune_result* result);
+/* Sets the point by hand (0 = default: the largest item, max resident CTAs;
+ * scatter RD_SCATTER_*, RD_SCATTER_LANE_PAIRS where it is the only layout). */
+rd_status rd_set_tuning(rd_handle* h, int32_t particles_per_item, int32_t ctas_per_sm, int32_t scatter);
+rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas_per_sm, int32_t* scatter);
 
 /* ---- Reverse mode: gradients of a rollout ----
  * No counterpart in the reference.  rd_adjoint_record runs `steps` steps of

@@ -47,7 +47,8 @@ EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "
            "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort", "rd_debug_wait_timeout",
            "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_graph_replays", "rd_io_bytes", "rd_host_alloc", "rd_host_free", "rd_batch_create",
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
-           "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_set_tuning", "rd_get_tuning",
+           "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_tune_trials", "rd_tune_key", "rd_tune_cache_get",
+           "rd_tune_cache_put", "rd_set_tuning", "rd_get_tuning",
            "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
            "rd_set_colors", "rd_device_colors", "rd_splat", "rd_initialize_particles", "rd_get_diagnostics",
            "rd_rasterize_noalloc", "rd_rasterize_noalloc_flags")
@@ -163,7 +164,40 @@ class Grads(ctypes.Structure):
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("particles_per_item", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
-                ("ms_per_step", ctypes.c_double), ("trials", ctypes.c_int32)]
+                ("ms_per_step", ctypes.c_double), ("trials", ctypes.c_int32), ("scatter", ctypes.c_int32),
+                ("from_cache", ctypes.c_int32)]
+
+
+class TuneTrial(ctypes.Structure):
+    _fields_ = [("particles_per_item", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
+                ("scatter", ctypes.c_int32), ("ms_per_step", ctypes.c_double)]
+
+
+SCATTER_LANE_PAIRS, SCATTER_RECORD_PAIRS = 0, 1
+SCATTER_NAMES = {SCATTER_LANE_PAIRS: "lane_pairs", SCATTER_RECORD_PAIRS: "record_pairs"}
+
+
+def _tune_dict(r):
+    return {"particles_per_item": r.particles_per_item, "ctas_per_sm": r.ctas_per_sm, "ms_per_step": r.ms_per_step,
+            "trials": r.trials, "scatter": SCATTER_NAMES.get(r.scatter, r.scatter), "from_cache": bool(r.from_cache)}
+
+
+def tune_cache_get(path: str, key: str):
+    """rd_tune_cache_get: the cached point for `key` in the file, or None."""
+    r, found = TuneResult(), ctypes.c_int32(0)
+    st = lib().rd_tune_cache_get(os.fsencode(path), key.encode(), ctypes.byref(r), ctypes.byref(found))
+    if st != RD_OK:
+        raise RDError(st, "rd_tune_cache_get")
+    return _tune_dict(r) if found.value else None
+
+
+def tune_cache_put(path: str, key: str, particles_per_item: int, ctas_per_sm: int, scatter: int = 0,
+                   ms_per_step: float = 0.0):
+    """rd_tune_cache_put: appends one point for `key` to the file."""
+    r = TuneResult(int(particles_per_item), int(ctas_per_sm), float(ms_per_step), 0, int(scatter), 0)
+    st = lib().rd_tune_cache_put(os.fsencode(path), key.encode(), ctypes.byref(r))
+    if st != RD_OK:
+        raise RDError(st, "rd_tune_cache_put")
 
 
 def lib():
@@ -207,9 +241,15 @@ def lib():
             L.rd_batch_get_grid.argtypes = [vp, ctypes.c_int32, vp, vp, ctypes.c_int]
             L.rd_batch_step.argtypes = [vp, ctypes.c_double, ctypes.c_int32]
             L.rd_set_graphs.argtypes = [vp, ctypes.c_int]
-            L.rd_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.POINTER(TuneResult)]
-            L.rd_set_tuning.argtypes = [vp, ctypes.c_int32, ctypes.c_int32]
-            L.rd_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+            L.rd_autotune.argtypes = [vp, ctypes.c_double, ctypes.c_int32, ctypes.c_char_p, ctypes.POINTER(TuneResult)]
+            L.rd_tune_trials.argtypes = [vp, ctypes.POINTER(TuneTrial), ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+            L.rd_tune_key.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+            L.rd_tune_cache_get.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(TuneResult),
+                                            ctypes.POINTER(ctypes.c_int32)]
+            L.rd_tune_cache_put.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(TuneResult)]
+            L.rd_set_tuning.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+            L.rd_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                        ctypes.POINTER(ctypes.c_int32)]
             L.rd_get_diagnostics.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Diagnostics)]
             L.rd_initialize_particles.argtypes = [vp, ctypes.POINTER(InitSpec), ctypes.POINTER(ctypes.c_int32)]
             L.rd_set_colors.argtypes = [vp, vp, ctypes.c_int]
@@ -511,20 +551,38 @@ class Simulation:
     def set_graphs(self, enable: bool):
         self._check(lib().rd_set_graphs(self._h, int(enable)), "rd_set_graphs")
 
-    def autotune(self, dt: float, steps: int = 10) -> dict:
-        """rd_autotune: picks the work-item size and CTAs per SM by timing."""
+    def autotune(self, dt: float, steps: int = 10, cache: str | None = None) -> dict:
+        """rd_autotune: picks the work-item size, CTAs per SM and scatter layout
+        by timing, or from the cache file `cache` when it holds this handle's key."""
         r = TuneResult()
-        self._check(lib().rd_autotune(self._h, float(dt), int(steps), ctypes.byref(r)), "rd_autotune")
-        return {"particles_per_item": r.particles_per_item, "ctas_per_sm": r.ctas_per_sm,
-                "ms_per_step": r.ms_per_step, "trials": r.trials}
+        path = os.fsencode(cache) if cache else None
+        self._check(lib().rd_autotune(self._h, float(dt), int(steps), path, ctypes.byref(r)), "rd_autotune")
+        return _tune_dict(r)
 
-    def set_tuning(self, particles_per_item: int = 0, ctas_per_sm: int = 0):
-        self._check(lib().rd_set_tuning(self._h, int(particles_per_item), int(ctas_per_sm)), "rd_set_tuning")
+    def tune_trials(self) -> list:
+        """rd_tune_trials: every point the last autotune timed."""
+        n = ctypes.c_int32(0)
+        self._check(lib().rd_tune_trials(self._h, None, 0, ctypes.byref(n)), "rd_tune_trials")
+        arr = (TuneTrial * max(n.value, 1))()
+        self._check(lib().rd_tune_trials(self._h, arr, n.value, ctypes.byref(n)), "rd_tune_trials")
+        return [{"particles_per_item": t.particles_per_item, "ctas_per_sm": t.ctas_per_sm,
+                 "scatter": SCATTER_NAMES.get(t.scatter, t.scatter), "ms_per_step": t.ms_per_step}
+                for t in arr[:n.value]]
+
+    def tune_key(self) -> str:
+        buf = ctypes.create_string_buffer(512)
+        self._check(lib().rd_tune_key(self._h, buf, 512), "rd_tune_key")
+        return buf.value.decode()
+
+    def set_tuning(self, particles_per_item: int = 0, ctas_per_sm: int = 0, scatter: int = SCATTER_LANE_PAIRS):
+        self._check(lib().rd_set_tuning(self._h, int(particles_per_item), int(ctas_per_sm), int(scatter)),
+                    "rd_set_tuning")
 
     def tuning(self):
-        a, b = ctypes.c_int32(), ctypes.c_int32()
-        self._check(lib().rd_get_tuning(self._h, ctypes.byref(a), ctypes.byref(b)), "rd_get_tuning")
-        return a.value, b.value
+        """(particles per item, CTAs per SM, scatter layout)."""
+        a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._check(lib().rd_get_tuning(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)), "rd_get_tuning")
+        return a.value, b.value, c.value
 
 
 class Batch(Simulation):

@@ -273,6 +273,8 @@ struct rd_handle {
     void* d_tmaps = nullptr;        // CUtensorMap per grid buffer and scene, [2][nscenes]
     int wp = 0;         // particles per work item (<= WorkP)
     int grid_mult = 0;  // persistent CTAs per SM of the step kernels (0: occupancy)
+    int scatter = RD_SCATTER_LANE_PAIRS;     // lane layout of the fused kernel's P2G scatter
+    std::vector<rd_tune_trial> tune_trials;  // the points the last rd_autotune timed
     cudaStream_t stream = nullptr;
     int sms = 0;
     int n = 0;
@@ -568,8 +570,18 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
 // The k_g2p2g instantiation for this handle: batch or single scene, with or
 // without the full F_P, and the order of the F update.
 template <typename T> using FusedKernel = void (*)(DevParams<T>, DevBufs);
+// Scatter layouts a handle can use: both for FP32 with the lagged-B order and
+// J_P only (the instantiations the record-pairs layout is compiled for), else
+// the lane-pairs layout alone.
+int scatter_layouts(const rd_handle* h) {
+    return h->prm.precision == RD_FP32 && h->prm.lagged_b && !h->prm.track_fp ? 2 : 1;
+}
 template <typename T> FusedKernel<T> fused_kernel(const rd_handle* h) {
     const bool lag = h->prm.lagged_b != 0;
+    if constexpr (sizeof(T) == 4) {
+        if (h->scatter == RD_SCATTER_RECORD_PAIRS && scatter_layouts(h) > 1)
+            return batched(h) ? k_g2p2g<T, false, true, true, true> : k_g2p2g<T, false, false, true, true>;
+    }
     if (batched(h)) return lag ? k_g2p2g<T, false, true, true> : k_g2p2g<T, false, true, false>;
     if (h->prm.track_fp) return lag ? k_g2p2g<T, true, false, true> : k_g2p2g<T, true, false, false>;
     return lag ? k_g2p2g<T, false, false, true> : k_g2p2g<T, false, false, false>;
@@ -941,10 +953,24 @@ template <typename T> rd_status occupancy(rd_handle* h) {
     RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k_p2g<T, true, true, false>, kP2GThreads<T>, sm), "occ"));
     h->occ_p2g = std::max(1, o);
     const int fsm = (int)fused_smem_bytes<T>();
-    const void* used = (const void*)fused_kernel<T>(h);
-    RD_TRY(check_cuda(h, cudaFuncSetAttribute(used, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm), "smem attr"));
-    RD_TRY(check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, used, kFusedThreads, fsm), "occ"));
-    h->occ_g2p = std::max(1, o);
+    // every scatter layout the handle can switch to: the smallest occupancy
+    const int layout = h->scatter;
+    int occ = 0;
+    for (int l = 0; l < scatter_layouts(h); ++l) {
+        h->scatter = l;
+        const void* used = (const void*)fused_kernel<T>(h);
+        rd_status st = check_cuda(h, cudaFuncSetAttribute(used, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm),
+                                  "smem attr");
+        if (st == RD_OK)
+            st = check_cuda(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, used, kFusedThreads, fsm), "occ");
+        if (st != RD_OK) {
+            h->scatter = layout;
+            return st;
+        }
+        occ = l == 0 ? o : std::min(occ, o);
+    }
+    h->scatter = layout;
+    h->occ_g2p = std::max(1, occ);
     return RD_OK;
 }
 
@@ -1263,15 +1289,96 @@ template <typename T> rd_status steps_impl(rd_handle* h, double dt, int nsteps) 
     return RD_OK;
 }
 
-// Times the step under each candidate work-item size and persistent grid
-// (CTAs per SM) from the same saved state, keeps the fastest and puts the
-// state back as it was (the next step re-sorts and rebuilds the grid).
-template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps, rd_tune_result* res) {
+// Tuning cache: a text file of "key<TAB>particles_per_item ctas_per_sm
+// scatter ms_per_step" lines; the last line with a key counts.
+bool tune_key_ok(const char* key) {
+    if (!key || !*key) return false;
+    for (const char* c = key; *c; ++c)
+        if (*c == '\t' || *c == '\n' || *c == '\r') return false;
+    return true;
+}
+
+bool tune_cache_find(const char* path, const char* key, rd_tune_result* out) {
+    FILE* f = std::fopen(path, "r");
+    if (!f) return false;
+    const size_t klen = std::strlen(key);
+    bool found = false;
+    std::string line;
+    char buf[512];
+    while (std::fgets(buf, sizeof buf, f)) {
+        line += buf;
+        if (line.back() != '\n' && !std::feof(f)) continue;  // a line longer than the buffer: read on
+        if (line.size() > klen && line.compare(0, klen, key) == 0 && line[klen] == '\t') {
+            int a = 0, b = 0, c = 0;
+            double ms = 0.0;
+            char tail = 0;
+            const int got = std::sscanf(line.c_str() + klen + 1, "%d %d %d %lf %c", &a, &b, &c, &ms, &tail);
+            if (got == 4 && a >= 0 && b >= 0 && (c == RD_SCATTER_LANE_PAIRS || c == RD_SCATTER_RECORD_PAIRS) &&
+                std::isfinite(ms)) {
+                *out = rd_tune_result{a, b, ms, 0, c, 1};
+                found = true;
+            }
+        }
+        line.clear();
+    }
+    std::fclose(f);
+    return found;
+}
+
+// Device architecture and SM count, precision, step options, scene count,
+// particle count, grid nodes and the largest grid of any scene.
+std::string tune_key_of(const rd_handle* h) {
+    int major = 0, minor = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, h->prm.device);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, h->prm.device);
+    int64_t particles = 0, nodes = 0;
+    int gmax[3] = {0, 0, 0};
+    const size_t nsc = std::max<size_t>(1, h->scenes.size());
+    for (size_t s = 0; s < nsc; ++s) {
+        const rd_params& p = h->scenes.empty() ? h->prm : h->scenes[s].prm;
+        particles += p.num_particles;
+        nodes += (int64_t)p.max_i * p.max_j * p.max_k;
+        gmax[0] = std::max(gmax[0], p.max_i);
+        gmax[1] = std::max(gmax[1], p.max_j);
+        gmax[2] = std::max(gmax[2], p.max_k);
+    }
+    char buf[256];
+    std::snprintf(buf, sizeof buf, "sm%d%d sms%d %s lagged%d trackfp%d scenes%zu particles%lld nodes%lld grid%dx%dx%d",
+                  major, minor, h->sms, h->prm.precision == RD_FP64 ? "fp64" : "fp32", h->prm.lagged_b ? 1 : 0,
+                  h->prm.track_fp ? 1 : 0, nsc, (long long)particles, (long long)nodes, gmax[0], gmax[1], gmax[2]);
+    return buf;
+}
+
+// Whether a cached point fits this handle.
+template <typename T> bool tune_point_ok(const rd_handle* h, const rd_tune_result& r) {
+    const int wmax = WorkP<T>::value;
+    return (r.particles_per_item == 0 || (r.particles_per_item >= wmax / 4 && r.particles_per_item <= wmax)) &&
+           r.ctas_per_sm <= h->occ_g2p && r.scatter < scatter_layouts(h);
+}
+
+// Times the step under each candidate work-item size, persistent grid (CTAs
+// per SM) and scatter layout from the same saved state, keeps the fastest and
+// puts the state back as it was (the next step re-sorts and rebuilds the grid).
+template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps, const char* cache_path,
+                                              rd_tune_result* res) {
     NvtxRange range("rd_autotune");
     const int wps_f[] = {128, 192, 256}, wps_d[] = {64, 96, 128};
     const int* wps = sizeof(T) == 4 ? wps_f : wps_d;
-    rd_tune_result best{WorkP<T>::value, 0, 0.0, 0};
+    rd_tune_result best{WorkP<T>::value, 0, 0.0, 0, RD_SCATTER_LANE_PAIRS, 0};
+    h->tune_trials.clear();
     if (h->n == 0) { *res = best; return RD_OK; }
+    const std::string key = tune_key_of(h);
+    if (cache_path) {
+        rd_tune_result hit;
+        if (tune_cache_find(cache_path, key.c_str(), &hit) && tune_point_ok<T>(h, hit)) {
+            h->wp = hit.particles_per_item;
+            h->grid_mult = hit.ctas_per_sm;
+            h->scatter = hit.scatter;
+            drop_graphs(h);
+            *res = hit;
+            return RD_OK;
+        }
+    }
     const size_t bytes = (size_t)h->planes * h->n * 4 * h->esize;
     void* saved = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1295,44 +1402,53 @@ template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps
     if (st == RD_OK) st = check_cuda(h, cudaEventCreate(&e1), "event");
     if (st == RD_OK)
         st = check_cuda(h, cudaMemcpyAsync(saved, h->pl[h->cur], bytes, cudaMemcpyDeviceToDevice, h->stream), "save");
-    const int old_wp = h->wp, old_mult = h->grid_mult;
+    const int old_wp = h->wp, old_mult = h->grid_mult, old_scatter = h->scatter;
     float best_ms = 0.f;
-    for (int a = 0; a < 3 && st == RD_OK; ++a)
-        for (int c = 1; c <= h->occ_g2p && st == RD_OK; ++c) {
-            h->wp = wps[a];
-            h->grid_mult = c;
-            drop_graphs(h);
-            if ((st = restore()) != RD_OK) break;
-            // two eager steps (sort, P2G), then one captured pair, untimed
-            if ((st = steps_impl<T>(h, dt, 2)) != RD_OK) break;
-            if ((st = steps_impl<T>(h, dt, 2)) != RD_OK) break;
-            if ((st = check_cuda(h, cudaEventRecord(e0, h->stream), "event")) != RD_OK) break;
-            if ((st = steps_impl<T>(h, dt, steps)) != RD_OK) break;
-            if ((st = check_cuda(h, cudaEventRecord(e1, h->stream), "event")) != RD_OK) break;
-            if ((st = check_cuda(h, cudaEventSynchronize(e1), "event sync")) != RD_OK) break;
-            float ms = 0.f;
-            if ((st = check_cuda(h, cudaEventElapsedTime(&ms, e0, e1), "event time")) != RD_OK) break;
-            ++best.trials;
-            if (best.trials == 1 || ms < best_ms) {
-                best_ms = ms;
-                best.particles_per_item = wps[a];
-                best.ctas_per_sm = c;
+    for (int l = 0; l < scatter_layouts(h) && st == RD_OK; ++l)
+        for (int a = 0; a < 3 && st == RD_OK; ++a)
+            for (int c = 1; c <= h->occ_g2p && st == RD_OK; ++c) {
+                h->wp = wps[a];
+                h->grid_mult = c;
+                h->scatter = l;
+                drop_graphs(h);
+                if ((st = restore()) != RD_OK) break;
+                // two eager steps (sort, P2G), then one captured pair, untimed
+                if ((st = steps_impl<T>(h, dt, 2)) != RD_OK) break;
+                if ((st = steps_impl<T>(h, dt, 2)) != RD_OK) break;
+                if ((st = check_cuda(h, cudaEventRecord(e0, h->stream), "event")) != RD_OK) break;
+                if ((st = steps_impl<T>(h, dt, steps)) != RD_OK) break;
+                if ((st = check_cuda(h, cudaEventRecord(e1, h->stream), "event")) != RD_OK) break;
+                if ((st = check_cuda(h, cudaEventSynchronize(e1), "event sync")) != RD_OK) break;
+                float ms = 0.f;
+                if ((st = check_cuda(h, cudaEventElapsedTime(&ms, e0, e1), "event time")) != RD_OK) break;
+                ++best.trials;
+                h->tune_trials.push_back(rd_tune_trial{wps[a], c, l, (double)ms / steps});
+                if (best.trials == 1 || ms < best_ms) {
+                    best_ms = ms;
+                    best.particles_per_item = wps[a];
+                    best.ctas_per_sm = c;
+                    best.scatter = l;
+                }
             }
-        }
     if (st != RD_OK) {
         h->wp = old_wp;
         h->grid_mult = old_mult;
+        h->scatter = old_scatter;
         drop_graphs(h);
         if (saved) restore();
         return cleanup(st);
     }
     h->wp = best.particles_per_item;
     h->grid_mult = best.ctas_per_sm;
-    best.ms_per_step = steps > 0 ? best_ms / steps : 0.0;
+    h->scatter = best.scatter;
+    best.ms_per_step = best_ms / steps;
     drop_graphs(h);
     st = restore();
     *res = best;
-    return cleanup(st);
+    st = cleanup(st);
+    if (st == RD_OK && cache_path && rd_tune_cache_put(cache_path, key.c_str(), &best) != RD_OK)
+        st = fail(h, RD_INVALID_ARG, "tuning cache: could not append to the file");
+    return st;
 }
 
 // ---------------------------------------------------------------- adjoint
@@ -2003,31 +2119,69 @@ rd_status rd_step(rd_handle* h, double dt, int32_t nsteps) {
     return RD_DISPATCH(h, steps_impl, h, dt, nsteps);
 }
 
-rd_status rd_autotune(rd_handle* h, double dt, int32_t steps, rd_tune_result* result) {
+rd_status rd_autotune(rd_handle* h, double dt, int32_t steps, const char* cache_path, rd_tune_result* result) {
     if (!h || !result || steps < 1 || !std::isfinite(dt)) return RD_INVALID_ARG;
     if (!all_set(h)) return fail(h, RD_INVALID_ARG, "every scene needs its particles first");
     ++h->version;
     cudaSetDevice(h->prm.device);
-    return RD_DISPATCH(h, autotune_impl, h, dt, steps, result);
+    return RD_DISPATCH(h, autotune_impl, h, dt, steps, cache_path, result);
 }
 
-rd_status rd_set_tuning(rd_handle* h, int32_t particles_per_item, int32_t ctas_per_sm) {
-    if (!h || particles_per_item < 0 || ctas_per_sm < 0) return RD_INVALID_ARG;
+rd_status rd_tune_trials(rd_handle* h, rd_tune_trial* out, int32_t cap, int32_t* count) {
+    if (!h || !count || cap < 0 || (cap > 0 && !out)) return RD_INVALID_ARG;
+    const int32_t n = (int32_t)std::min<size_t>((size_t)cap, h->tune_trials.size());
+    for (int32_t i = 0; i < n; ++i) out[i] = h->tune_trials[i];
+    *count = (int32_t)h->tune_trials.size();
+    return RD_OK;
+}
+
+rd_status rd_tune_key(rd_handle* h, char* buf, size_t len) {
+    if (!h || !buf || len == 0) return RD_INVALID_ARG;
+    const std::string k = tune_key_of(h);
+    if (k.size() + 1 > len) return RD_TOO_LARGE;
+    std::memcpy(buf, k.c_str(), k.size() + 1);
+    return RD_OK;
+}
+
+rd_status rd_tune_cache_get(const char* path, const char* key, rd_tune_result* out, int32_t* found) {
+    if (!path || !out || !found || !tune_key_ok(key)) return RD_INVALID_ARG;
+    *found = tune_cache_find(path, key, out) ? 1 : 0;
+    return RD_OK;
+}
+
+rd_status rd_tune_cache_put(const char* path, const char* key, const rd_tune_result* r) {
+    if (!path || !r || !tune_key_ok(key) || r->particles_per_item < 0 || r->ctas_per_sm < 0 ||
+        (r->scatter != RD_SCATTER_LANE_PAIRS && r->scatter != RD_SCATTER_RECORD_PAIRS) ||
+        !std::isfinite(r->ms_per_step))
+        return RD_INVALID_ARG;
+    FILE* f = std::fopen(path, "a");
+    if (!f) return RD_INVALID_ARG;
+    const int ok = std::fprintf(f, "%s\t%d %d %d %.9g\n", key, r->particles_per_item, r->ctas_per_sm, r->scatter,
+                                r->ms_per_step);
+    return (std::fclose(f) == 0 && ok > 0) ? RD_OK : RD_INVALID_ARG;
+}
+
+rd_status rd_set_tuning(rd_handle* h, int32_t particles_per_item, int32_t ctas_per_sm, int32_t scatter) {
+    if (!h || particles_per_item < 0 || ctas_per_sm < 0 ||
+        (scatter != RD_SCATTER_LANE_PAIRS && scatter != RD_SCATTER_RECORD_PAIRS))
+        return RD_INVALID_ARG;
     const int wmax = h->prm.precision == RD_FP64 ? WorkP<double>::value : WorkP<float>::value;
     if (particles_per_item != 0 && (particles_per_item < wmax / 4 || particles_per_item > wmax))
         return fail(h, RD_INVALID_ARG, "particles per item out of range");
     cudaSetDevice(h->prm.device);
     h->wp = particles_per_item;
     h->grid_mult = ctas_per_sm;
+    h->scatter = scatter < scatter_layouts(h) ? scatter : RD_SCATTER_LANE_PAIRS;
     drop_graphs(h);
     return RD_OK;
 }
 
-rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas_per_sm) {
-    if (!h || !particles_per_item || !ctas_per_sm) return RD_INVALID_ARG;
+rd_status rd_get_tuning(rd_handle* h, int32_t* particles_per_item, int32_t* ctas_per_sm, int32_t* scatter) {
+    if (!h || !particles_per_item || !ctas_per_sm || !scatter) return RD_INVALID_ARG;
     const int wmax = h->prm.precision == RD_FP64 ? WorkP<double>::value : WorkP<float>::value;
     *particles_per_item = h->wp > 0 ? std::min(h->wp, wmax) : wmax;
     *ctas_per_sm = h->grid_mult > 0 ? std::min(h->grid_mult, h->occ_g2p) : h->occ_g2p;
+    *scatter = h->scatter;
     return RD_OK;
 }
 

@@ -130,8 +130,13 @@ def test_autotune_picks_a_valid_pair_and_restores_state(built_pkg):
     ref = make_batch(built_pkg, batch)
     r = tuned.autotune(dt, steps=4)
     assert r["particles_per_item"] in (128, 192, 256)
-    assert r["trials"] >= 3 and r["ms_per_step"] > 0
-    assert tuned.tuning() == (r["particles_per_item"], r["ctas_per_sm"])
+    assert r["trials"] >= 6 and r["ms_per_step"] > 0 and not r["from_cache"]
+    trials = tuned.tune_trials()
+    assert len(trials) == r["trials"]
+    assert {t["scatter"] for t in trials} == {"lane_pairs", "record_pairs"}
+    assert min(t["ms_per_step"] for t in trials) == pytest.approx(r["ms_per_step"])
+    layout = {"lane_pairs": built_pkg.SCATTER_LANE_PAIRS, "record_pairs": built_pkg.SCATTER_RECORD_PAIRS}
+    assert tuned.tuning() == (r["particles_per_item"], r["ctas_per_sm"], layout[r["scatter"]])
     tuned.step(dt, 5)
     ref.step(dt, 5)
     for s in range(len(batch)):
@@ -140,12 +145,31 @@ def test_autotune_picks_a_valid_pair_and_restores_state(built_pkg):
             assert rel(a[k], c[k]) < 1e-5, (s, k)
 
 
-@pytest.mark.parametrize("wp", [64, 128, 192])
-def test_item_size_does_not_change_results(built_pkg, orc, wp):
+def test_autotune_cache_round_trip(built_pkg, tmp_path):
+    """A tuned point goes to the cache file under the handle's key; a second
+    handle of the same scenes takes it from there without timing."""
+    batch = small_batch(seed=10, nscenes=3)
+    dt = batch[0].dt
+    cache = str(tmp_path / "tune.txt")
+    first = make_batch(built_pkg, batch)
+    r1 = first.autotune(dt, steps=3, cache=cache)
+    assert not r1["from_cache"] and r1["trials"] > 0
+    second = make_batch(built_pkg, batch)
+    assert second.tune_key() == first.tune_key()
+    r2 = second.autotune(dt, steps=3, cache=cache)
+    assert r2["from_cache"] and r2["trials"] == 0 and second.tune_trials() == []
+    for k in ("particles_per_item", "ctas_per_sm", "scatter"):
+        assert r2[k] == r1[k], k
+    assert second.tuning() == first.tuning()
+
+
+@pytest.mark.parametrize("wp,scatter", [(64, 0), (128, 0), (192, 0), (128, 1), (256, 1)])
+def test_item_size_and_scatter_layout_do_not_change_results(built_pkg, orc, wp, scatter):
     from rd_gb300 import scenes
     sc = scenes.snowball(seed=8, n=5000, grid=32)
     s = built_pkg.Simulation(scene_params(built_pkg, sc))
-    s.set_tuning(wp, 1)
+    s.set_tuning(wp, 1, scatter)
+    assert s.tuning()[2] == scatter
     s.set_particles(sc.x, sc.v, sc.mass)
     s.init_volumes()
     o = oracle_of(orc, sc)
