@@ -14,7 +14,8 @@ inputs.
   64-scene batch stepped together in one handle, each against its own oracle.
 * cube: the 65,536-particle, 50-step, checkpoint-every-10 rollout of the
   gradient workload in the FP64 build, reverse-mode dL/dv0 along two random
-  directions and dL/dE, dL/dnu against central finite differences at 1e-4.
+  directions against central finite differences at 1e-4, and dL/dv0 and dL/dE
+  of a per-particle weighted loss on the same rollout.
 
 Errors are norm-wise, ||gpu - ref|| / ||ref||; B is measured against its
 natural scale ||v|| h because it vanishes for a rigid translation."""
@@ -143,51 +144,73 @@ def test_uneven_batch_extremes_match_oracle(built_pkg, orc):
         assert all(e < (1e-6 if k == "grid_mass" else TOL1) for k, e in errs.items()), (pick[s], sc.n, errs)
 
 
-def cube_loss(pkg, sc, v0, grads, **mat):
-    target = np.array([0.55, 0.3, 0.5])
+def cube_rollout(pkg, sc, v0, grad_fn, **mat):
+    """The cube's 50-step, checkpoint-every-10 FP64 rollout from v0; returns the
+    final positions and, when grad_fn (dL/dx_T of the positions) is given, the
+    gradients."""
     sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, precision=pkg.RD_FP64, **sc.params(**mat)))
     sim.set_particles(sc.x.astype(np.float64), v0, sc.mass.astype(np.float64))
     sim.init_volumes()
     sim.adjoint_record(sc.dt, sc.steps, 10)
     xT = sim.get_particles(("x",))["x"].astype(np.float64)
-    cen = xT.mean(0)
-    loss = float(np.sum((cen - target) ** 2))
-    g = None
-    if grads:
-        gx = np.tile(2.0 * (cen - target) / sc.n, (sc.n, 1))
-        g = sim.adjoint_backward(gx)
+    g = sim.adjoint_backward(grad_fn(xT)) if grad_fn is not None else None
     assert sim.flags() == 0
     sim.close()
-    return loss, g
+    return xT, g
+
+
+TARGET = np.array([0.55, 0.3, 0.5])
+
+
+def centroid_loss(xT):
+    return float(np.sum((xT.mean(0) - TARGET) ** 2))
+
+
+def centroid_grad(xT):
+    return np.tile(2.0 * (xT.mean(0) - TARGET) / len(xT), (len(xT), 1))
 
 
 def test_cube_rollout_gradient_matches_central_differences_fp64(built_pkg):
     """The 65,536-particle cube, 64^3, 50 steps, checkpoint every 10, loss
-    ||centroid(x_T) - (0.55, 0.3, 0.5)||^2, in the FP64 build.  The initial
+    ||centroid(x_T) - (0.55, 0.3, 0.5)||^2, in the FP64 build: dL/dv0 along
+    two random directions against central differences.  The initial
     velocities carry a random field (the workload starts at rest, where every
     particle moves alike) so the stress, the plastic split and the grid all
-    carry gradient; F_E starts at the identity, the all-tie case of the
-    singular-value backward."""
+    act; F_E starts at the identity, the all-tie case of the singular-value
+    backward.  Internal forces conserve momentum and move no centroid, so this
+    loss does not depend on E or nu (the reverse pass gives ~1e-27 there); a
+    second loss, sum_i c_i . x_T,i / N with random c, weighs every particle
+    differently and is checked along v0 and E."""
     from rd_gb300 import scenes
     sc = scenes.cube()
     assert (sc.n, sc.grid, sc.steps) == (65536, (64, 64, 64), 50)
     rng = np.random.default_rng(5)
     v0 = sc.v.astype(np.float64) + rng.normal(0.0, 0.5, (sc.n, 3))
-    L0, g = cube_loss(built_pkg, sc, v0, True)
+    xT0, g = cube_rollout(built_pkg, sc, v0, centroid_grad)
     assert np.all(np.isfinite(g["v0"]))
+    # the loss is smooth to ~1e-7 relative over steps of 1e-4..1e-3 here;
+    # below 1e-5 the rounding of the 50-step rollout dominates the quotient
+    eps = 1e-4
     for k in range(2):
         e = rng.normal(size=v0.shape)
-        # the loss is smooth to ~1e-7 relative over 1e-4..1e-3 here; below 1e-5 the
-        # rounding of the 50-step rollout dominates the difference quotient
-        eps = 1e-4
-        fd = (cube_loss(built_pkg, sc, v0 + eps * e, False)[0] - cube_loss(built_pkg, sc, v0 - eps * e, False)[0]) / (2 * eps)
+        fd = (centroid_loss(cube_rollout(built_pkg, sc, v0 + eps * e, None)[0]) -
+              centroid_loss(cube_rollout(built_pkg, sc, v0 - eps * e, None)[0])) / (2 * eps)
         ad = float(np.sum(g["v0"] * e))
         assert abs(fd - ad) <= 1e-4 * max(abs(fd), abs(ad)), (k, fd, ad)
-    for name, eps in (("E", 1.0), ("nu", 1e-6)):
-        base = sc.material[name]
-        lp = cube_loss(built_pkg, sc, v0, False, **{name: base + eps})[0]
-        lm = cube_loss(built_pkg, sc, v0, False, **{name: base - eps})[0]
-        fd = (lp - lm) / (2 * eps)
-        ad = float(g[name][0])
-        assert ad != 0.0, name
-        assert abs(fd - ad) <= 1e-4 * max(abs(fd), abs(ad)), (name, fd, ad)
+    assert abs(g["E"][0]) * sc.material["E"] < 1e-9 * centroid_loss(xT0)
+    c = rng.normal(size=v0.shape)
+
+    def wloss(xT):
+        return float(np.sum(c * xT)) / sc.n
+
+    _, gw = cube_rollout(built_pkg, sc, v0, lambda xT: c / sc.n)
+    e = rng.normal(size=v0.shape)
+    fd = (wloss(cube_rollout(built_pkg, sc, v0 + eps * e, None)[0]) -
+          wloss(cube_rollout(built_pkg, sc, v0 - eps * e, None)[0])) / (2 * eps)
+    ad = float(np.sum(gw["v0"] * e))
+    assert abs(fd - ad) <= 1e-4 * max(abs(fd), abs(ad)), ("v0, weighted loss", fd, ad)
+    dE = 1e-4 * sc.material["E"]
+    fd = (wloss(cube_rollout(built_pkg, sc, v0, None, E=sc.material["E"] + dE)[0]) -
+          wloss(cube_rollout(built_pkg, sc, v0, None, E=sc.material["E"] - dE)[0])) / (2 * dE)
+    ad = float(gw["E"][0])
+    assert abs(fd - ad) <= 1e-4 * max(abs(fd), abs(ad)), ("E, weighted loss", fd, ad)
