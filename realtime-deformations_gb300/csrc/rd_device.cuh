@@ -268,6 +268,18 @@ __device__ __forceinline__ float rsqrt_acc(float x) {
 __device__ __forceinline__ double rsqrt_acc(double x) { return 1.0 / sqrt(x); }
 __device__ __forceinline__ float div_fast(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double div_fast(double a, double b) { return a / b; }
+// Reciprocal within about an ulp in FP32 (the hardware approximation, no
+// IEEE rounding step); exact division in FP64.
+__device__ __forceinline__ float rcp_fast(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double rcp_fast(double x) { return 1.0 / x; }
+// Square root for a Jacobi rotation angle, which only needs to be close:
+// the hardware approximation in FP32.
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ double sqrt_approx(double x) { return sqrt(x); }
 
 // SVD of an F that is close to a rotation (the elastic F_E of the snow model
 // stays within the plasticity clamp): F = U diag(s) V^T together with s - 1
@@ -321,7 +333,7 @@ __device__ __forceinline__ void svd3_near(const T F[9], T U[9], T s[3], T sm1[3]
             if (abs_(apq) > tol) {
                 rotated = true;
                 const T theta = div_fast(A[q][q] - A[p][p], T(2) * apq);
-                const T t = div_fast(copysign(T(1), theta), abs_(theta) + sqrt_(fma(theta, theta, T(1))));
+                const T t = div_fast(copysign(T(1), theta), abs_(theta) + sqrt_approx(fma(theta, theta, T(1))));
                 const T c = rsqrt_acc(fma(t, t, T(1)));
                 const T sn = t * c;
                 const T tau = div_fast(sn, T(1) + c);
@@ -345,8 +357,8 @@ __device__ __forceinline__ void svd3_near(const T F[9], T U[9], T s[3], T sm1[3]
     for (int c = 0; c < 3; ++c) {
         const T e = A[c][c];
         s[c] = sqrt_(T(1) + e);
-        sm1[c] = e / (T(1) + s[c]);
-        const T inv = T(1) / s[c];
+        sm1[c] = e * rcp_fast(T(1) + s[c]);
+        const T inv = rcp_fast(s[c]);
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
             V[3 * r + c] = v[r][c];

@@ -1321,11 +1321,25 @@ __device__ __forceinline__ void g2p_gather(const vec4<T>* __restrict__ gv, const
         for (int oy = 0; oy < 4; ++oy) {
             T col[3] = {T(0), T(0), T(0)}, colz[3] = {T(0), T(0), T(0)};
             const int rowc = ((St.rel[0] + ox) * kTile + (St.rel[1] + oy)) * kTile + St.rel[2];
+            if constexpr (sizeof(T) == 4) {
+                // (sum wz v, sum wz dz v) of each velocity component as one pair
+                float2 c0 = make_float2(0.f, 0.f), c1 = c0, c2 = c0;
 #pragma unroll
-            for (int oz = 0; oz < 4; ++oz) {
-                const vec4<T> v = gv[rowc + oz];
-                col[0] += St.w[2][oz] * v.x; col[1] += St.w[2][oz] * v.y; col[2] += St.w[2][oz] * v.z;
-                colz[0] += wzd[oz] * v.x; colz[1] += wzd[oz] * v.y; colz[2] += wzd[oz] * v.z;
+                for (int oz = 0; oz < 4; ++oz) {
+                    const vec4<T> v = gv[rowc + oz];
+                    const float2 wz2 = make_float2(St.w[2][oz], wzd[oz]);
+                    c0 = __ffma2_rn(wz2, make_float2(v.x, v.x), c0);
+                    c1 = __ffma2_rn(wz2, make_float2(v.y, v.y), c1);
+                    c2 = __ffma2_rn(wz2, make_float2(v.z, v.z), c2);
+                }
+                col[0] = c0.x; colz[0] = c0.y; col[1] = c1.x; colz[1] = c1.y; col[2] = c2.x; colz[2] = c2.y;
+            } else {
+#pragma unroll
+                for (int oz = 0; oz < 4; ++oz) {
+                    const vec4<T> v = gv[rowc + oz];
+                    col[0] += St.w[2][oz] * v.x; col[1] += St.w[2][oz] * v.y; col[2] += St.w[2][oz] * v.z;
+                    colz[0] += wzd[oz] * v.x; colz[1] += wzd[oz] * v.y; colz[2] += wzd[oz] * v.z;
+                }
             }
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
@@ -1360,9 +1374,12 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
     stress_from_split(P, sp, p.Jp, P.fscale * (p.vol * P.dinv), G6);
     store_particle_back(pout, n, s, p);
     if (TRACK_FP) store_fp(pout, n, s, FP);
-    finite = isfinite(p.Jp);
+    // a NaN or infinity anywhere makes the sum non-finite (the values are far
+    // from overflowing)
+    T sum = p.Jp;
 #pragma unroll
-    for (int e = 0; e < 9; ++e) finite = finite && isfinite(p.F[e]);
+    for (int e = 0; e < 9; ++e) sum += p.F[e];
+    finite = isfinite(sum);
 }
 
 // One work item of k_g2p2g; P is the item's scene.  LAGGED: the F update
@@ -1398,9 +1415,10 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             T v0 = T(0), v1 = T(0), v2 = T(0);
             const vec4<T> g4 = S.graw[c];
             if (g4.x != T(0)) {
-                v0 = g4.y / g4.x + P.dt * P.g[0];
-                v1 = g4.z / g4.x + P.dt * P.g[1];
-                v2 = g4.w / g4.x + P.dt * P.g[2];
+                const T im = rcp_fast(g4.x);
+                v0 = g4.y * im + P.dt * P.g[0];
+                v1 = g4.z * im + P.dt * P.g[1];
+                v2 = g4.w * im + P.dt * P.g[2];
                 const int ix = c / (kTile * kTile), iy = (c / kTile) % kTile, iz = c % kTile;
                 if (P.bc == 1 && wall_node(P, org[0] + ix, org[1] + iy, org[2] + iz)) v0 = v1 = v2 = T(0);
                 if (P.ncol) {
@@ -1443,10 +1461,12 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
 #pragma unroll
             for (int a = 0; a < 3; ++a) p.x[a] = clampx(p.x[a] + p.v[a] * P.dt, P.xlo, P.xhi[a]);
             store_particle_front(pout, n, s, p);
-            finite = finite && isfinite(p.x[0]) && isfinite(p.x[1]) && isfinite(p.x[2]) && isfinite(p.v[0]) &&
-                     isfinite(p.v[1]) && isfinite(p.v[2]);
+            {
+                T sum = (p.x[0] + p.x[1]) + (p.x[2] + p.v[0]) + (p.v[1] + p.v[2]);
 #pragma unroll
-            for (int e = 0; e < 9; ++e) finite = finite && isfinite(p.B[e]);
+                for (int e = 0; e < 9; ++e) sum += p.B[e];
+                finite = finite && isfinite(sum);
+            }
             if (!finite) raise_flag(D.flags, 2u);
             // next step's P2G record
             Stencil<T> S2;
