@@ -504,8 +504,9 @@ __device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T
                                          Split<T>& sp, T* s_out = nullptr, T* sm1_out = nullptr,
                                          T* V_out = nullptr) {
     T A[9];
+    const T ddt = P.dinv * P.dt;
 #pragma unroll
-    for (int e = 0; e < 9; ++e) A[e] = Bm[e] * P.dinv * P.dt;
+    for (int e = 0; e < 9; ++e) A[e] = Bm[e] * ddt;
     A[0] += T(1); A[4] += T(1); A[8] += T(1);
     T Fs[9];
     matmul3(Fs, A, F);
@@ -529,13 +530,19 @@ __device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T
             sp.scm1[c] = sm1[c];
         }
     }
-    sp.sgn = (det3(sp.U) * det3(V) < T(0)) ? T(-1) : T(1);
+    sp.sgn = det3(Fs) < T(0) ? T(-1) : T(1);
+    if (!(s[0] < P.lo || s[0] > P.hi || s[1] < P.lo || s[1] > P.hi || s[2] < P.lo || s[2] > P.hi)) {
+        // nothing clamped: U S V^T is F* itself
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
+        for (int e = 0; e < 9; ++e) F[e] = Fs[e];
+    } else {
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-            F[3 * r + c] = sp.U[3 * r] * sp.sc[0] * V[3 * c] + sp.U[3 * r + 1] * sp.sc[1] * V[3 * c + 1] +
-                           sp.U[3 * r + 2] * sp.sc[2] * V[3 * c + 2];
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                F[3 * r + c] = sp.U[3 * r] * sp.sc[0] * V[3 * c] + sp.U[3 * r + 1] * sp.sc[1] * V[3 * c + 1] +
+                               sp.U[3 * r + 2] * sp.sc[2] * V[3 * c + 2];
+    }
     Jp = Jp * ratio;
     if (TRACK_FP) {
         T r[3], Mv[9], out[9];
@@ -1385,7 +1392,7 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
 // One work item of k_g2p2g; P is the item's scene.  LAGGED: the F update
 // uses the B of the previous G2P (the reference's order), else the B just
 // gathered.
-template <typename T, bool TRACK_FP, bool LAGGED, bool PAIRS>
+template <typename T, bool TRACK_FP, bool LAGGED, bool PAIRS, bool END_BARRIER>
 __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
                                            const int4 it, bool has_next, int4 nit, const DevParams<T>* nscene) {
     static_assert(!PAIRS || sizeof(T) == 4, "the record-pairs scatter is FP32");
@@ -1411,6 +1418,10 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         }
         // the (m, p) tile arrived by TMA (nodes outside the grid read as
         // zero): the grid update, walls and colliders into velocities
+        // a tile clear of the sticky walls (most of them) skips the per-node test
+        const int bw = P.bc_width;
+        const bool walls = P.bc == 1 && (org[0] < bw || org[1] < bw || org[2] < bw || org[0] + kTile > P.M[0] - bw ||
+                                         org[1] + kTile > P.M[1] - bw || org[2] + kTile > P.M[2] - bw);
         for (int c = threadIdx.x; c < kTileCells; c += blockDim.x) {
             T v0 = T(0), v1 = T(0), v2 = T(0);
             const vec4<T> g4 = S.graw[c];
@@ -1420,7 +1431,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
                 v1 = g4.z * im + P.dt * P.g[1];
                 v2 = g4.w * im + P.dt * P.g[2];
                 const int ix = c / (kTile * kTile), iy = (c / kTile) % kTile, iz = c % kTile;
-                if (P.bc == 1 && wall_node(P, org[0] + ix, org[1] + iy, org[2] + iz)) v0 = v1 = v2 = T(0);
+                if (walls && wall_node(P, org[0] + ix, org[1] + iy, org[2] + iz)) v0 = v1 = v2 = T(0);
                 if (P.ncol) {
                     T vv[3] = {v0, v1, v2};
                     collide_node(P, static_cast<const Collider<T>*>(D.colliders), (T)(org[0] + ix) * P.h,
@@ -1500,7 +1511,10 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         __syncthreads();
         p2g_flush<T, CA>(P, S.p, porg, gnext);
         mark_around(P, D.gmark_next, it.x);
-        __syncthreads();
+        // a single scene: the next item's first barrier (after its tile wait)
+        // separates this flush from the next item's writes to shared memory; a
+        // batch copies the next scene's parameters before that barrier
+        if (END_BARRIER) __syncthreads();
     }
 }
 
@@ -1548,10 +1562,10 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
         const bool has_next = wn < nw;
         const int4 nit = has_next ? D.work[wn] : make_int4(0, 0, 0, 0);
         if constexpr (BATCH)
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS>(S.par, D, S, it, has_next, nit,
-                                                   has_next ? &scenes[nit.w] : nullptr);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, true>(S.par, D, S, it, has_next, nit,
+                                                         has_next ? &scenes[nit.w] : nullptr);
         else
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS>(P0, D, S, it, has_next, nit, nullptr);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, false>(P0, D, S, it, has_next, nit, nullptr);
     }
 }
 
