@@ -296,7 +296,8 @@ def measure_link(local, nbytes=1 << 30, reps=3):
 
 def measure_snowball(pkg, local, warmup):
     """The 8,192-particle snowball on 64^3 for its 200 steps (graph-pair replay):
-    a launch- and latency-bound step; CUDA events on the handle's stream."""
+    a launch- and latency-bound step, autotuned first (small work items give
+    more CTAs); CUDA events on the handle's stream."""
     import torch
     graft.load_package()
     from rd_gb300 import scenes
@@ -304,6 +305,10 @@ def measure_snowball(pkg, local, warmup):
     sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, device=local, **sc.params()))
     stream = torch.cuda.ExternalStream(sim.stream(), device=local)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sim.set_particles(sc.x, sc.v, sc.mass)
+    sim.init_volumes()
+    tune = sim.autotune(sc.dt, steps=20)
+    tune["candidates"] = sim.tune_trials()
     best = None
     for _ in range(3):
         sim.set_particles(sc.x, sc.v, sc.mass)
@@ -323,7 +328,7 @@ def measure_snowball(pkg, local, warmup):
     ms, launches, replays = best
     return {"value": sc.n * sc.steps / (ms / 1e3), "unit": "particle-steps/s", "steps": sc.steps,
             "warmup": warmup, "ms_per_step": ms / sc.steps, "gpu_launches": launches, "graph_replays": replays,
-            "flags": flags, "timing": "best of 3 passes from the initial state",
+            "flags": flags, "timing": "best of 3 passes from the initial state", "tuning": tune,
             "workload": "snowball: 8,192 particles uniform in a sphere r = 0.1 at (0.5, 0.6, 0.5), 64^3, "
                         "v0 = (0, -2, 0), sticky walls, 200 steps, FP32"}
 

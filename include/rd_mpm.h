@@ -320,8 +320,8 @@ rd_status rd_batch_step(rd_handle* h, double dt, int32_t nsteps);
 rd_status rd_set_graphs(rd_handle* h, int enable);
 
 /* Autotuner: times `steps` steps of the current state (from the same saved
- * state each time) for each work-item size (FP32: 128, 192, 256 particles;
- * FP64: 64, 96, 128), each persistent grid of 1 .. max resident CTAs per SM of
+ * state each time) for each work-item size (FP32: 64, 128, 192, 256 particles;
+ * FP64: 32, 64, 96, 128), each persistent grid of 1 .. max resident CTAs per SM of
  * the fused kernel and, for FP32 handles with the lagged-B order and without
  * the full F_P, each scatter layout of its P2G (RD_SCATTER_*: how the 64
  * stencil nodes of a record map to a warp's lanes); keeps the fastest and

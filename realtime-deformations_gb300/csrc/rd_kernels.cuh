@@ -266,16 +266,33 @@ __global__ void __launch_bounds__(256) k_tile_sums(const uint32_t* __restrict__ 
 // of the next sort.  With `list` given, the indices of the non-empty tiles
 // go to list[0 ..) in ascending order and their number to list[ntiles].  One
 // CTA of 1024 threads; each thread takes kPrefixPer consecutive tiles per
-// trip, loaded together, so the trips (and their barriers) are few.
+// trip, loaded together, so the trips (and their barriers) are few.  With
+// `bcount` given (grids of at most kTileSumsInPrefix tiles) the CTA first
+// sums the block counts into the tiles itself, a warp per tile, which saves
+// the k_tile_sums launch of small scenes.
 constexpr int kPrefixPer = 8;
+constexpr int kTileSumsInPrefix = 1024;
 
 __global__ void __launch_bounds__(1024) k_tile_prefix(uint32_t* __restrict__ sums, int ntiles,
                                                       uint32_t* __restrict__ nwork_next_sort, uint32_t n_expected,
-                                                      uint32_t* flags, uint32_t* __restrict__ list) {
+                                                      uint32_t* flags, uint32_t* __restrict__ list,
+                                                      const uint32_t* __restrict__ bcount = nullptr,
+                                                      int nblocks = 0) {
     __shared__ uint2 s_w[32];   // per warp: (particles, non-empty tiles)
     __shared__ uint2 s_carry;   // totals of the previous trips
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     if (tid == 0) { s_carry = make_uint2(0u, 0u); *nwork_next_sort = 0u; }
+    if (bcount) {
+        for (int t = wid; t < ntiles; t += 32) {
+            const int b0 = t * kBlocksPerTile + 2 * lane;
+            uint32_t sum = 0;
+            if (b0 < nblocks) sum += bcount[b0];
+            if (b0 + 1 < nblocks) sum += bcount[b0 + 1];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+            if (lane == 0) sums[t] = sum;
+        }
+    }
     __syncthreads();
     for (int base = 0; base < ntiles; base += 1024 * kPrefixPer) {
         const int t0 = base + tid * kPrefixPer;

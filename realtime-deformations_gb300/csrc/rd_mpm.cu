@@ -276,6 +276,11 @@ struct rd_handle {
     int scatter = RD_SCATTER_LANE_PAIRS;     // lane layout of the fused kernel's P2G scatter
     std::vector<rd_tune_trial> tune_trials;  // the points the last rd_autotune timed
     cudaStream_t stream = nullptr;
+    // the step's grid clear runs on `side` while the sort runs on `stream`
+    // (forked and joined with the two events, so a captured step graph holds
+    // the two branches)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int sms = 0;
     int n = 0;
     size_t ncells = 0;
@@ -547,16 +552,23 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     uint32_t* nw = h->nwork2 + (h->nb ^ 1);
     uint32_t* nw_next = h->nwork2 + h->nb;
     long t = tmark_begin(h, RD_KERNEL_SCAN);
-    k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, h->stream>>>(h->bcount, h->nblocks, ntiles,
-                                                                             h->tile_sums);
-    k_tile_prefix<<<1, 1024, 0, h->stream>>>(h->tile_sums, ntiles, nw_next, (uint32_t)h->n, h->flags, h->tile_list);
+    if (ntiles <= kTileSumsInPrefix) {  // small grids: the prefix kernel sums the tiles itself
+        k_tile_prefix<<<1, 1024, 0, h->stream>>>(h->tile_sums, ntiles, nw_next, (uint32_t)h->n, h->flags,
+                                                 h->tile_list, h->bcount, h->nblocks);
+    } else {
+        k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, h->stream>>>(h->bcount, h->nblocks, ntiles,
+                                                                                 h->tile_sums);
+        RD_TRY(launched(h, "k_tile_sums"));
+        k_tile_prefix<<<1, 1024, 0, h->stream>>>(h->tile_sums, ntiles, nw_next, (uint32_t)h->n, h->flags,
+                                                 h->tile_list);
+    }
     const unsigned scan_grid = (unsigned)std::min<size_t>((size_t)ntiles, (size_t)h->sms * 2);
     k_scan<<<scan_grid, kScanThreads, 0, h->stream>>>(h->counts, h->cursor, h->bcount, h->tile_sums, h->tile_list,
                                                       ntiles, h->nkeys, h->work, nw, (uint32_t)h->work_cap,
                                                       (uint32_t)work_size<T>(h), h->flags, h->d_sblock,
                                                       (int)h->scenes.size());
     tmark_end(h, t);
-    RD_TRY(launched(h, "k_scan", 3));
+    RD_TRY(launched(h, "k_scan", 2));
     h->nb ^= 1;
     t = tmark_begin(h, RD_KERNEL_SCATTER);
     k_scatter<<<blocks_for(h->n, 256), 256, 0, h->stream>>>(h->n, h->keys[h->cur], h->cursor, h->perm);
@@ -593,16 +605,18 @@ template <typename T> unsigned persistent_grid(const rd_handle* h, int occ) {
     return (unsigned)std::max<size_t>(1, std::min<size_t>(max_items, (size_t)h->sms * per_sm));
 }
 
-// Zeroes the marked node blocks of grid buffer `which` (k_grid_clear).
-template <typename T> rd_status clear_grid(rd_handle* h, int which) {
+// Zeroes the marked node blocks of grid buffer `which` (k_grid_clear), on
+// `st` (the handle's stream by default).
+template <typename T> rd_status clear_grid(rd_handle* h, int which, cudaStream_t st = nullptr) {
+    if (!st) st = h->stream;
     const DevParams<T> P = make_params<T>(h, 0.0, T(0));
     DevBufs D = bufs<T>(h);
     const unsigned nb = (unsigned)std::min<size_t>(blocks_for((size_t)h->nblocks, 256), (size_t)h->sms * 16);
     vec4<T>* grid = static_cast<vec4<T>*>(h->grid[which]);
     if (batched(h))
-        k_grid_clear<T, true><<<nb, 256, 0, h->stream>>>(P, D, grid, h->gmark[which], h->nblocks);
+        k_grid_clear<T, true><<<nb, 256, 0, st>>>(P, D, grid, h->gmark[which], h->nblocks);
     else
-        k_grid_clear<T, false><<<nb, 256, 0, h->stream>>>(P, D, grid, h->gmark[which], h->nblocks);
+        k_grid_clear<T, false><<<nb, 256, 0, st>>>(P, D, grid, h->gmark[which], h->nblocks);
     return launched(h, "k_grid_clear");
 }
 
@@ -617,10 +631,21 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
     }
     const bool batch = batched(h);
     if (batch) RD_TRY(ensure_table<T>(h, dt, (T)dt));
+    // a steady step clears the next grid buffer (the one the previous step
+    // read; nothing in the sort touches it) on the side stream while the sort
+    // runs; per-kernel timing keeps every launch on the handle's stream
+    const bool rebuild = !(h->fgrid_valid && h->fgrid_dt == dt);
+    const bool fork = !rebuild && !h->sorted && !h->timing && h->side;
+    if (fork) {
+        RD_TRY(check_cuda(h, cudaEventRecord(h->ev_fork, h->stream), "fork"));
+        RD_TRY(check_cuda(h, cudaStreamWaitEvent(h->side, h->ev_fork, 0), "fork"));
+        RD_TRY(clear_grid<T>(h, h->g ^ 1, h->side));
+        RD_TRY(check_cuda(h, cudaEventRecord(h->ev_join, h->side), "join"));
+    }
     if (!h->sorted) RD_TRY(sort_particles<T>(h));
     DevParams<T> P = make_params<T>(h, dt, (T)dt);
     long t;
-    if (!(h->fgrid_valid && h->fgrid_dt == dt)) {  // P2G of the current state
+    if (rebuild) {  // P2G of the current state
         t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
         RD_TRY(clear_grid<T>(h, h->g));
         tmark_end(h, t);
@@ -645,9 +670,13 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
         RD_TRY(launched(h, "k_p2g"));
         if (reorder) h->cur ^= 1;  // the ordered copy is the state now; perm is the identity
     }
-    t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
-    RD_TRY(clear_grid<T>(h, h->g ^ 1));
-    tmark_end(h, t);
+    if (fork) {
+        RD_TRY(check_cuda(h, cudaStreamWaitEvent(h->stream, h->ev_join, 0), "join"));
+    } else {
+        t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
+        RD_TRY(clear_grid<T>(h, h->g ^ 1));
+        tmark_end(h, t);
+    }
     DevBufs D = bufs<T>(h);
     t = tmark_begin(h, RD_KERNEL_G2P2G);
     const unsigned fg = persistent_grid<T>(h, h->occ_g2p);
@@ -1013,6 +1042,9 @@ void release(rd_handle* h) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->h_scenes) cudaFreeHost(h->h_scenes);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -1154,6 +1186,10 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
     if (cudaGetDeviceProperties(&prop, p.device) != cudaSuccess) return bail(RD_CUDA_ERROR);
     h->sms = prop.multiProcessorCount;
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(RD_CUDA_ERROR);
+    if (cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        return bail(RD_CUDA_ERROR);
     const size_t n = std::max<size_t>(1, (size_t)h->n);
     const size_t v4 = 4 * h->esize;
     const size_t wp = p.precision == RD_FP64 ? WorkP<double>::value : WorkP<float>::value;
@@ -1362,7 +1398,7 @@ template <typename T> bool tune_point_ok(const rd_handle* h, const rd_tune_resul
 template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps, const char* cache_path,
                                               rd_tune_result* res) {
     NvtxRange range("rd_autotune");
-    const int wps_f[] = {128, 192, 256}, wps_d[] = {64, 96, 128};
+    const int wps_f[] = {64, 128, 192, 256}, wps_d[] = {32, 64, 96, 128};
     const int* wps = sizeof(T) == 4 ? wps_f : wps_d;
     rd_tune_result best{WorkP<T>::value, 0, 0.0, 0, RD_SCATTER_LANE_PAIRS, 0};
     h->tune_trials.clear();
@@ -1405,7 +1441,7 @@ template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps
     const int old_wp = h->wp, old_mult = h->grid_mult, old_scatter = h->scatter;
     float best_ms = 0.f;
     for (int l = 0; l < scatter_layouts(h) && st == RD_OK; ++l)
-        for (int a = 0; a < 3 && st == RD_OK; ++a)
+        for (int a = 0; a < 4 && st == RD_OK; ++a)
             for (int c = 1; c <= h->occ_g2p && st == RD_OK; ++c) {
                 h->wp = wps[a];
                 h->grid_mult = c;

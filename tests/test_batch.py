@@ -95,8 +95,9 @@ def test_graph_replay_matches_eager_launches(built_pkg):
         s.step(sc.dt, 3)
         l0 = s.launch_count()
         s.step(sc.dt, 10)
-        # steady steps: tile sums, tile prefix, scan, scatter, grid clear and the fused kernel
-        assert s.launch_count() - l0 == 60
+        # steady steps: tile prefix (summing the tiles itself on a grid this
+        # small), scan, scatter, grid clear and the fused kernel
+        assert s.launch_count() - l0 == 50
         out.append(s.get_particles())
     for k in ("x", "v", "FE", "Jp"):
         assert rel(out[0][k], out[1][k]) < 1e-5
@@ -129,8 +130,8 @@ def test_autotune_picks_a_valid_pair_and_restores_state(built_pkg):
     tuned = make_batch(built_pkg, batch)
     ref = make_batch(built_pkg, batch)
     r = tuned.autotune(dt, steps=4)
-    assert r["particles_per_item"] in (128, 192, 256)
-    assert r["trials"] >= 6 and r["ms_per_step"] > 0 and not r["from_cache"]
+    assert r["particles_per_item"] in (64, 128, 192, 256)
+    assert r["trials"] >= 8 and r["ms_per_step"] > 0 and not r["from_cache"]
     trials = tuned.tune_trials()
     assert len(trials) == r["trials"]
     assert {t["scatter"] for t in trials} == {"lane_pairs", "record_pairs"}
