@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(256) k_tile_sums(const uint32_t* __restrict__ 
 // sums the block counts into the tiles itself, a warp per tile, which saves
 // the k_tile_sums launch of small scenes.
 constexpr int kPrefixPer = 8;
-constexpr int kTileSumsInPrefix = 1024;
+constexpr int kTileSumsInPrefix = 128;
 
 __global__ void __launch_bounds__(1024) k_tile_prefix(uint32_t* __restrict__ sums, int ntiles,
                                                       uint32_t* __restrict__ nwork_next_sort, uint32_t n_expected,
