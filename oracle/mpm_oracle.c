@@ -542,6 +542,145 @@ void orc_advect(const orc_params* P, real dt, orc_state* S) {
         }
 }
 
+/* ---- implicit time integration (material_point_method.cpp:160-233) --------
+ * Dead code in the reference (nothing calls timeIntegration), restated for the
+ * GPU's rd_time_integration: the energy of the grid velocities v of the cells
+ * with mass,
+ *   E(v) = sum_i 1/2 m_i |v_i - v*_i|^2 + sum_p V_p Psi(Fhat_p(v), F_P,p),
+ *   Fhat_p = (I + dt sum_i v_i grad w_ip^T) F_E,p,
+ *   Psi = mu ||Fhat - R||^2 + lambda / 2 (J - 1)^2,  R = polar rotation of Fhat,
+ * with v* the grid velocities at the call, and mu = mu0 h, lambda = lambda0 h
+ * where, as the reference writes it (:194-199), h = exp(xi * 1 - det F_P)
+ * (mode 0; mode 1 is the intended exp(xi (1 - det F_P))).  The reference's
+ * own constants are mu0 = lambda0 = 1, xi = 10 (material_point_method.hpp:
+ * 213-216).  The reference minimises E with LBFGS on finite differences; here
+ * the gradient is analytic:
+ *   dE/dv_i = m_i (v_i - v*_i) + dt sum_p V_p P_p F_E,p^T grad w_ip,
+ *   P = 2 mu (Fhat - R) + lambda (J - 1) J Fhat^-T. */
+
+/* WeightCalculator::weightNxDerivative (material_point_method.hpp:32-51): the
+ * literals are double, the argument float. */
+static real weight_nx_derivative(real x) {
+    const real a = (real)fabs((double)x);
+    const double xd = (double)x;
+    if (a < 1.0f) {
+        if (x >= 0) return (real)(3.0 / 2.0 * xd * xd - (double)((real)2 * x));
+        return (real)(-3.0 / 2.0 * xd * xd - (double)((real)2 * x));
+    }
+    if (a < 2.0) {
+        if (x >= 0) {
+            const double t = (double)((real)2 - x);
+            return (real)(-0.5 * t * t);
+        }
+        const double t = (double)((real)2 + x);
+        return (real)(0.5 * t * t);
+    }
+    return (real)0;
+}
+
+/* WeightCalculator::wipGrad (material_point_method.hpp:59-70). */
+static void wip_grad(const orc_params* P, int i, int j, int k, const real* pos, real* g) {
+    const real h = (real)P->h;
+    const real xc = (pos[0] - (real)i * h) / h;
+    const real yc = (pos[1] - (real)j * h) / h;
+    const real zc = (pos[2] - (real)k * h) / h;
+    const real nx = weight_nx(xc), ny = weight_nx(yc), nz = weight_nx(zc);
+    const double ih = 1.0 / (double)h;
+    g[0] = (real)(ih * (double)weight_nx_derivative(xc) * (double)ny * (double)nz);
+    g[1] = (real)(ih * (double)nx * (double)weight_nx_derivative(yc) * (double)nz);
+    g[2] = (real)(ih * (double)nx * (double)ny * (double)weight_nx_derivative(zc));
+}
+
+/* The polar rotation R, the energy density and, when Pout is given, its
+ * derivative P (ElasticPlasticEnergyDensity, material_point_method.cpp:
+ * 192-210; fNorm2 sums in double). */
+static real implicit_density(const real* F, real mu, real lambda, real* Pout) {
+    real R[9];
+    polar_rotation(R, F);
+    double n2 = 0.0;
+    for (int e = 0; e < 9; ++e) {
+        const real d = F[e] - R[e];
+        n2 += (double)(d * d);
+    }
+    const real J = mat_det(F);
+    if (Pout) {
+        /* (J - 1) J F^-T = (J - 1) cof(F) */
+        const real cof[9] = {F[4] * F[8] - F[5] * F[7], F[5] * F[6] - F[3] * F[8], F[3] * F[7] - F[4] * F[6],
+                             F[2] * F[7] - F[1] * F[8], F[0] * F[8] - F[2] * F[6], F[1] * F[6] - F[0] * F[7],
+                             F[1] * F[5] - F[2] * F[4], F[2] * F[3] - F[0] * F[5], F[0] * F[4] - F[1] * F[3]};
+        for (int e = 0; e < 9; ++e) Pout[e] = (real)2 * mu * (F[e] - R[e]) + lambda * (J - (real)1) * cof[e];
+    }
+    return mu * (real)n2 + lambda / (real)2 * (J - (real)1) * (J - (real)1);
+}
+
+/* Energy (material_point_method.cpp:160-173) at the dense velocity field vel
+ * (cells x 3; only cells with mass count), ElasticPotential (:175-190) summed
+ * in `real` over the particles in order; the gradient (dense, cells x 3, zero
+ * where there is no mass) when grad is given.  G holds the masses and the
+ * grid velocities v* of the call. */
+double orc_implicit_energy(const orc_params* P, const orc_state* S, const orc_grid* G, real dt, double mu0,
+                           double lambda0, double xi, int mode, const real* vel, real* grad) {
+    const size_t nc = ncells(P);
+    double kinetic = 0.0;
+    if (grad) memset(grad, 0, 3 * nc * sizeof(real));
+    for (size_t c = 0; c < nc; ++c) {
+        if (G->mass[c] == (real)0) continue;
+        const real d[3] = {vel[3 * c] - G->vel[3 * c], vel[3 * c + 1] - G->vel[3 * c + 1],
+                           vel[3 * c + 2] - G->vel[3 * c + 2]};
+        const real len = (real)sqrt((double)(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+        kinetic += 0.5 * (double)G->mass[c] * (double)len * (double)len;
+        if (grad)
+            for (int a = 0; a < 3; ++a) grad[3 * c + a] = G->mass[c] * d[a];
+    }
+    real acc = 0;
+    for (int p = 0; p < S->n; ++p) {
+        const real* pos = S->x + 3 * p;
+        real Fh[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        int b[3];
+        base_cell(P, pos, b);
+        /* the nodes with a non-zero weight gradient, in the reference's
+         * (x-major) order of its used cells */
+        for (int dx = 1; dx <= 4; ++dx)
+            for (int dy = 1; dy <= 4; ++dy)
+                for (int dz = 1; dz <= 4; ++dz) {
+                    const int i = b[0] + dx - 2, j = b[1] + dy - 2, k = b[2] + dz - 2;
+                    const size_t c = cidx(P, i, j, k);
+                    if (G->mass[c] == (real)0) continue;
+                    real g[3];
+                    wip_grad(P, i, j, k, pos, g);
+                    const real vd[3] = {vel[3 * c] * dt, vel[3 * c + 1] * dt, vel[3 * c + 2] * dt};
+                    for (int r = 0; r < 3; ++r)
+                        for (int q = 0; q < 3; ++q) Fh[3 * r + q] += vd[r] * g[q]; /* outerProduct(v dt, grad w) */
+                }
+        mat_mul(Fh, Fh, S->FE + 9 * p);
+        const real jp = mat_det(S->FP + 9 * p);
+        const real e = mode == 0 ? (real)xi * (real)1 - jp : (real)xi * ((real)1 - jp);
+        const real hard = orc_exp(e);
+        const real mu = (real)mu0 * hard, lambda = (real)lambda0 * hard;
+        real Pm[9];
+        acc += S->vol[p] * implicit_density(Fh, mu, lambda, grad ? Pm : NULL);
+        if (!grad) continue;
+        /* dt V P F_E^T, applied to each node's weight gradient */
+        real FT[9], A[9];
+        mat_transpose(FT, S->FE + 9 * p);
+        mat_mul(A, Pm, FT);
+        const real s = dt * S->vol[p];
+        for (int e2 = 0; e2 < 9; ++e2) A[e2] *= s;
+        for (int dx = 1; dx <= 4; ++dx)
+            for (int dy = 1; dy <= 4; ++dy)
+                for (int dz = 1; dz <= 4; ++dz) {
+                    const int i = b[0] + dx - 2, j = b[1] + dy - 2, k = b[2] + dz - 2;
+                    const size_t c = cidx(P, i, j, k);
+                    if (G->mass[c] == (real)0) continue;
+                    real g[3], Ag[3];
+                    wip_grad(P, i, j, k, pos, g);
+                    mat_vec(Ag, A, g);
+                    for (int a = 0; a < 3; ++a) grad[3 * c + a] += Ag[a];
+                }
+    }
+    return kinetic + (double)acc;
+}
+
 /* main.cpp:53-54 */
 void orc_init(const orc_params* P, orc_state* S, orc_grid* G) {
     orc_rasterize(P, S, G);

@@ -166,6 +166,9 @@ def _lib(dtype):
         lib.orc_collisions.argtypes = [P, G]
         lib.orc_weight.argtypes = [rt]
         lib.orc_weight.restype = rt
+        lib.orc_implicit_energy.argtypes = [P, S, G, rt, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        lib.orc_implicit_energy.restype = ctypes.c_double
         _LIBS[key] = lib
     return _LIBS[key]
 
@@ -240,6 +243,18 @@ class OracleSim:
     def move_colliders(self, dt: float):
         self.lib.orc_move_colliders(dt)
 
+    def implicit_energy(self, vel, dt: float, mu0: float = 1.0, lambda0: float = 1.0, xi: float = 10.0,
+                        hardening: int = 0, grad: bool = False):
+        """The implicit integration's energy (orc_implicit_energy) at the dense
+        grid velocities vel (cells x 3) against the current grid (masses and
+        v*), and its gradient (cells x 3) when grad is set."""
+        v = np.ascontiguousarray(np.asarray(vel, self.dtype).reshape(-1, 3))
+        g = np.zeros_like(v) if grad else None
+        e = self.lib.orc_implicit_energy(ctypes.byref(self._cp), ctypes.byref(self._cs), ctypes.byref(self._cg), dt,
+                                         mu0, lambda0, xi, hardening, v.ctypes.data,
+                                         g.ctypes.data if grad else None)
+        return (e, g) if grad else e
+
     @property
     def C(self):
         return self.B * self.dtype.type(self.dinv)
@@ -292,6 +307,9 @@ class RefSim:
             L.rdref_initialize_particles.argtypes = [vp, ctypes.c_uint] + [ctypes.c_float] * 6
             L.rdref_set_colliders.argtypes = [ctypes.c_int, ctypes.c_void_p]
             L.rdref_move_colliders.argtypes = [ctypes.c_float]
+            L.rdref_energy.argtypes = [vp, ctypes.c_void_p, ctypes.c_float]
+            L.rdref_energy.restype = ctypes.c_float
+            L.rdref_time_integration.argtypes = [vp, ctypes.c_float]
             cls._lib = L
         return cls._lib
 
@@ -364,6 +382,16 @@ class RefSim:
         m = np.zeros(self.n, np.float32)
         self.lib().rdref_get_mass(self.h, m.ctypes.data)
         return m
+
+    def energy(self, vel, dt: float) -> float:
+        """The reference's implicit Energy at the dense grid velocities vel."""
+        v = np.ascontiguousarray(np.asarray(vel, np.float32).reshape(-1, 3))
+        return float(self.lib().rdref_energy(self.h, v.ctypes.data, dt))
+
+    def time_integration(self, dt: float):
+        """The reference's timeIntegration: its LBFGS minimiser of Energy
+        written to the grid velocities."""
+        self.lib().rdref_time_integration(self.h, dt)
 
     def grid(self):
         nc = self.p.mi * self.p.mj * self.p.mk

@@ -179,6 +179,25 @@ void rdref_move_colliders(float dt) {
     for (auto& o : g_objects) o->move(dt);
 }
 
+// The reference's implicit energy (material_point_method.cpp:160-173, a
+// private method made reachable by the build's P2 patch) at grid velocities
+// given densely, cells x 3: the entries of its used cells, in their order,
+// form the VectorXf it takes.
+float rdref_energy(void* p, const float* vel, float dt) {
+    auto* s = static_cast<LagrangeEulerView*>(p);
+    Eigen::VectorXf v(s->used_cells.size() * 3);
+    for (size_t u = 0; u < s->used_cells.size(); ++u) {
+        const auto& c = s->used_cells[u];
+        const size_t idx = ((size_t)c.x * s->MAX_J + c.y) * s->MAX_K + c.z;
+        for (int a = 0; a < 3; ++a) v[3 * u + a] = vel[3 * idx + a];
+    }
+    return s->Energy(v, dt);
+}
+
+// timeIntegration (material_point_method.cpp:212-233): LBFGS over the used
+// cells' velocities; the grid then holds the minimiser it found.
+void rdref_time_integration(void* p, float dt) { static_cast<LagrangeEulerView*>(p)->timeIntegration(dt); }
+
 // main.cpp:53-54
 void rdref_init(void* p) {
     rdref_stage(p, 0, 0.0f);

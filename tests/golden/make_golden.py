@@ -19,6 +19,11 @@ Fixtures (all FP32, matrices row-major n x 9, grids as sparse cell lists):
   45 degrees about z moving at (0.1, 0, 0), on a 32^3 grid, dt = 1e-4: the
   grid after the collision stage of step 1 and the state after 3 steps, the
   boxes moved before each step as main.cpp:188 does (P4).
+* implicit_12.npz - the reference's implicit time integration (timeIntegration,
+  material_point_method.cpp:212-233, which its driver never calls): 40 particles
+  in a ball on a 12^3 grid, h = 1/12, random velocities and near-identity F_E,
+  after init and a rasterize; its Energy at v* and at three perturbed velocity
+  fields (dt = 1e-3), and the grid velocities its L-BFGS leaves, dense.
 
     python tests/golden/make_golden.py [REFERENCE_ROOT] [fixture ...]
 """
@@ -127,7 +132,33 @@ def colliders():
     return out
 
 
-FIXTURES = {"ref_scene_20": ref_scene, "perturbed_16": perturbed, "colliders_32": colliders}
+def implicit():
+    rng = np.random.default_rng(3)
+    G, n, dt = 12, 40, 1e-3
+    h = 1.0 / G
+    d = rng.normal(size=(n, 3))
+    d = d / np.linalg.norm(d, axis=1, keepdims=True) * rng.uniform(size=(n, 1)) ** (1 / 3) * 0.12
+    x = (d + 0.5).astype(np.float32)
+    v = rng.normal(0, 0.5, (n, 3)).astype(np.float32)
+    m = np.full(n, 1e-3, np.float32)
+    FE = (np.eye(3).reshape(1, 9) + 0.02 * rng.normal(size=(n, 9))).astype(np.float32)
+    r = orc.RefSim(orc.Params(G, G, G, h), x, v, m, FE=FE, p4=1)
+    r.init()
+    r.stage("rasterize")
+    g = r.grid()
+    used = g["mass"] != 0
+    fields = [g["vel"]] + [(g["vel"] + s * rng.normal(size=g["vel"].shape) * used[:, None]).astype(np.float32)
+                           for s in (0.1, 1.0, 10.0)]
+    energies = np.array([r.energy(f, dt) for f in fields], np.float32)
+    r.time_integration(dt)
+    vel_ref = r.grid()["vel"]
+    return {"grid": np.array([G, G, G]), "h": np.float32(h), "dt": np.float32(dt), "n": n, "x0": x, "v0": v,
+            "m0": m, "FE0": FE, "vol0": r.particles()["vol"], "gmass": g["mass"], "vstar": g["vel"],
+            "fields": np.stack(fields), "energies": energies, "vel_ref": vel_ref,
+            "energy_ref": np.float32(r.energy(vel_ref, dt))}
+
+
+FIXTURES = {"ref_scene_20": ref_scene, "perturbed_16": perturbed, "colliders_32": colliders, "implicit_12": implicit}
 
 
 def main():
