@@ -394,6 +394,16 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, uint64_
         : "memory");
 }
 
+// The tensor maps live in global memory, written by the host (cudaMemcpy),
+// and the TMA unit reads them through a proxy of its own that may still hold
+// a map an earlier allocation kept at the same address: a thread orders its
+// later copies with one map after the host's write of it by this acquire
+// fence (PTX ISA, fence.proxy.tensormap; .sys scope for a host write) before
+// its first copy with that map.
+__device__ __forceinline__ void tmap_acquire(const void* tmap) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(tmap) : "memory");
+}
+
 // Waits for the phase `parity` of bar to complete, for at most `tries`
 // polls; false when it gave up.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int tries) {

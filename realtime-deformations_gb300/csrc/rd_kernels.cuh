@@ -1284,6 +1284,7 @@ template <typename T> struct FusedShared {
     P2GTile<T, kBlk + 2> p;
     DevParams<T> par;        // the item's scene (batches)
     uint64_t tbar;           // mbarrier of the tile copy
+    int tmap_scene;          // the scene whose tensor map thread 0 last fenced (-1: none)
 };
 // Dynamic shared memory of k_g2p2g: the struct plus room to align it to the
 // 128 bytes a TMA destination needs.
@@ -1312,15 +1313,21 @@ __global__ void k_wait_probe(int tries, uint32_t* flags, int* gave_up) {
     }
 }
 
-// One thread: the grid tile of work item `it` (the kTile^3 nodes from its
-// tile origin) into S.graw by TMA.  P is the item's scene.
+// One thread (always thread 0): the grid tile of work item `it` (the kTile^3
+// nodes from its tile origin) into S.graw by TMA.  P is the item's scene.  The
+// first copy with a scene's map is preceded by the acquire fence (the items
+// of a CTA come in scene order, so that is once a scene).
 template <typename T>
 __device__ __forceinline__ void issue_tile(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S, int4 it,
                                            int scene) {
     int org[3];
     tile_origin(P, it.x, org);
-    tma_load_4d(S.graw, static_cast<const char*>(D.tmaps) + 128 * (size_t)scene, &S.tbar,
-                (uint32_t)(kTileCells * sizeof(vec4<T>)), org[2], org[1], org[0]);
+    const char* map = static_cast<const char*>(D.tmaps) + 128 * (size_t)scene;
+    if (S.tmap_scene != scene) {
+        tmap_acquire(map);
+        S.tmap_scene = scene;
+    }
+    tma_load_4d(S.graw, map, &S.tbar, (uint32_t)(kTileCells * sizeof(vec4<T>)), org[2], org[1], org[0]);
 }
 
 // G2P of one particle from the velocity tile (updateParticleVelocities,
@@ -1546,7 +1553,10 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
         *reinterpret_cast<FusedShared<T>*>(smem_fused + ((128u - (smem_addr(smem_fused) & 127u)) & 127u));
     const DevParams<T>* scenes = static_cast<const DevParams<T>*>(D.scenes);
     const uint32_t nw = min(*D.nwork, D.work_cap);
-    if (threadIdx.x == 0) mbar_init(&S.tbar);
+    if (threadIdx.x == 0) {
+        mbar_init(&S.tbar);
+        S.tmap_scene = -1;
+    }
     __syncthreads();
     uint32_t wi = blockIdx.x;
     if (threadIdx.x == 0 && wi < nw) {
