@@ -384,6 +384,14 @@ public:
         }
         stage(RD_STAGE_COLLISIONS, timeDelta);
     }
+    // material_point_method.cpp:212-233 (rd_time_integration): the grid
+    // velocities become the minimiser of the reference's implicit energy, with
+    // its L-BFGS settings unless opts says otherwise.
+    rd_implicit_result timeIntegration(float timeDelta, const rd_implicit_opts* opts = nullptr) {
+        rd_implicit_result r{};
+        check(rd_time_integration(sim_, timeDelta, opts, &r), "rd_time_integration");
+        return r;
+    }
     void updateDeformationGradient(float timeDelta) {
         stage(RD_STAGE_DEFORMATION, timeDelta);
         if (logger.enabled(Logger::LogLevel::INFO)) {

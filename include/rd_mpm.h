@@ -389,6 +389,54 @@ typedef struct rd_grads {
 rd_status rd_adjoint_record(rd_handle* h, double dt, int32_t steps, int32_t checkpoint_every);
 rd_status rd_adjoint_backward(rd_handle* h, const void* grad_x, const void* grad_v, int where, rd_grads* grads);
 
+/* ---- Implicit time integration (timeIntegration, material_point_method.cpp:212-233) ----
+ * The reference writes an implicit grid update that its driver never calls:
+ * the grid velocities v of the cells with mass are replaced by the minimiser of
+ *   E(v) = sum_i 1/2 m_i |v_i - v*_i|^2 + sum_p V_p Psi(Fhat_p(v), F_P,p)
+ * (Energy and ElasticPotential, :160-190), v* = the grid velocities at the
+ * call, Fhat_p = (I + dt sum_i v_i grad w_ip^T) F_E,p, Psi = mu ||Fhat - R||^2 +
+ * lambda / 2 (J - 1)^2 with R the polar rotation of Fhat (:192-210) and
+ * mu = mu0 e, lambda = lambda0 e, where the reference's e is exp(xi * 1 - det F_P)
+ * (RD_HARDENING_REFERENCE; RD_HARDENING_INTENDED is exp(xi (1 - det F_P))).  The
+ * reference minimises with L-BFGS (history 8, backtracking line search with
+ * factor 0.7 and Armijo constant 1e-4, at most 50 iterations, stopping when the
+ * gradient's or the step's norm falls below 1e-2) on finite-difference
+ * gradients; here the same L-BFGS runs on the device with the analytic gradient
+ *   dE/dv_i = m_i (v_i - v*_i) + dt sum_p V_p P_p F_E,p^T grad w_ip,
+ *   P = 2 mu (Fhat - R) + lambda (J - 1) J Fhat^-T.
+ * It acts on the stage-mode grid: call it after RD_STAGE_RASTERIZE (and the
+ * force and grid-velocity stages, as the step order wants); single-scene
+ * handles.  opts NULL: the reference's settings and constants (mu0 = lambda0 =
+ * 1, xi = 10, material_point_method.hpp:213-216).  Allocates its vectors on
+ * the first call (3 reals per cell with mass, times 2 * history + 6). */
+enum { RD_HARDENING_REFERENCE = 0, RD_HARDENING_INTENDED = 1 };
+typedef struct rd_implicit_opts {
+    int32_t max_iters;    /* L-BFGS iterations (50) */
+    int32_t history;      /* correction pairs kept, 1..32 (8) */
+    double grad_tol;      /* stop when |gradient| < grad_tol (1e-2) ... */
+    double step_tol;      /* ... or when |x_k+1 - x_k| < step_tol (1e-2) */
+    double mu0, lambda0, xi;
+    int32_t hardening;    /* RD_HARDENING_* */
+    int32_t ls_max_iters; /* backtracking steps before the line search fails (200) */
+} rd_implicit_opts;
+void rd_default_implicit_opts(rd_implicit_opts* opts);
+typedef struct rd_implicit_result {
+    int32_t iterations;   /* L-BFGS iterations taken */
+    int32_t evaluations;  /* energy evaluations (with or without gradient) */
+    int32_t converged;    /* 1: a tolerance was met; 0: max_iters; -1: the line search failed */
+    int32_t unknowns;     /* 3 x cells with mass */
+    double energy_start, energy; /* E(v*) and E at the result */
+    double grad_norm;     /* |dE/dv| at the result */
+} rd_implicit_result;
+rd_status rd_time_integration(rd_handle* h, double dt, const rd_implicit_opts* opts, rd_implicit_result* result);
+/* E(v) and, when grad is given, dE/dv at the velocity field vel (cells x 3,
+ * dense, index i*MAX_J*MAX_K + j*MAX_K + k; only cells with mass count) against
+ * the current stage-mode grid (masses, v*); grad is written densely, zero where
+ * there is no mass.  Host or device arrays per `where`; the grid is left as it
+ * was. */
+rd_status rd_implicit_energy(rd_handle* h, double dt, const rd_implicit_opts* opts, const void* vel, void* grad,
+                             int where, double* energy);
+
 /* Rasterize without allocating.  No counterpart in the reference: it exists for
  * callers that cannot allocate GPU memory - an engine that has handed the whole
  * device to its own pool allocator, or a real-time frame loop where

@@ -264,6 +264,74 @@ class OracleSim:
         return np.linalg.det(self.FP.reshape(-1, 3, 3).astype(np.float64))
 
 
+def implicit_lbfgs(fg, x0, max_iters=50, history=8, grad_tol=1e-2, step_tol=1e-2, ls_max_iters=200):
+    """The L-BFGS of rd_time_integration restated in numpy (FP64), for the
+    parity test of the device solver: Nocedal & Wright 7.2 with the two-loop
+    recursion scaled by s.y / y.y, a backtracking Armijo line search (factor
+    0.7, constant 1e-4) from a unit step, and steepest descent with a step of
+    min(1, 1 / |g|_inf) whenever the direction does not descend - as the
+    reference's vendored minimiser (external/mcloptlib LBFGS.hpp,
+    Backtracking.hpp) is configured by mathy.hpp:10-36.  fg(x) -> (E, grad).
+    Returns (x, E, iterations, converged) with converged 1 (a tolerance),
+    0 (max_iters) or -1 (line search failed)."""
+    x = np.array(x0, np.float64)
+    fx, g = fg(x)
+    pairs = []
+    gamma, alpha_init = 1.0, 1.0
+    converged, k = 0, 0
+    while k < max_iters:
+        x_old, g_old = x.copy(), g.copy()
+        q = g.copy()
+        alphas = []
+        for s, y in reversed(pairs):
+            rho = 1.0 / np.dot(y, s)
+            a = rho * np.dot(q, s)
+            alphas.append((rho, a))
+            q -= a * y
+        q *= gamma
+        for (s, y), (rho, a) in zip(pairs, reversed(alphas)):
+            beta = rho * np.dot(q, y)
+            q += (a - beta) * s
+        direction = np.dot(g, q)
+        if not direction > 0.0:
+            q = g.copy()
+            pairs = []
+            gmax = np.max(np.abs(g))
+            alpha_init = min(1.0, 1.0 / gmax) if gmax > 0 else 1.0
+            direction = np.dot(g, q)
+        a, ls = alpha_init, 0
+        while ls < ls_max_iters:
+            fa, _ = fg(x - a * q)
+            if fa <= fx - 1e-4 * a * direction:
+                break
+            a *= 0.7
+            ls += 1
+        if ls >= ls_max_iters:
+            converged = -1
+            break
+        x = x - a * q
+        step = a * np.linalg.norm(q)
+        if np.linalg.norm(g) < grad_tol or step < step_tol:
+            converged = 1
+            fx = fa
+            k += 1
+            break
+        fx, g = fg(x)
+        s, y = x - x_old, g - g_old
+        pairs.append((s, y))
+        if len(pairs) > history:
+            pairs.pop(0)
+        yy = np.dot(y, y)
+        if not abs(yy) > 0.0:
+            k += 1
+            break
+        gamma = np.dot(s, y) / yy
+        alpha_init = 1.0
+        k += 1
+    fx, g = fg(x)
+    return x, fx, k, converged
+
+
 def collider_spec(colliders) -> np.ndarray:
     """Flat float64 array, 13 per collider: translation (3), rotation as a
     unit quaternion (w, x, y, z), scale (half extents, 3), velocity (3)."""

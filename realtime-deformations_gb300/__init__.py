@@ -51,7 +51,8 @@ EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "
            "rd_tune_cache_put", "rd_set_tuning", "rd_get_tuning",
            "rd_adjoint_record", "rd_adjoint_backward", "rd_set_colliders", "rd_move_colliders",
            "rd_set_colors", "rd_device_colors", "rd_splat", "rd_initialize_particles", "rd_get_diagnostics",
-           "rd_rasterize_noalloc", "rd_rasterize_noalloc_flags")
+           "rd_rasterize_noalloc", "rd_rasterize_noalloc_flags", "rd_default_implicit_opts", "rd_time_integration",
+           "rd_implicit_energy")
 KERNELS = ("keys", "scan", "scatter", "grid_clear", "p2g", "g2p2g", "adj_g2p", "adj_p2g")
 
 
@@ -168,6 +169,33 @@ class TuneResult(ctypes.Structure):
                 ("from_cache", ctypes.c_int32)]
 
 
+class ImplicitOpts(ctypes.Structure):
+    _fields_ = [("max_iters", ctypes.c_int32), ("history", ctypes.c_int32), ("grad_tol", ctypes.c_double),
+                ("step_tol", ctypes.c_double), ("mu0", ctypes.c_double), ("lambda0", ctypes.c_double),
+                ("xi", ctypes.c_double), ("hardening", ctypes.c_int32), ("ls_max_iters", ctypes.c_int32)]
+
+
+class ImplicitResult(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("evaluations", ctypes.c_int32), ("converged", ctypes.c_int32),
+                ("unknowns", ctypes.c_int32), ("energy_start", ctypes.c_double), ("energy", ctypes.c_double),
+                ("grad_norm", ctypes.c_double)]
+
+
+HARDENING_REFERENCE, HARDENING_INTENDED = 0, 1
+
+
+def implicit_opts(**kw) -> ImplicitOpts:
+    """rd_default_implicit_opts (the reference's L-BFGS settings and constants)
+    with the given fields replaced."""
+    o = ImplicitOpts()
+    lib().rd_default_implicit_opts(ctypes.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown implicit option {k}")
+        setattr(o, k, v)
+    return o
+
+
 class TuneTrial(ctypes.Structure):
     _fields_ = [("particles_per_item", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
                 ("scatter", ctypes.c_int32), ("ms_per_step", ctypes.c_double)]
@@ -248,6 +276,12 @@ def lib():
                                             ctypes.POINTER(ctypes.c_int32)]
             L.rd_tune_cache_put.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(TuneResult)]
             L.rd_set_tuning.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+            L.rd_default_implicit_opts.argtypes = [ctypes.POINTER(ImplicitOpts)]
+            L.rd_default_implicit_opts.restype = None
+            L.rd_time_integration.argtypes = [vp, ctypes.c_double, ctypes.POINTER(ImplicitOpts),
+                                              ctypes.POINTER(ImplicitResult)]
+            L.rd_implicit_energy.argtypes = [vp, ctypes.c_double, ctypes.POINTER(ImplicitOpts), vp, vp, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_double)]
             L.rd_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                                         ctypes.POINTER(ctypes.c_int32)]
             L.rd_get_diagnostics.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(Diagnostics)]
@@ -391,6 +425,28 @@ class Simulation:
 
     def stage(self, name: str, dt: float = 0.0):
         self._check(lib().rd_stage(self._h, STAGES[name], float(dt)), f"rd_stage({name})")
+
+    def time_integration(self, dt: float, **opts) -> dict:
+        """rd_time_integration: the grid velocities replaced by the minimiser of
+        the reference's implicit energy (options as rd_implicit_opts fields)."""
+        o, r = implicit_opts(**opts), ImplicitResult()
+        self._check(lib().rd_time_integration(self._h, float(dt), ctypes.byref(o), ctypes.byref(r)),
+                    "rd_time_integration")
+        return {k: getattr(r, k) for k, _ in ImplicitResult._fields_}
+
+    def implicit_energy(self, vel, dt: float, grad: bool = False, **opts):
+        """rd_implicit_energy at the dense velocity field vel (cells x 3):
+        the energy, and (energy, gradient) with grad."""
+        p = self.params
+        nc = p.max_i * p.max_j * p.max_k
+        v = np.ascontiguousarray(np.asarray(vel, self.dtype).reshape(nc, 3))
+        g = np.zeros((nc, 3), self.dtype) if grad else None
+        e = ctypes.c_double()
+        o = implicit_opts(**opts)
+        self._check(lib().rd_implicit_energy(self._h, float(dt), ctypes.byref(o), v.ctypes.data,
+                                             g.ctypes.data if grad else None, RD_HOST, ctypes.byref(e)),
+                    "rd_implicit_energy")
+        return (e.value, g) if grad else e.value
 
     def get_grid(self, force: bool = False):
         p = self.params
@@ -684,6 +740,10 @@ class LagrangeEulerView:
             self.sim.set_colliders(objs)
             self._colliders = objs
         self.sim.stage("collisions", timeDelta)
+
+    def timeIntegration(self, timeDelta: float, **opts):
+        """material_point_method.cpp:212-233 (rd_time_integration)."""
+        return self.sim.time_integration(timeDelta, **opts)
 
     def updateDeformationGradient(self, timeDelta: float):
         self.sim.stage("deformation", timeDelta)

@@ -18,6 +18,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include "rd_adjoint.cuh"
+#include "rd_implicit.cuh"
 #include "rd_kernels.cuh"
 #include "rd_init.cuh"
 #include "rd_view.cuh"
@@ -208,6 +209,20 @@ struct rd_graph {
 
 // Reverse-mode rollout: checkpoints of the forward states, the per-segment
 // stores of the recomputed states and grids, and the adjoint buffers.
+// Buffers of rd_time_integration, allocated on its first call: the list of
+// cells with mass and a dense gradient accumulator (per cell), the compact
+// L-BFGS vectors (3 reals per cell with mass; grown when a call needs more)
+// and the reduction words.
+struct rd_implicit_data {
+    uint32_t* idx = nullptr;  // cells with mass, then their count at idx[ncells]
+    void* gacc = nullptr;     // vec4 per cell: the particles' part of the gradient
+    size_t cap = 0;           // cells the compact vectors hold
+    int hist = 0;             // correction pairs they hold
+    void* vec = nullptr;      // vstar, x, g, xold, gold, q, then s[hist], y[hist]
+    double* red = nullptr;    // device reductions
+    double* hred = nullptr;   // their page-locked host copy
+};
+
 struct rd_adjoint_data {
     bool recorded = false;
     uint64_t version = 0;  // handle version the record belongs to
@@ -255,6 +270,7 @@ struct rd_handle {
     rd_params prm{};                    // scene 0's (precision, device, flags for all)
     uint64_t version = 0;               // bumped by every public call that changes the state
     rd_adjoint_data adj;
+    rd_implicit_data imp;
     std::vector<rd_scene_info> scenes;  // one, or a batch
     void* d_scenes = nullptr;           // DevParams<T> per scene (batches)
     uint32_t* d_sblock = nullptr;       // first block of each scene, then the total
@@ -1018,6 +1034,14 @@ void drop_graphs(rd_handle* h) {
 void release(rd_handle* h) {
     for (cudaEvent_t e : h->ev)
         if (e) cudaEventDestroy(e);
+    {
+        rd_implicit_data& m = h->imp;
+        void* ip[] = {m.idx, m.gacc, m.vec, m.red};
+        for (void* p : ip)
+            if (p) cudaFree(p);
+        if (m.hred) cudaFreeHost(m.hred);
+        m = rd_implicit_data{};
+    }
     h->ev.clear();
     drop_graphs(h);
     rd_adjoint_data& a = h->adj;
@@ -1485,6 +1509,312 @@ template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps
     if (st == RD_OK && cache_path && rd_tune_cache_put(cache_path, key.c_str(), &best) != RD_OK)
         st = fail(h, RD_INVALID_ARG, "tuning cache: could not append to the file");
     return st;
+}
+
+
+// ---------------------------------------------------------------- implicit
+rd_implicit_opts implicit_defaults() {
+    rd_implicit_opts o;
+    o.max_iters = 50;
+    o.history = 8;
+    o.grad_tol = 1e-2;
+    o.step_tol = 1e-2;
+    o.mu0 = 1.0;
+    o.lambda0 = 1.0;
+    o.xi = 10.0;
+    o.hardening = RD_HARDENING_REFERENCE;
+    o.ls_max_iters = 200;
+    return o;
+}
+
+bool implicit_opts_ok(const rd_implicit_opts& o) {
+    return o.max_iters >= 0 && o.history >= 1 && o.history <= 32 && o.grad_tol >= 0 && o.step_tol >= 0 &&
+           std::isfinite(o.mu0) && std::isfinite(o.lambda0) && std::isfinite(o.xi) &&
+           (o.hardening == RD_HARDENING_REFERENCE || o.hardening == RD_HARDENING_INTENDED) && o.ls_max_iters >= 1;
+}
+
+// The solver's view of one call: the cells with mass, the compact vectors and
+// the device reductions; every helper runs on the handle's stream.
+template <typename T> struct Implicit {
+    rd_handle* h;
+    DevParams<T> P;
+    ImpParams<T> Q;
+    int nused = 0, n3 = 0;
+    T *vstar = nullptr, *x = nullptr, *g = nullptr, *xold = nullptr, *gold = nullptr, *q = nullptr;
+    T* s(int i) const { return static_cast<T*>(h->imp.vec) + (size_t)(6 + i) * 3 * h->imp.cap; }
+    T* y(int i) const { return static_cast<T*>(h->imp.vec) + (size_t)(6 + h->imp.hist + i) * 3 * h->imp.cap; }
+    int evaluations = 0;
+    vec4<T>* grid() const { return static_cast<vec4<T>*>(h->grid[h->g]); }
+
+    unsigned blocks(size_t n) const { return (unsigned)std::min<size_t>(blocks_for(n, 256), (size_t)h->sms * 8); }
+
+    // Finds the cells with mass and sizes the buffers.
+    rd_status setup(int hist) {
+        rd_implicit_data& m = h->imp;
+        const size_t nc = h->ncells;
+        if (!m.idx) {
+            RD_TRY(check_cuda(h, cudaMalloc(&m.idx, (nc + 1) * sizeof(uint32_t)), "implicit cell list"));
+            RD_TRY(check_cuda(h, cudaMalloc(&m.gacc, nc * sizeof(vec4<T>)), "implicit gradient"));
+            RD_TRY(check_cuda(h, cudaMalloc(&m.red, 4 * sizeof(double)), "implicit reductions"));
+            RD_TRY(check_cuda(h, cudaMallocHost(&m.hred, 4 * sizeof(double)), "implicit reductions"));
+        }
+        // zero everywhere: particles that moved since the rasterize may reach cells without mass
+        RD_TRY(check_cuda(h, cudaMemsetAsync(m.gacc, 0, nc * sizeof(vec4<T>), h->stream), "implicit gradient"));
+        RD_TRY(check_cuda(h, cudaMemsetAsync(m.idx + nc, 0, sizeof(uint32_t), h->stream), "implicit count"));
+        k_imp_used<T><<<blocks_for(nc, 256), 256, 0, h->stream>>>(grid(), nc, m.idx, m.idx + nc);
+        RD_TRY(launched(h, "k_imp_used"));
+        uint32_t cnt = 0;
+        RD_TRY(check_cuda(h, cudaMemcpyAsync(&cnt, m.idx + nc, sizeof cnt, cudaMemcpyDeviceToHost, h->stream), "count"));
+        RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "count"));
+        nused = (int)cnt;
+        n3 = 3 * nused;
+        if ((size_t)nused > m.cap || hist > m.hist) {
+            if (m.vec) cudaFree(m.vec);
+            m.vec = nullptr;
+            m.cap = std::max<size_t>({(size_t)nused + nused / 4, m.cap, 1});
+            m.hist = std::max(hist, m.hist);
+            RD_TRY(check_cuda(h, cudaMalloc(&m.vec, (size_t)(6 + 2 * m.hist) * 3 * m.cap * sizeof(T)),
+                              "implicit vectors"));
+        }
+        T* base = static_cast<T*>(m.vec);
+        const size_t stride = 3 * m.cap;
+        vstar = base; x = base + stride; g = base + 2 * stride; xold = base + 3 * stride;
+        gold = base + 4 * stride; q = base + 5 * stride;
+        return RD_OK;
+    }
+
+    rd_status fetch(int k, double* out) {
+        RD_TRY(check_cuda(h, cudaMemcpyAsync(h->imp.hred, h->imp.red, k * sizeof(double), cudaMemcpyDeviceToHost,
+                                             h->stream), "reduction"));
+        RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "reduction"));
+        for (int i = 0; i < k; ++i) out[i] = h->imp.hred[i];
+        return RD_OK;
+    }
+
+    // E at the trial point xp + a d (d null: xp), written into the grid; with
+    // gout, the gradient there too.
+    rd_status energy(const T* xp, T a, const T* d, T* gout, double* e) {
+        ++evaluations;
+        k_imp_put<T><<<blocks_for(nused, 256), 256, 0, h->stream>>>(grid(), h->imp.idx, nused, xp, a, d);
+        RD_TRY(launched(h, "k_imp_put"));
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->imp.red, 0, sizeof(double), h->stream), "reduction"));
+        const vec4<T>* pl = static_cast<const vec4<T>*>(h->pl[h->cur]);
+        vec4<T>* gacc = static_cast<vec4<T>*>(h->imp.gacc);
+        if (h->n > 0) {
+            if (gout)
+                k_imp_particles<T, true><<<blocks_for(h->n, kThreads), kThreads, 0, h->stream>>>(P, Q, pl, grid(), gacc,
+                                                                                               h->imp.red);
+            else
+                k_imp_particles<T, false><<<blocks_for(h->n, kThreads), kThreads, 0, h->stream>>>(P, Q, pl, grid(), gacc,
+                                                                                                h->imp.red);
+            RD_TRY(launched(h, "k_imp_particles"));
+        }
+        if (gout)
+            k_imp_cells<T, true><<<blocks_for(nused, 256), 256, 0, h->stream>>>(grid(), h->imp.idx, nused, vstar, xp, a,
+                                                                               d, gacc, gout, h->imp.red);
+        else
+            k_imp_cells<T, false><<<blocks_for(nused, 256), 256, 0, h->stream>>>(grid(), h->imp.idx, nused, vstar, xp,
+                                                                                a, d, gacc, gout, h->imp.red);
+        RD_TRY(launched(h, "k_imp_cells"));
+        return fetch(1, e);
+    }
+
+    // (a . b, b . b)
+    rd_status dot(const T* a, const T* b, double out[2]) {
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->imp.red, 0, 2 * sizeof(double), h->stream), "reduction"));
+        k_imp_dot<T><<<blocks(n3), 256, 0, h->stream>>>(a, b, n3, h->imp.red);
+        RD_TRY(launched(h, "k_imp_dot"));
+        return fetch(2, out);
+    }
+    rd_status axpy(T* yv, double a, const T* xv) {
+        k_imp_axpy<T><<<blocks(n3), 256, 0, h->stream>>>(yv, (T)a, xv, n3);
+        return launched(h, "k_imp_axpy");
+    }
+    rd_status sub(T* z, const T* a, const T* b) {
+        k_imp_sub<T><<<blocks(n3), 256, 0, h->stream>>>(z, a, b, n3);
+        return launched(h, "k_imp_sub");
+    }
+    rd_status copy(T* dst, const T* src) {
+        return check_cuda(h, cudaMemcpyAsync(dst, src, (size_t)n3 * sizeof(T), cudaMemcpyDeviceToDevice, h->stream),
+                          "copy");
+    }
+    rd_status absmax(const T* v, double* out) {
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->imp.red, 0, sizeof(double), h->stream), "reduction"));
+        k_imp_absmax<T><<<blocks(n3), 256, 0, h->stream>>>(
+            v, n3, reinterpret_cast<unsigned long long*>(h->imp.red));
+        RD_TRY(launched(h, "k_imp_absmax"));
+        return fetch(1, out);
+    }
+};
+
+template <typename T> rd_status implicit_begin(rd_handle* h, double dt, const rd_implicit_opts& o, Implicit<T>& I) {
+    if (batched(h)) return fail(h, RD_NOT_SUPPORTED, "implicit integration drives a single scene");
+    if (h->grid_mode != GRID_V)
+        return fail(h, RD_INVALID_ARG, "implicit integration needs the stage-mode grid (run the rasterize stage)");
+    I.h = h;
+    I.P = make_params<T>(h, dt, T(1));
+    I.Q = ImpParams<T>{(T)dt, (T)o.mu0, (T)o.lambda0, (T)o.xi, o.hardening == RD_HARDENING_INTENDED ? 1 : 0};
+    return I.setup(o.history);
+}
+
+// timeIntegration (material_point_method.cpp:212-233): L-BFGS over the
+// velocities of the cells with mass (Nocedal & Wright, Numerical
+// Optimization, 7.2, as the vendored minimiser implements it: two-loop
+// recursion with the scaling s.y / y.y, backtracking Armijo line search,
+// steepest descent with a step of min(1, 1 / |g|_inf) whenever the direction
+// is not a descent direction).
+template <typename T> rd_status time_integration_impl(rd_handle* h, double dt, const rd_implicit_opts& o,
+                                                      rd_implicit_result* res) {
+    NvtxRange range("rd_time_integration");
+    Implicit<T> I;
+    RD_TRY(implicit_begin<T>(h, dt, o, I));
+    rd_implicit_result r{};
+    r.unknowns = I.n3;
+    if (I.nused == 0) {
+        *res = r;
+        return RD_OK;
+    }
+    k_imp_gather<T><<<blocks_for(I.nused, 256), 256, 0, h->stream>>>(I.grid(), h->imp.idx, I.nused, I.vstar);
+    RD_TRY(launched(h, "k_imp_gather"));
+    RD_TRY(I.copy(I.x, I.vstar));
+    double fx = 0.0;
+    RD_TRY(I.energy(I.x, T(0), nullptr, I.g, &fx));
+    r.energy_start = fx;
+    const int M = o.history;
+    std::vector<double> rho(M), alpha(M);
+    int npairs = 0, head = 0;  // ring of correction pairs: the newest at (head - 1) mod M
+    double gamma = 1.0, alpha_init = 1.0;
+    int k = 0;
+    r.converged = 0;
+    for (; k < o.max_iters; ++k) {
+        RD_TRY(I.copy(I.xold, I.x));
+        RD_TRY(I.copy(I.gold, I.g));
+        RD_TRY(I.copy(I.q, I.g));
+        // first loop, newest pair first
+        for (int j = npairs - 1; j >= 0; --j) {
+            const int c = (head - npairs + j + 2 * M) % M;
+            double sy[2], sq[2];
+            RD_TRY(I.dot(I.y(c), I.s(c), sy));  // y . s
+            rho[j] = 1.0 / sy[0];
+            RD_TRY(I.dot(I.q, I.s(c), sq));  // q . s
+            alpha[j] = rho[j] * sq[0];
+            RD_TRY(I.axpy(I.q, -alpha[j], I.y(c)));
+        }
+        k_imp_scale<T><<<I.blocks(I.n3), 256, 0, h->stream>>>(I.q, (T)gamma, I.n3);
+        RD_TRY(launched(h, "k_imp_scale"));
+        for (int j = 0; j < npairs; ++j) {
+            const int c = (head - npairs + j + 2 * M) % M;
+            double yq[2];
+            RD_TRY(I.dot(I.q, I.y(c), yq));
+            const double beta = rho[j] * yq[0];
+            RD_TRY(I.axpy(I.q, alpha[j] - beta, I.s(c)));
+        }
+        double qg[2];
+        RD_TRY(I.dot(I.g, I.q, qg));  // (g . q, q . q)
+        double dir = qg[0];
+        if (!(dir > 0.0)) {  // not a descent direction: steepest descent
+            RD_TRY(I.copy(I.q, I.g));
+            npairs = 0;
+            double gmax = 0.0;
+            RD_TRY(I.absmax(I.g, &gmax));
+            alpha_init = gmax > 0.0 ? std::min(1.0, 1.0 / gmax) : 1.0;
+            RD_TRY(I.dot(I.g, I.q, qg));
+            dir = qg[0];
+        }
+        // backtracking along -q from x: f(x - a q) <= f(x) - 1e-4 a (g . q)
+        double a = alpha_init, fa = 0.0;
+        int ls = 0;
+        for (; ls < o.ls_max_iters; ++ls) {
+            RD_TRY(I.energy(I.x, (T)(-a), I.q, nullptr, &fa));
+            if (fa <= fx - 1e-4 * a * dir) break;
+            a *= 0.7;
+        }
+        if (ls >= o.ls_max_iters) {
+            r.converged = -1;
+            break;
+        }
+        RD_TRY(I.axpy(I.x, -a, I.q));
+        const double step = a * std::sqrt(qg[1]);
+        double gn[2];
+        RD_TRY(I.dot(I.g, I.g, gn));
+        if (std::sqrt(gn[0]) < o.grad_tol || step < o.step_tol) {  // the gradient before the step, as the reference tests it
+            r.converged = 1;
+            fx = fa;
+            ++k;
+            break;
+        }
+        RD_TRY(I.energy(I.x, T(0), nullptr, I.g, &fx));
+        const int c = head;
+        RD_TRY(I.sub(I.s(c), I.x, I.xold));
+        RD_TRY(I.sub(I.y(c), I.g, I.gold));
+        head = (head + 1) % M;
+        npairs = std::min(npairs + 1, M);
+        double ys[2];
+        RD_TRY(I.dot(I.s(c), I.y(c), ys));  // (s . y, y . y)
+        if (!(std::abs(ys[1]) > 0.0)) {
+            ++k;
+            break;
+        }
+        gamma = ys[0] / ys[1];
+        alpha_init = 1.0;
+    }
+    // the result into the grid, and the energy and gradient there
+    RD_TRY(I.energy(I.x, T(0), nullptr, I.g, &fx));
+    double gn[2];
+    RD_TRY(I.dot(I.g, I.g, gn));
+    r.iterations = k;
+    r.evaluations = I.evaluations;
+    r.energy = fx;
+    r.grad_norm = std::sqrt(gn[0]);
+    *res = r;
+    return RD_OK;
+}
+
+template <typename T> rd_status implicit_energy_impl(rd_handle* h, double dt, const rd_implicit_opts& o,
+                                                     const void* vel, void* grad, int where, double* energy) {
+    Implicit<T> I;
+    RD_TRY(implicit_begin<T>(h, dt, o, I));
+    const size_t nc = h->ncells;
+    // the field in, as the compact trial point (the grid gets it back afterwards)
+    const T* dv = static_cast<const T*>(vel);
+    T* dense = nullptr;
+    rd_status st = check_cuda(h, cudaMalloc(&dense, nc * 3 * sizeof(T)), "implicit field");
+    if (st != RD_OK) return st;
+    auto done = [&](rd_status s2) {
+        cudaStreamSynchronize(h->stream);
+        cudaFree(dense);
+        return s2;
+    };
+    if (cudaMemcpyAsync(dense, dv, nc * 3 * sizeof(T), where == RD_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                        h->stream) != cudaSuccess)
+        return done(check_cuda(h, cudaGetLastError(), "implicit field"));
+    if (I.nused > 0) {
+        k_imp_gather<T><<<blocks_for(I.nused, 256), 256, 0, h->stream>>>(I.grid(), h->imp.idx, I.nused, I.vstar);
+        if ((st = launched(h, "k_imp_gather")) != RD_OK) return done(st);
+        k_imp_take<T><<<blocks_for(I.nused, 256), 256, 0, h->stream>>>(dense, h->imp.idx, I.nused, I.x);
+        if ((st = launched(h, "k_imp_take")) != RD_OK) return done(st);
+    }
+    double e = 0.0;
+    st = I.nused > 0 ? I.energy(I.x, T(0), nullptr, grad ? I.g : nullptr, &e) : RD_OK;
+    if (st == RD_OK && grad) {
+        if ((st = check_cuda(h, cudaMemsetAsync(dense, 0, nc * 3 * sizeof(T), h->stream), "gradient")) == RD_OK &&
+            I.nused > 0) {
+            k_imp_spread<T><<<blocks_for(I.nused, 256), 256, 0, h->stream>>>(dense, h->imp.idx, I.nused, I.g);
+            st = launched(h, "k_imp_spread");
+        }
+        if (st == RD_OK)
+            st = check_cuda(h, cudaMemcpyAsync(grad, dense, nc * 3 * sizeof(T),
+                                               where == RD_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                                               h->stream), "gradient out");
+    }
+    // the grid's own velocities back
+    if (st == RD_OK && I.nused > 0) {
+        k_imp_put<T><<<blocks_for(I.nused, 256), 256, 0, h->stream>>>(I.grid(), h->imp.idx, I.nused, I.vstar, T(0),
+                                                                     nullptr);
+        st = launched(h, "k_imp_put");
+    }
+    *energy = e;
+    return done(st);
 }
 
 // ---------------------------------------------------------------- adjoint
@@ -2260,6 +2590,28 @@ rd_status rd_adjoint_record(rd_handle* h, double dt, int32_t steps, int32_t chec
     cudaSetDevice(h->prm.device);
     ++h->version;
     return RD_DISPATCH(h, adjoint_record_impl, h, dt, steps, checkpoint_every);
+}
+
+void rd_default_implicit_opts(rd_implicit_opts* opts) {
+    if (opts) *opts = implicit_defaults();
+}
+
+rd_status rd_time_integration(rd_handle* h, double dt, const rd_implicit_opts* opts, rd_implicit_result* result) {
+    if (!h || !result || !std::isfinite(dt)) return RD_INVALID_ARG;
+    const rd_implicit_opts o = opts ? *opts : implicit_defaults();
+    if (!implicit_opts_ok(o)) return fail(h, RD_INVALID_ARG, "implicit options out of range");
+    ++h->version;
+    cudaSetDevice(h->prm.device);
+    return RD_DISPATCH(h, time_integration_impl, h, dt, o, result);
+}
+
+rd_status rd_implicit_energy(rd_handle* h, double dt, const rd_implicit_opts* opts, const void* vel, void* grad,
+                             int where, double* energy) {
+    if (!h || !vel || !energy || !std::isfinite(dt) || (where != RD_HOST && where != RD_DEVICE)) return RD_INVALID_ARG;
+    const rd_implicit_opts o = opts ? *opts : implicit_defaults();
+    if (!implicit_opts_ok(o)) return fail(h, RD_INVALID_ARG, "implicit options out of range");
+    cudaSetDevice(h->prm.device);
+    return RD_DISPATCH(h, implicit_energy_impl, h, dt, o, vel, grad, where, energy);
 }
 
 rd_status rd_adjoint_backward(rd_handle* h, const void* grad_x, const void* grad_v, int where, rd_grads* grads) {
