@@ -66,12 +66,13 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-baseline", type=int, default=1, help="time the single-core CPU baseline (rank 0, N=1)")
     ap.add_argument("--adjoint", type=int, default=1, help="measure forward + adjoint on the 65,536-particle cube")
-    ap.add_argument("--only", choices=("batched", "adjoint", "batched_adjoint", "snowball", "profile"),
+    ap.add_argument("--only", choices=("batched", "adjoint", "batched_adjoint", "snowball", "implicit", "profile"),
                     default=None,
                     help="run one secondary measurement alone and print its JSON; 'profile' only initialises "
                          "the workload and runs --warmup + --steps steps (for ncu captures)")
     ap.add_argument("--snowball", type=int, default=1, help="measure the 8,192-particle snowball on 64^3")
     ap.add_argument("--link", type=int, default=1, help="measure the host link (pinned copies each way)")
+    ap.add_argument("--implicit", type=int, default=1, help="time timeIntegration (implicit L-BFGS)")
     ap.add_argument("--batch-steps", type=int, default=-1,
                     help="timed steps of the batched-forward workload (64 uneven scenes); -1: as many as "
                          "--steps, so the batch and the plain forward it is compared with run equally long; "
@@ -331,6 +332,102 @@ def measure_snowball(pkg, local, warmup):
             "flags": flags, "timing": "best of 3 passes from the initial state", "tuning": tune,
             "workload": "snowball: 8,192 particles uniform in a sphere r = 0.1 at (0.5, 0.6, 0.5), 64^3, "
                         "v0 = (0, -2, 0), sticky walls, 200 steps, FP32"}
+
+
+def implicit_ball(n, G, seed=3):
+    """A ball of n particles (r = 0.12 at the centre) on a G^3 grid with random
+    velocities and near-identity F_E: the shape of the reference's own test of
+    timeIntegration (40 particles on 12^3)."""
+    from rd_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    x = scenes.uniform_ball(rng, n, (0.5, 0.5, 0.5), 0.12).astype(np.float32)
+    v = rng.normal(0, 0.5, (n, 3)).astype(np.float32)
+    m = np.full(n, 1e-3, np.float32)
+    FE = (np.eye(3).reshape(1, 9) + 0.02 * rng.normal(size=(n, 9))).astype(np.float32)
+    return x, v, m, FE
+
+
+def measure_implicit(pkg, local, reps=5):
+    """timeIntegration (the implicit L-BFGS over the grid velocities) at the
+    reference's settings: on its own test's shape (40 particles, 12^3, dt 1e-3)
+    against the reference's timeIntegration timed on one host core, and on the
+    8,192-particle snowball on 64^3 after one explicit grid update.  Host wall
+    time per call (the solver's host loop reads every dot product back)."""
+    graft.load_package()
+    from rd_gb300 import scenes
+    out = {}
+    G, n, dt = 12, 40, 1e-3
+    x, v, m, FE = implicit_ball(n, G)
+    sim = pkg.Simulation(pkg.make_params(G, G, G, n, 1.0 / G, device=local))
+    best, res = None, None
+    for _ in range(reps):
+        sim.set_particles(x, v, m, FE=FE)
+        sim.init_volumes()
+        sim.stage("rasterize")
+        sim.synchronize()
+        t0 = time.perf_counter()
+        res = sim.time_integration(dt)
+        el = time.perf_counter() - t0
+        best = el if best is None or el < best else best
+    vel_ours = sim.get_grid()["vel"].astype(np.float64)
+    sim.close()
+    # both minimisers' results scored by one energy: the oracle's, FP64, at
+    # the v* of this state (the reference's Energy reads v* from the grid it
+    # overwrites, so its own value afterwards leaves out the kinetic term)
+    orc = graft.load_oracle()
+    o = orc.OracleSim(orc.Params(G, G, G, 1.0 / G), x, v, m, FE=FE, dtype=np.float64)
+    o.init()
+    o.stage("rasterize")
+    small = {"workload": f"ball of {n} particles on {G}^3 (the reference's implicit test shape), dt {dt}, FP32, "
+                         "the reference's L-BFGS settings",
+             "ms_per_call": best * 1e3, "iterations": res["iterations"], "evaluations": res["evaluations"],
+             "unknowns": res["unknowns"], "energy_start": res["energy_start"], "energy": res["energy"],
+             "energy_fp64": o.implicit_energy(vel_ours, dt), "converged": res["converged"]}
+    if orc.ref_available():
+        r = orc.RefSim(orc.Params(G, G, G, 1.0 / G), x, v, m, FE=FE, p4=1)
+        r.init()
+        r.stage("rasterize")
+        core = sorted(os.sched_getaffinity(0))[-1] if hasattr(os, "sched_getaffinity") else 0
+        old = pin_to_core(core)
+        try:
+            t0 = time.perf_counter()
+            r.time_integration(dt)
+            el = time.perf_counter() - t0
+        finally:
+            if old is not None:
+                os.sched_setaffinity(0, old)
+        small["reference"] = {"ms_per_call": el * 1e3,
+                              "energy_fp64": o.implicit_energy(r.grid()["vel"].astype(np.float64), dt), "cores": 1,
+                              "cpu_model": cpu_model(),
+                              "kind": "reference: its timeIntegration (L-BFGS on finite-difference gradients of "
+                                      "Energy), compiled headless on this host"}
+    else:
+        small["reference"] = {"unavailable": "the headless reference build is not present on this host"}
+    out["reference_shape"] = small
+    sc = scenes.snowball()
+    sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, device=local, **sc.params()))
+    best = None
+    for _ in range(3):
+        sim.set_particles(sc.x, sc.v, sc.mass)
+        sim.init_volumes()
+        for st in ("rasterize", "forces"):
+            sim.stage(st)
+        sim.stage("grid_velocities", sc.dt)
+        sim.synchronize()
+        t0 = time.perf_counter()
+        res = sim.time_integration(sc.dt)
+        el = time.perf_counter() - t0
+        best = el if best is None or el < best else best
+    flags = sim.flags()
+    sim.close()
+    out["snowball"] = {"workload": "snowball: 8,192 particles, 64^3, after rasterize, forces and the grid update, "
+                                   "FP32, the reference's L-BFGS settings",
+                       "ms_per_call": best * 1e3, "iterations": res["iterations"],
+                       "evaluations": res["evaluations"], "unknowns": res["unknowns"],
+                       "energy_start": res["energy_start"], "energy": res["energy"],
+                       "converged": res["converged"],
+                       "particle_evaluations_per_s": sc.n * res["evaluations"] / best, "flags": flags}
+    return out
 
 
 def measure_batched(pkg, local, steps, warmup, plain_value):
@@ -721,6 +818,8 @@ def run_ours(args):
     }
     if args.snowball:
         out["snowball"] = measure_snowball(pkg, local, max(args.warmup, 3))
+    if args.implicit and rank == 0:
+        out["implicit"] = measure_implicit(pkg, local)
     batch_steps = args.steps if args.batch_steps < 0 else args.batch_steps
     if batch_steps > 0:
         out["batched_forward"] = measure_batched(pkg, local, batch_steps, max(args.warmup, 3), value)
@@ -821,6 +920,8 @@ def run_only(args):
         sim.close()
     elif args.only == "snowball":
         out = measure_snowball(pkg, 0, max(args.warmup, 3))
+    elif args.only == "implicit":
+        out = measure_implicit(pkg, 0)
     elif args.only == "batched":
         out = measure_batched(pkg, 0, args.steps, max(args.warmup, 3), float("nan"))
     elif args.only == "adjoint":

@@ -370,7 +370,7 @@ __device__ __forceinline__ void svd3_near(const T F[9], T U[9], T s[3], T sm1[3]
 // ---------------------------------------------------------------- TMA
 // Tile copies with the tensor memory accelerator: cp.async.bulk.tensor into
 // shared memory, completion tracked by an mbarrier (one arrival with the
-// expected byte count per copy).  The tensor map lives in global memory.
+// expected byte count per copy).  The tensor map is a kernel parameter.
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar) {
@@ -392,16 +392,6 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, uint64_
         "[%6];" ::"r"(smem_addr(dst)),
         "l"(tmap), "r"(0), "r"(z), "r"(y), "r"(x), "r"(b)
         : "memory");
-}
-
-// The tensor maps live in global memory, written by the host (cudaMemcpy),
-// and the TMA unit reads them through a proxy of its own that may still hold
-// a map an earlier allocation kept at the same address: a thread orders its
-// later copies with one map after the host's write of it by this acquire
-// fence (PTX ISA, fence.proxy.tensormap; .sys scope for a host write) before
-// its first copy with that map.
-__device__ __forceinline__ void tmap_acquire(const void* tmap) {
-    asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;" ::"l"(tmap) : "memory");
 }
 
 // Waits for the phase `parity` of bar to complete, for at most `tries`

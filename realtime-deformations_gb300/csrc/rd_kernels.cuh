@@ -73,9 +73,6 @@ struct DevBufs {
     const uint32_t* spoff;
     int nscenes;
     const void* colliders;  // Collider<T>[ncol]
-    // tensor maps (128 bytes each, one per scene) of `grid` for the fused
-    // kernel's tile copies: the grid as (channel, z, y, x), box 4 x kTile^3
-    const void* tmaps;
 };
 
 // A box collider on the device: R (world from box, row-major), centre t, half
@@ -1284,7 +1281,6 @@ template <typename T> struct FusedShared {
     P2GTile<T, kBlk + 2> p;
     DevParams<T> par;        // the item's scene (batches)
     uint64_t tbar;           // mbarrier of the tile copy
-    int tmap_scene;          // the scene whose tensor map thread 0 last fenced (-1: none)
 };
 // Dynamic shared memory of k_g2p2g: the struct plus room to align it to the
 // 128 bytes a TMA destination needs.
@@ -1313,21 +1309,41 @@ __global__ void k_wait_probe(int tries, uint32_t* flags, int* gave_up) {
     }
 }
 
+// Tensor maps of a launch's grid tiles, passed by value as the fused
+// kernel's __grid_constant__ parameter, so a copy reads a map that is
+// constant for the launch and never one in memory the host rewrites: one for
+// a single scene, one per scene for the first kBatchMaps scenes of a batch
+// (the tiles of later scenes are loaded by the threads themselves).
+constexpr int kBatchMaps = 128;
+template <int N> struct TileMaps {
+    CUtensorMap m[N];
+};
+template <bool BATCH> using FusedMaps = TileMaps<BATCH ? kBatchMaps : 1>;
+
 // One thread (always thread 0): the grid tile of work item `it` (the kTile^3
-// nodes from its tile origin) into S.graw by TMA.  P is the item's scene.  The
-// first copy with a scene's map is preceded by the acquire fence (the items
-// of a CTA come in scene order, so that is once a scene).
+// nodes from its tile origin) into S.graw by TMA with `map`, the tensor map
+// of the item's scene region of this step's grid.
 template <typename T>
-__device__ __forceinline__ void issue_tile(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S, int4 it,
-                                           int scene) {
+__device__ __forceinline__ void issue_tile(const DevParams<T>& P, const CUtensorMap* map, FusedShared<T>& S,
+                                           int4 it) {
     int org[3];
     tile_origin(P, it.x, org);
-    const char* map = static_cast<const char*>(D.tmaps) + 128 * (size_t)scene;
-    if (S.tmap_scene != scene) {
-        tmap_acquire(map);
-        S.tmap_scene = scene;
-    }
     tma_load_4d(S.graw, map, &S.tbar, (uint32_t)(kTileCells * sizeof(vec4<T>)), org[2], org[1], org[0]);
+}
+
+// All threads: the grid tile of work item `it` (scene P, the kTile^3 nodes
+// from its tile origin; nodes outside the scene's grid as zero) into S.graw
+// with plain loads, for a batch scene without a tensor map; the caller
+// synchronises before use.
+template <typename T>
+__device__ __forceinline__ void load_tile(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S, int4 it) {
+    int org[3];
+    tile_origin(P, it.x, org);
+    const vec4<T>* g = static_cast<const vec4<T>*>(D.grid) + P.goff;
+    for (int c = threadIdx.x; c < kTileCells; c += blockDim.x) {
+        size_t lin;
+        S.graw[c] = cell_of_tile(P, org, c, lin) ? g[lin] : mk4<T>(T(0), T(0), T(0), T(0));
+    }
 }
 
 // G2P of one particle from the velocity tile (updateParticleVelocities,
@@ -1415,10 +1431,14 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
 
 // One work item of k_g2p2g; P is the item's scene.  LAGGED: the F update
 // uses the B of the previous G2P (the reference's order), else the B just
-// gathered.
-template <typename T, bool TRACK_FP, bool LAGGED, bool PAIRS, bool END_BARRIER>
+// gathered.  The item's grid tile is in S.graw; once it is converted,
+// thread 0 copies the next item's tile (nit) in by TMA while this item runs,
+// with maps[0] for a single scene or maps[scene] for a batch scene that has a
+// map (the next item's scene parameters from the batch's table).  BATCH: P
+// is the item's scene copied to shared memory, and the item ends on a barrier.
+template <typename T, bool TRACK_FP, bool LAGGED, bool PAIRS, bool BATCH>
 __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
-                                           const int4 it, bool has_next, int4 nit, const DevParams<T>* nscene) {
+                                           const int4 it, bool has_next, int4 nit, const CUtensorMap* maps) {
     static_assert(!PAIRS || sizeof(T) == 4, "the record-pairs scatter is FP32");
     constexpr int CA = kBlk + 2;
     const vec4<T>* __restrict__ pin = static_cast<const vec4<T>*>(D.pin);
@@ -1469,8 +1489,14 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         for (int c = threadIdx.x; c < P2GTile<T, CA>::NC; c += blockDim.x) S.p.cnt[c] = 0;
         __syncthreads();
         // S.graw is free again: copy the next item's tile while this one runs
-        // (nscene: the next item's scene in a batch, else this item's)
-        if (threadIdx.x == 0 && has_next) issue_tile(nscene ? *nscene : P, D, S, nit, nscene ? nit.w : 0);
+        if (threadIdx.x == 0 && has_next) {
+            if constexpr (BATCH) {
+                if (nit.w < kBatchMaps)
+                    issue_tile(static_cast<const DevParams<T>*>(D.scenes)[nit.w], maps + nit.w, S, nit);
+            } else {
+                issue_tile(P, maps, S, nit);
+            }
+        }
         int rcell = 0xff, rrank = 0;  // this thread's record: cell and rank within it
         if (j < count) {
             const int s = it.y + j;
@@ -1538,41 +1564,50 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         // a single scene: the next item's first barrier (after its tile wait)
         // separates this flush from the next item's writes to shared memory; a
         // batch copies the next scene's parameters before that barrier
-        if (END_BARRIER) __syncthreads();
+        if (BATCH) __syncthreads();
     }
 }
 
 // BATCH: the work items belong to different scenes (D.scenes); otherwise all
-// to the scene P0.  PAIRS: the scatter's lane layout p2g_runs_pairs (FP32)
-// instead of p2g_runs; the autotuner picks one.
+// to the scene P0.  Tiles come by TMA with the maps of `maps` (TileMaps),
+// except in batch scenes past the first kBatchMaps, whose items load their
+// tiles with plain loads.  PAIRS: the scatter's lane layout p2g_runs_pairs
+// (FP32) instead of p2g_runs; the autotuner picks one.
 template <typename T, bool TRACK_FP, bool BATCH, bool LAGGED, bool PAIRS = false>
 __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlocks : 1)
-    k_g2p2g(DevParams<T> P0, DevBufs D) {
+    k_g2p2g(DevParams<T> P0, DevBufs D, const __grid_constant__ FusedMaps<BATCH> maps) {
     extern __shared__ __align__(128) unsigned char smem_fused[];
     FusedShared<T>& S =
         *reinterpret_cast<FusedShared<T>*>(smem_fused + ((128u - (smem_addr(smem_fused) & 127u)) & 127u));
     const DevParams<T>* scenes = static_cast<const DevParams<T>*>(D.scenes);
     const uint32_t nw = min(*D.nwork, D.work_cap);
-    if (threadIdx.x == 0) {
-        mbar_init(&S.tbar);
-        S.tmap_scene = -1;
-    }
+    if (threadIdx.x == 0) mbar_init(&S.tbar);
     __syncthreads();
     uint32_t wi = blockIdx.x;
     if (threadIdx.x == 0 && wi < nw) {
         const int4 it0 = D.work[wi];
-        if constexpr (BATCH) issue_tile(scenes[it0.w], D, S, it0, it0.w);
-        else issue_tile(P0, D, S, it0, 0);
+        if constexpr (BATCH) {
+            if (it0.w < kBatchMaps) issue_tile(scenes[it0.w], &maps.m[it0.w], S, it0);
+        } else {
+            issue_tile(P0, &maps.m[0], S, it0);
+        }
     }
-    // the tile of item k completes phase k & 1 of the mbarrier; the next
-    // item's copy is issued inside g2p2g_item once this tile is converted
+    // the k-th TMA tile of this CTA completes phase k & 1 of the mbarrier; the
+    // next item's copy is issued inside g2p2g_item once this tile is converted
     uint32_t parity = 0u;
     for (; wi < nw; wi += gridDim.x) {
         const int4 it = D.work[wi];
-        if constexpr (BATCH) copy_scene(S.par, D.scenes, it.w);
-        const bool arrived = mbar_wait(&S.tbar, parity, kTileWaitTries);
-        parity ^= 1u;
-        // every thread decides together (this barrier also publishes S.par)
+        bool arrived = true;
+        if constexpr (BATCH) {
+            copy_scene(S.par, D.scenes, it.w);
+            if (it.w >= kBatchMaps) load_tile(scenes[it.w], D, S, it);
+        }
+        if (!BATCH || it.w < kBatchMaps) {
+            arrived = mbar_wait(&S.tbar, parity, kTileWaitTries);
+            parity ^= 1u;
+        }
+        // every thread decides together (this barrier also publishes S.par
+        // and a loaded tile)
         if (__syncthreads_or(!arrived)) {
             if (threadIdx.x == 0) {
                 raise_flag(D.flags, 8u);
@@ -1589,10 +1624,9 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
         const bool has_next = wn < nw;
         const int4 nit = has_next ? D.work[wn] : make_int4(0, 0, 0, 0);
         if constexpr (BATCH)
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, true>(S.par, D, S, it, has_next, nit,
-                                                         has_next ? &scenes[nit.w] : nullptr);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, true>(S.par, D, S, it, has_next, nit, &maps.m[0]);
         else
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, false>(P0, D, S, it, has_next, nit, nullptr);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, false>(P0, D, S, it, has_next, nit, &maps.m[0]);
     }
 }
 

@@ -61,24 +61,18 @@ __device__ __forceinline__ void store_rows(T* __restrict__ dst, int r0, int cnt,
     for (int e = threadIdx.x; e < cnt * K; e += blockDim.x) d[e] = sh[e];
 }
 
-// Particles off .. off + n - 1 of planes holding ntot particles (one scene of
-// a batch, or all of a single scene), from structure-of-arrays input in
-// particle id order; particle i goes to slot off + i.  With keys (a single
-// scene, P its parameters) it also writes the first sort's keys and
-// histogram, as k_keys would: the loads from host memory bound this kernel,
-// so the keys cost nothing here.
+// The particle of row r0 + threadIdx.x of the caller's structure-of-arrays
+// input (r0: the block's first row); absent fields take their defaults
+// (B = 0, F_E = F_P = I, J_P = det F_P or 1, V = 0).  Called by every thread
+// of a kIoThreads block; false for a row past n.  p.id is not set.
 template <typename T>
-__global__ void __launch_bounds__(kIoThreads)
-    k_pack(int n, int off, int ntot, const T* __restrict__ x, const T* __restrict__ v, const T* __restrict__ B,
-           const T* __restrict__ FE, const T* __restrict__ FP, const T* __restrict__ Jp, const T* __restrict__ mass,
-           const T* __restrict__ vol, vec4<T>* __restrict__ pl, int track_fp, DevParams<T> P,
-           uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, uint32_t* __restrict__ bcount,
-           uint32_t* __restrict__ flags) {
-    __shared__ T sh[9 * kIoThreads];
-    const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
+__device__ __forceinline__ bool pack_row(int n, int r0, const T* __restrict__ x, const T* __restrict__ v,
+                                         const T* __restrict__ B, const T* __restrict__ FE, const T* __restrict__ FP,
+                                         const T* __restrict__ Jp, const T* __restrict__ mass,
+                                         const T* __restrict__ vol, Particle<T>& p, T (&FPm)[9], T* sh) {
+    const int i = r0 + threadIdx.x;
     const int cnt = min((int)blockDim.x, n - r0);
-    Particle<T> p;
-    T FPm[9], t3[3];
+    T t3[3];
     load_rows(x, r0, cnt, t3, sh);
 #pragma unroll
     for (int a = 0; a < 3; ++a) p.x[a] = t3[a];
@@ -103,10 +97,31 @@ __global__ void __launch_bounds__(kIoThreads)
 #pragma unroll
         for (int e = 0; e < 9; ++e) FPm[e] = (e % 4 == 0) ? T(1) : T(0);
     }
-    if (i >= n) return;
+    if (i >= n) return false;
     p.m = mass[i];
     p.vol = vol ? vol[i] : T(0);
     p.Jp = Jp ? Jp[i] : (FP ? det3(FPm) : T(1));
+    return true;
+}
+
+// Particles off .. off + n - 1 of planes holding ntot particles (one scene of
+// a batch, or all of a single scene), from structure-of-arrays input in
+// particle id order; particle i goes to slot off + i.  With keys (a single
+// scene, P its parameters) it also writes the first sort's keys and
+// histogram, as k_keys would: the loads from host memory bound this kernel,
+// so the keys cost nothing here.
+template <typename T>
+__global__ void __launch_bounds__(kIoThreads)
+    k_pack(int n, int off, int ntot, const T* __restrict__ x, const T* __restrict__ v, const T* __restrict__ B,
+           const T* __restrict__ FE, const T* __restrict__ FP, const T* __restrict__ Jp, const T* __restrict__ mass,
+           const T* __restrict__ vol, vec4<T>* __restrict__ pl, int track_fp, DevParams<T> P,
+           uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, uint32_t* __restrict__ bcount,
+           uint32_t* __restrict__ flags) {
+    __shared__ T sh[9 * kIoThreads];
+    const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
+    Particle<T> p;
+    T FPm[9];
+    if (!pack_row(n, r0, x, v, B, FE, FP, Jp, mass, vol, p, FPm, sh)) return;
     p.id = (uint32_t)(off + i);
     store_particle(pl, (size_t)ntot, (size_t)(off + i), p);
     if (track_fp) store_fp(pl, (size_t)ntot, (size_t)(off + i), FPm);
@@ -117,6 +132,63 @@ __global__ void __launch_bounds__(kIoThreads)
         keys[off + i] = key;
         count_key(counts, bcount, key);
     }
+}
+
+// An upload in sorted order (a single scene of n particles), pass 1: the
+// positions alone, for the sort's keys and histogram (as k_pack writes them);
+// xcopy (may be null) keeps the rows on the device for pass 2, so the host
+// link carries them once.
+template <typename T>
+__global__ void __launch_bounds__(kIoThreads)
+    k_pack_keys(int n, const T* __restrict__ x, T* __restrict__ xcopy, DevParams<T> P, uint32_t* __restrict__ keys,
+                uint32_t* __restrict__ counts, uint32_t* __restrict__ bcount, uint32_t* __restrict__ flags) {
+    __shared__ T sh[3 * kIoThreads];
+    const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
+    const int cnt = min((int)blockDim.x, n - r0);
+    T t3[3];
+    load_rows(x, r0, cnt, t3, sh);
+    if (xcopy) store_rows(xcopy, r0, cnt, t3, sh);
+    if (i >= n) return;
+    const int b[3] = {base_of(t3[0], P.h), base_of(t3[1], P.h), base_of(t3[2], P.h)};
+    if (!stencil_in_grid(P, b)) raise_flag(flags, 1u);
+    const uint32_t key = sort_key(P, b);
+    keys[i] = key;
+    count_key(counts, bcount, key);
+}
+
+// Pass 2 (after the scan): each particle goes straight to its sorted slot -
+// the scan's cursor of its key, taken as k_scatter takes it - so the
+// permutation is the identity and the first step's P2G reads the particles
+// in order.  The host link bounds the pass; the scattered 16-byte stores
+// merge in L2.
+template <typename T>
+__global__ void __launch_bounds__(kIoThreads)
+    k_pack_place(int n, const T* __restrict__ x, const T* __restrict__ v, const T* __restrict__ B,
+                 const T* __restrict__ FE, const T* __restrict__ FP, const T* __restrict__ Jp,
+                 const T* __restrict__ mass, const T* __restrict__ vol, vec4<T>* __restrict__ pl, int track_fp,
+                 const uint32_t* __restrict__ keys, uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm,
+                 uint32_t* __restrict__ flags) {
+    __shared__ T sh[9 * kIoThreads];
+    const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
+    Particle<T> p;
+    T FPm[9];
+    if (!pack_row(n, r0, x, v, B, FE, FP, Jp, mass, vol, p, FPm, sh)) return;
+    p.id = (uint32_t)i;
+    const uint32_t key = keys[i];
+    const uint32_t peers = __match_any_sync(__activemask(), key);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(cursor + key, (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    const uint32_t slot = base + __popc(peers & lanemask_lt());
+    if (slot >= (uint32_t)n) {  // counts that do not add up to n (flagged by the scan too)
+        raise_flag(flags, 4u);
+        return;
+    }
+    store_particle(pl, (size_t)n, (size_t)slot, p);
+    if (track_fp) store_fp(pl, (size_t)n, (size_t)slot, FPm);
+    perm[slot] = slot;
 }
 
 // The slot of each particle of a scene (particles off .. off + n - 1 in
@@ -286,7 +358,8 @@ struct rd_handle {
     int col_mode = RD_COLLIDE_REFERENCE;
     double col_mu = 0.5;
     void* d_col = nullptr;          // Collider<T>[RD_MAX_COLLIDERS]
-    void* d_tmaps = nullptr;        // CUtensorMap per grid buffer and scene, [2][nscenes]
+    TileMaps<1> smaps[2] = {};      // TMA maps of grid[0], grid[1] (single scene; kernel parameters)
+    TileMaps<kBatchMaps>* bmaps = nullptr;  // [2]: the same per scene of a batch (the first kBatchMaps)
     int wp = 0;         // particles per work item (<= WorkP)
     int grid_mult = 0;  // persistent CTAs per SM of the step kernels (0: occupancy)
     int scatter = RD_SCATTER_LANE_PAIRS;     // lane layout of the fused kernel's P2G scatter
@@ -323,6 +396,7 @@ struct rd_handle {
     void* grid[2] = {nullptr, nullptr};  // (m, p) of this step / the next (fused); (m, v) in stage mode
     int g = 0;                           // current grid buffer
     bool fgrid_valid = false;            // grid[g] holds P2G(x) for rd_step with fgrid_dt
+    bool in_order = false;               // planes in the current sort's slot order (perm the identity)
     double fgrid_dt = 0.0;
     void* gforce = nullptr;
     uint32_t* flags = nullptr;
@@ -476,7 +550,6 @@ template <typename T> DevBufs bufs(rd_handle* h) {
     D.spoff = h->d_spoff;
     D.nscenes = (int)h->scenes.size();
     D.colliders = h->d_col;
-    D.tmaps = static_cast<const char*>(h->d_tmaps) + (size_t)h->g * h->scenes.size() * sizeof(CUtensorMap);
     return D;
 }
 
@@ -539,14 +612,16 @@ template <typename T> int work_size(const rd_handle* h) {
 }
 
 // Sort by block key: histogram (unless the last fused G2P already counted),
-// scan + work items, scatter into perm.
-template <typename T> rd_status sort_particles(rd_handle* h) {
+// scan + work items, scatter into perm (unless the caller places the
+// particles by the scan's cursors itself: scatter false).
+template <typename T> rd_status sort_particles(rd_handle* h, bool scatter = true) {
     if (h->n == 0) {
         RD_TRY(check_cuda(h, cudaMemsetAsync(h->nwork2, 0, 2 * sizeof(uint32_t), h->stream), "memset nwork"));
         h->sorted = true;
         return RD_OK;
     }
     DevParams<T> P = make_params<T>(h, 0.0, T(0));
+    h->in_order = false;  // a new permutation
     if (!h->keys_valid) {
         RD_TRY(check_cuda(h, cudaMemsetAsync(h->counts, 0, sizeof(uint32_t) * h->nkeys, h->stream), "memset counts"));
         RD_TRY(check_cuda(h, cudaMemsetAsync(h->bcount, 0, sizeof(uint32_t) * h->nblocks, h->stream), "memset counts"));
@@ -586,10 +661,12 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
     tmark_end(h, t);
     RD_TRY(launched(h, "k_scan", 2));
     h->nb ^= 1;
-    t = tmark_begin(h, RD_KERNEL_SCATTER);
-    k_scatter<<<blocks_for(h->n, 256), 256, 0, h->stream>>>(h->n, h->keys[h->cur], h->cursor, h->perm);
-    tmark_end(h, t);
-    RD_TRY(launched(h, "k_scatter"));
+    if (scatter) {
+        t = tmark_begin(h, RD_KERNEL_SCATTER);
+        k_scatter<<<blocks_for(h->n, 256), 256, 0, h->stream>>>(h->n, h->keys[h->cur], h->cursor, h->perm);
+        tmark_end(h, t);
+        RD_TRY(launched(h, "k_scatter"));
+    }
     h->keys_valid = false;  // counts consumed
     h->sorted = true;
     return RD_OK;
@@ -597,22 +674,30 @@ template <typename T> rd_status sort_particles(rd_handle* h) {
 
 // The k_g2p2g instantiation for this handle: batch or single scene, with or
 // without the full F_P, and the order of the F update.
-template <typename T> using FusedKernel = void (*)(DevParams<T>, DevBufs);
+template <typename T> using SingleFused = void (*)(DevParams<T>, DevBufs, const FusedMaps<false>);
+template <typename T> using BatchFused = void (*)(DevParams<T>, DevBufs, const FusedMaps<true>);
 // Scatter layouts a handle can use: both for FP32 with the lagged-B order and
 // J_P only (the instantiations the record-pairs layout is compiled for), else
 // the lane-pairs layout alone.
 int scatter_layouts(const rd_handle* h) {
     return h->prm.precision == RD_FP32 && h->prm.lagged_b && !h->prm.track_fp ? 2 : 1;
 }
-template <typename T> FusedKernel<T> fused_kernel(const rd_handle* h) {
+template <typename T> BatchFused<T> batch_fused_kernel(const rd_handle* h) {
+    if constexpr (sizeof(T) == 4) {
+        if (h->scatter == RD_SCATTER_RECORD_PAIRS && scatter_layouts(h) > 1) return k_g2p2g<T, false, true, true, true>;
+    }
+    return h->prm.lagged_b ? k_g2p2g<T, false, true, true> : k_g2p2g<T, false, true, false>;
+}
+template <typename T> SingleFused<T> single_fused_kernel(const rd_handle* h) {
     const bool lag = h->prm.lagged_b != 0;
     if constexpr (sizeof(T) == 4) {
-        if (h->scatter == RD_SCATTER_RECORD_PAIRS && scatter_layouts(h) > 1)
-            return batched(h) ? k_g2p2g<T, false, true, true, true> : k_g2p2g<T, false, false, true, true>;
+        if (h->scatter == RD_SCATTER_RECORD_PAIRS && scatter_layouts(h) > 1) return k_g2p2g<T, false, false, true, true>;
     }
-    if (batched(h)) return lag ? k_g2p2g<T, false, true, true> : k_g2p2g<T, false, true, false>;
     if (h->prm.track_fp) return lag ? k_g2p2g<T, true, false, true> : k_g2p2g<T, true, false, false>;
     return lag ? k_g2p2g<T, false, false, true> : k_g2p2g<T, false, false, false>;
+}
+template <typename T> const void* fused_kernel(const rd_handle* h) {
+    return batched(h) ? (const void*)batch_fused_kernel<T>(h) : (const void*)single_fused_kernel<T>(h);
 }
 
 template <typename T> unsigned persistent_grid(const rd_handle* h, int occ) {
@@ -671,7 +756,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
         // plane buffer in order, so the fused kernel reads them sequentially.
         // Not in the adjoint's stored segments, whose plane buffers are the
         // store's slots.
-        const bool reorder = !h->split_out && !h->prm.track_fp;
+        const bool reorder = !h->split_out && !h->prm.track_fp && !h->in_order;
         if (reorder) {
             D.reorder_out = h->pl[h->cur ^ 1];
             D.perm_reset = h->perm;
@@ -696,7 +781,10 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
     DevBufs D = bufs<T>(h);
     t = tmark_begin(h, RD_KERNEL_G2P2G);
     const unsigned fg = persistent_grid<T>(h, h->occ_g2p);
-    fused_kernel<T>(h)<<<fg, kFusedThreads, fused_smem_bytes<T>(), h->stream>>>(P, D);
+    if (batch)
+        batch_fused_kernel<T>(h)<<<fg, kFusedThreads, fused_smem_bytes<T>(), h->stream>>>(P, D, h->bmaps[h->g]);
+    else
+        single_fused_kernel<T>(h)<<<fg, kFusedThreads, fused_smem_bytes<T>(), h->stream>>>(P, D, h->smaps[h->g]);
     tmark_end(h, t);
     RD_TRY(launched(h, "k_g2p2g"));
     h->cur ^= 1;
@@ -847,6 +935,33 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, cons
     if (keys) {
         RD_TRY(check_cuda(h, cudaMemsetAsync(h->counts, 0, sizeof(uint32_t) * h->nkeys, h->stream), "memset counts"));
         RD_TRY(check_cuda(h, cudaMemsetAsync(h->bcount, 0, sizeof(uint32_t) * h->nblocks, h->stream), "memset counts"));
+    }
+    // A single scene after its first step: the upload sorts the particles on
+    // the way in - keys from the positions, the scan, then every particle to
+    // its sorted slot - so the next step's P2G reads them in order.  It
+    // replaces the step's scatter, its permuted-read P2G and its reordering
+    // copy; the first upload keeps the one-pass route (k_pack), which costs
+    // less when the particles' order is not yet that of a sort.
+    if (keys && h->last_dt > 0.0 && !h->split_out) {
+        const DevParams<T> P = make_params<T>(h, 0.0, T(0));
+        const unsigned nb = blocks_for(n, kIoThreads);
+        k_pack_keys<T><<<nb, kIoThreads, 0, h->stream>>>((int)n, ptr[0], ptr[0] == d[0] ? nullptr : d[0], P,
+                                                         h->keys[h->cur], h->counts, h->bcount, h->flags);
+        RD_TRY(launched(h, "k_pack_keys"));
+        h->keys_valid = true;
+        h->sorted = false;
+        RD_TRY(sort_particles<T>(h, false));
+        k_pack_place<T><<<nb, kIoThreads, 0, h->stream>>>(
+            (int)n, d[0], ptr[1], ptr[2], ptr[3], ptr[4], ptr[5], ptr[6], ptr[7], static_cast<vec4<T>*>(h->pl[h->cur]),
+            h->prm.track_fp, h->keys[h->cur], h->cursor, h->perm, h->flags);
+        RD_TRY(launched(h, "k_pack_place"));
+        sc.set = true;
+        h->keys_valid = false;
+        h->sorted = true;
+        h->in_order = true;
+        h->fgrid_valid = false;
+        h->grid_mode = GRID_NONE;
+        return RD_OK;
     }
     if (n > 0) {
         k_pack<T><<<blocks_for(n, kIoThreads), kIoThreads, 0, h->stream>>>(
@@ -1061,11 +1176,13 @@ void release(rd_handle* h) {
     void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->slot_of, h->counts, h->bcount, h->gmark[0],
                     h->gmark[1], h->cursor, h->work,
                     h->nwork2, h->tile_sums, h->tile_list, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
-                    h->d_col, h->d_tmaps, h->rgba, h->zid, h->img,
+                    h->d_col, h->rgba, h->zid, h->img,
                     h->d_scenes, h->d_sblock, h->d_spoff};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->h_scenes) cudaFreeHost(h->h_scenes);
+    delete[] h->bmaps;
+    h->bmaps = nullptr;
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->side) cudaStreamDestroy(h->side);
@@ -1114,9 +1231,12 @@ bool valid_scene(const rd_params& p) {
 // sorted order too, since the block keys of scene s precede those of s + 1),
 // its grid nodes [goff_s, goff_s + cells_s) of each grid buffer.
 // Tensor maps of both grid buffers for the fused kernel's tile copies: per
-// scene, its grid region as a 4-D tensor (channel, z, y, x) of the element
-// type, box 4 x kTile^3; nodes outside the region read as zero.  The encoder
-// is the driver's cuTensorMapEncodeTiled, fetched through the runtime.
+// scene (the first kBatchMaps of a batch), its grid region as a 4-D tensor
+// (channel, z, y, x) of the element type, box 4 x kTile^3; nodes outside the
+// region read as zero.  They are passed by value as the kernel's
+// __grid_constant__ parameter (TileMaps), so no map is read from memory the
+// host writes.  The encoder is the driver's cuTensorMapEncodeTiled, fetched
+// through the runtime.
 rd_status encode_tile_maps(rd_handle* h) {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     static std::mutex mu;
@@ -1132,28 +1252,31 @@ rd_status encode_tile_maps(rd_handle* h) {
             encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
         }
     }
-    const size_t ns = h->scenes.size();
-    std::vector<CUtensorMap> maps(2 * ns);
+    const bool batch = batched(h);
+    if (batch) {
+        h->bmaps = new (std::nothrow) TileMaps<kBatchMaps>[2]();
+        if (!h->bmaps) return fail(h, RD_OOM, "tensor maps");
+    }
+    const size_t ns = std::min<size_t>(h->scenes.size(), kBatchMaps);
     const cuuint64_t es = (cuuint64_t)h->esize;
-    for (int b = 0; b < 2; ++b)
-        for (size_t s = 0; s < ns; ++s) {
-            const rd_scene_info& sc = h->scenes[s];
-            const cuuint64_t M0 = (cuuint64_t)sc.prm.max_i, M1 = (cuuint64_t)sc.prm.max_j, M2 = (cuuint64_t)sc.prm.max_k;
-            const cuuint64_t dims[4] = {4, M2, M1, M0};
-            const cuuint64_t strides[3] = {4 * es, 4 * es * M2, 4 * es * M2 * M1};
-            const cuuint32_t box[4] = {4, (cuuint32_t)kTile, (cuuint32_t)kTile, (cuuint32_t)kTile};
-            const cuuint32_t estr[4] = {1, 1, 1, 1};
-            void* base = static_cast<char*>(h->grid[b]) + sc.goff * 4 * es;
-            const CUresult r = encode(&maps[b * ns + s],
-                                      es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base,
-                                      dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-            if (r != CUDA_SUCCESS) return fail(h, RD_CUDA_ERROR, "tensor map of a grid tile");
-        }
-    RD_TRY(check_cuda(h, cudaMalloc(&h->d_tmaps, maps.size() * sizeof(CUtensorMap)), "tensor maps"));
-    return check_cuda(h, cudaMemcpy(h->d_tmaps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice),
-                      "tensor maps");
+    for (size_t k = 0; k < 2 * ns; ++k) {
+        const int b = (int)(k / ns);
+        const size_t s = k % ns;
+        const rd_scene_info& sc = h->scenes[s];
+        const cuuint64_t M0 = (cuuint64_t)sc.prm.max_i, M1 = (cuuint64_t)sc.prm.max_j, M2 = (cuuint64_t)sc.prm.max_k;
+        const cuuint64_t dims[4] = {4, M2, M1, M0};
+        const cuuint64_t strides[3] = {4 * es, 4 * es * M2, 4 * es * M2 * M1};
+        const cuuint32_t box[4] = {4, (cuuint32_t)kTile, (cuuint32_t)kTile, (cuuint32_t)kTile};
+        const cuuint32_t estr[4] = {1, 1, 1, 1};
+        void* base = static_cast<char*>(h->grid[b]) + sc.goff * 4 * es;
+        const CUresult r = encode(batch ? &h->bmaps[b].m[s] : &h->smaps[b].m[0],
+                                  es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base,
+                                  dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(h, RD_CUDA_ERROR, "tensor map of a grid tile");
+    }
+    return RD_OK;
 }
 
 rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
@@ -1264,8 +1387,12 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
         for (int s = 0; s < nscenes; ++s) { sb[s] = h->scenes[s].block_base; sp[s] = h->scenes[s].poff; }
         sb[nscenes] = (uint32_t)blocks;
         sp[nscenes] = (uint32_t)ntot;
-        if (cudaMemcpy(h->d_sblock, sb.data(), sb.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(h->d_spoff, sp.data(), sp.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+        // in the handle's stream (a plain cudaMemcpy from pageable memory may
+        // return before its data lands, and the handle's streams do not wait
+        // for the legacy stream); the creation's final synchronisation covers it
+        if (cudaMemcpyAsync(h->d_sblock, sb.data(), sb.size() * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+            cudaMemcpyAsync(h->d_spoff, sp.data(), sp.size() * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+            cudaStreamSynchronize(h->stream) != cudaSuccess)
             return bail(RD_CUDA_ERROR);
     }
     cudaMemsetAsync(h->counts, 0, (size_t)h->nkeys * 4, h->stream);
@@ -2269,9 +2396,14 @@ template <typename T> rd_status upload_colliders(rd_handle* h) {
     for (size_t k = 0; k < d.size(); ++k) d[k] = device_collider<T>(h->cols[k]);
     // the previous set may still be read by queued steps
     RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "sync"));
-    if (!d.empty())
-        RD_TRY(check_cuda(h, cudaMemcpy(h->d_col, d.data(), d.size() * sizeof(Collider<T>), cudaMemcpyHostToDevice),
+    // in stream order with the steps that read them (a plain cudaMemcpy from
+    // pageable memory may return before its data lands)
+    if (!d.empty()) {
+        RD_TRY(check_cuda(h, cudaMemcpyAsync(h->d_col, d.data(), d.size() * sizeof(Collider<T>), cudaMemcpyHostToDevice,
+                                             h->stream),
                           "colliders"));
+        RD_TRY(check_cuda(h, cudaStreamSynchronize(h->stream), "sync"));
+    }
     return RD_OK;
 }
 

@@ -154,8 +154,7 @@ def implicit():
     vel_ref = r.grid()["vel"]
     return {"grid": np.array([G, G, G]), "h": np.float32(h), "dt": np.float32(dt), "n": n, "x0": x, "v0": v,
             "m0": m, "FE0": FE, "vol0": r.particles()["vol"], "gmass": g["mass"], "vstar": g["vel"],
-            "fields": np.stack(fields), "energies": energies, "vel_ref": vel_ref,
-            "energy_ref": np.float32(r.energy(vel_ref, dt))}
+            "fields": np.stack(fields), "energies": energies, "vel_ref": vel_ref}
 
 
 FIXTURES = {"ref_scene_20": ref_scene, "perturbed_16": perturbed, "colliders_32": colliders, "implicit_12": implicit}
