@@ -27,17 +27,24 @@ __device__ __forceinline__ dvec4 ld_stream(const dvec4* p) {
     dvec4 r; r.x = a.x; r.y = a.y; r.z = b.x; r.w = b.y; return r;
 }
 __device__ __forceinline__ void st_stream(float4* p, float4 v) { __stcs(p, v); }
+// Half k (0: x, y; 1: z, w) of a plane element.
+__device__ __forceinline__ void st_stream_half(float4* p, int k, float a, float b) {
+    __stcs(reinterpret_cast<float2*>(p) + k, make_float2(a, b));
+}
 __device__ __forceinline__ void st_stream(dvec4* p, dvec4 v) {
     double2* q = reinterpret_cast<double2*>(p);
     __stcs(q, make_double2(v.x, v.y)); __stcs(q + 1, make_double2(v.z, v.w));
+}
+__device__ __forceinline__ void st_stream_half(dvec4* p, int k, double a, double b) {
+    __stcs(reinterpret_cast<double2*>(p) + k, make_double2(a, b));
 }
 
 // ---------------------------------------------------------------- state
 // Particle state: 7 planes of vec4 (structure of arrays of 16/32-byte
 // vectors, so every plane access of a warp is one fully coalesced request):
 //   0: x y z mass      1: vx vy vz volume
-//   2: B00 B01 B02 B10 3: B11 B12 B20 B21   4: B22 F00 F01 F02
-//   5: F10 F11 F12 F20 6: F21 F22 Jp id
+//   2: B00 B01 B02 B10 3: B11 B12 B20 B21   4: F00 F01 F02 F10
+//   5: F11 F12 F20 F21 6: F22 Jp B22 id
 // B is the reference's APIC matrix (C = B * DpInverse), F the elastic F_E,
 // Jp = det F_P, id the particle's original index.  With track_fp three more
 // planes carry the full plastic F_P: 7: P00 P01 P02 P10  8: P11 P12 P20 P21
@@ -66,13 +73,15 @@ __device__ __forceinline__ void load_particle(const vec4<T>* __restrict__ pl, si
     p.v[0] = b.x; p.v[1] = b.y; p.v[2] = b.z; p.vol = b.w;
     p.B[0] = c.x; p.B[1] = c.y; p.B[2] = c.z; p.B[3] = c.w;
     p.B[4] = d.x; p.B[5] = d.y; p.B[6] = d.z; p.B[7] = d.w;
-    p.B[8] = e.x; p.F[0] = e.y; p.F[1] = e.z; p.F[2] = e.w;
-    p.F[3] = f.x; p.F[4] = f.y; p.F[5] = f.z; p.F[6] = f.w;
-    p.F[7] = g.x; p.F[8] = g.y; p.Jp = g.z; p.id = real_to_id<T>(g.w);
+    p.F[0] = e.x; p.F[1] = e.y; p.F[2] = e.z; p.F[3] = e.w;
+    p.F[4] = f.x; p.F[5] = f.y; p.F[6] = f.z; p.F[7] = f.w;
+    p.F[8] = g.x; p.Jp = g.y; p.B[8] = g.z; p.id = real_to_id<T>(g.w);
 }
 
-// Planes 0-4 (x, m, v, volume, B, F00..F02) and planes 5-6 (F10..F22, J_P,
-// id) can be stored apart: the F_E / J_P part is final before the G2P gather.
+// The F_E / J_P part of a particle (planes 4 and 5 and the first half of
+// plane 6) is final before the G2P gather and is stored apart from the rest
+// (planes 0-3 and the second half of plane 6), so none of F is live across
+// the gather.
 template <typename T>
 __device__ __forceinline__ void store_particle_front(vec4<T>* __restrict__ pl, size_t n, size_t i,
                                                      const Particle<T>& p) {
@@ -80,18 +89,24 @@ __device__ __forceinline__ void store_particle_front(vec4<T>* __restrict__ pl, s
     st_stream(pl + 1 * n + i, mk4<T>(p.v[0], p.v[1], p.v[2], p.vol));
     st_stream(pl + 2 * n + i, mk4<T>(p.B[0], p.B[1], p.B[2], p.B[3]));
     st_stream(pl + 3 * n + i, mk4<T>(p.B[4], p.B[5], p.B[6], p.B[7]));
-    st_stream(pl + 4 * n + i, mk4<T>(p.B[8], p.F[0], p.F[1], p.F[2]));
+    st_stream_half(pl + 6 * n + i, 1, p.B[8], id_to_real<T>(p.id));
 }
 template <typename T>
 __device__ __forceinline__ void store_particle_back(vec4<T>* __restrict__ pl, size_t n, size_t i,
                                                     const Particle<T>& p) {
-    st_stream(pl + 5 * n + i, mk4<T>(p.F[3], p.F[4], p.F[5], p.F[6]));
-    st_stream(pl + 6 * n + i, mk4<T>(p.F[7], p.F[8], p.Jp, id_to_real<T>(p.id)));
+    st_stream(pl + 4 * n + i, mk4<T>(p.F[0], p.F[1], p.F[2], p.F[3]));
+    st_stream(pl + 5 * n + i, mk4<T>(p.F[4], p.F[5], p.F[6], p.F[7]));
+    st_stream_half(pl + 6 * n + i, 0, p.F[8], p.Jp);
 }
 template <typename T>
 __device__ __forceinline__ void store_particle(vec4<T>* __restrict__ pl, size_t n, size_t i, const Particle<T>& p) {
-    store_particle_front(pl, n, i, p);
-    store_particle_back(pl, n, i, p);
+    st_stream(pl + 0 * n + i, mk4<T>(p.x[0], p.x[1], p.x[2], p.m));
+    st_stream(pl + 1 * n + i, mk4<T>(p.v[0], p.v[1], p.v[2], p.vol));
+    st_stream(pl + 2 * n + i, mk4<T>(p.B[0], p.B[1], p.B[2], p.B[3]));
+    st_stream(pl + 3 * n + i, mk4<T>(p.B[4], p.B[5], p.B[6], p.B[7]));
+    st_stream(pl + 4 * n + i, mk4<T>(p.F[0], p.F[1], p.F[2], p.F[3]));
+    st_stream(pl + 5 * n + i, mk4<T>(p.F[4], p.F[5], p.F[6], p.F[7]));
+    st_stream(pl + 6 * n + i, mk4<T>(p.F[8], p.Jp, p.B[8], id_to_real<T>(p.id)));
 }
 
 // The plastic split F* = U diag(s) V^T of one particle (U, V row-major) and

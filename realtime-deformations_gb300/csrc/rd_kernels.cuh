@@ -5,6 +5,8 @@
 // and the stage kernels serve rd_stage, which runs the reference's seven
 // stages one by one (material_point_method.cpp:94-350).
 #pragma once
+#include <cuda.h>  // CUtensorMap (TileMaps)
+
 #include "rd_device.cuh"
 
 namespace rd {
@@ -63,6 +65,13 @@ struct DevBufs {
     // in order (null: no copy)
     void* reorder_out;
     uint32_t* perm_reset;
+    // k_p2g with the force: P F^T of each particle, computed during an upload
+    // (3 vec4 planes by slot, row-major, the last 3 entries unused), read
+    // instead of computed (null: computed)
+    const void* stress;
+    // fused kernel, single scene: slot_of[id] = the sorted slot each particle
+    // is written to, for the next download (null: not kept)
+    uint32_t* slot_of;
     uint32_t* bcount;  // particles per 4x4x4 block (the block sums of counts)
     uint8_t* gmark;       // blocks of grid that hold data (set by every writer)
     uint8_t* gmark_next;  // the same for grid_next
@@ -491,6 +500,22 @@ __device__ __forceinline__ void stress_PFt_svd(const DevParams<T>& P, const T F[
         for (int c = 0; c < 3; ++c)
             out[3 * r + c] = U[3 * r] * dg[0] * U[3 * c] + U[3 * r + 1] * dg[1] * U[3 * c + 1] +
                              U[3 * r + 2] * dg[2] * U[3 * c + 2] + (r == c ? iso : T(0));
+}
+
+// The 9 entries of P F^T as 3 vec4 planes of n elements (the stress of the
+// first P2G after an upload, computed while the upload is bound by the link).
+template <typename T>
+__device__ __forceinline__ void store_stress(vec4<T>* __restrict__ st, size_t n, size_t i, const T G[9]) {
+    st[i] = mk4<T>(G[0], G[1], G[2], G[3]);
+    st[n + i] = mk4<T>(G[4], G[5], G[6], G[7]);
+    st[2 * n + i] = mk4<T>(G[8], T(0), T(0), T(0));
+}
+template <typename T>
+__device__ __forceinline__ void load_stress(const vec4<T>* __restrict__ st, size_t n, size_t i, T G[9]) {
+    const vec4<T> a = st[i], b = st[n + i], c = st[2 * n + i];
+    G[0] = a.x; G[1] = a.y; G[2] = a.z; G[3] = a.w;
+    G[4] = b.x; G[5] = b.y; G[6] = b.z; G[7] = b.w;
+    G[8] = c.x;
 }
 
 template <typename T>
@@ -1165,7 +1190,7 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
     tile_origin(P, it.x, org);
     const int count = min(it.z, min(WorkP<T>::value, P.n - it.y));
     __syncthreads();
-    bool stray = false;  // a record outside the cell space
+    bool stray = false;  // a record outside the cell space, or one whose cell is not its key's
     // phase 1: a record per particle
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         Particle<T> p;
@@ -1181,7 +1206,12 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
             stray = true;
             continue;
         }
-        if (!stencil_in_grid(P, St.b)) raise_flag(D.flags, 1u);
+        if (!stencil_in_grid(P, St.b)) {
+            raise_flag(D.flags, 1u);
+            // a base cell past the grid's end was clamped in its sort key, so
+            // its record's cell need not be its key's: sort the records
+            stray = stray || St.b[0] > P.M[0] - 1 || St.b[1] > P.M[1] - 1 || St.b[2] > P.M[2] - 1;
+        }
         T A[9];
         T mv[3] = {T(0), T(0), T(0)};
 #pragma unroll
@@ -1194,7 +1224,8 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
         }
         if (FORCE) {
             T G[9];
-            stress_PFt(P, p.F, p.Jp, G);
+            if (D.stress) load_stress(static_cast<const vec4<T>*>(D.stress), n, D.perm[it.y + j], G);
+            else stress_PFt(P, p.F, p.Jp, G);
             const T sc = P.fscale * (p.vol * P.dinv);
 #pragma unroll
             for (int e = 0; e < 9; ++e) A[e] -= sc * G[e];
@@ -1206,16 +1237,27 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
         S.scell[j] = (uint8_t)cell;
     }
     // The item is a run of the global sort by cell key and nothing has moved
-    // since, so its records are grouped by cell already, in item order; only
-    // a particle outside the cell space (flagged above) needs the record sort.
+    // since, so its records are grouped by cell already, in item order: the
+    // slot after each cell's last record is its run's end (p2g_runs reads
+    // off + cnt, so off = 0 and cnt = end).  Only a particle outside the cell
+    // space or with a clamped key (flagged above) needs the record sort.
     int total = count;
     if (__syncthreads_or(stray)) {
         for (int j = threadIdx.x; j < count; j += blockDim.x)
             if (S.cellof[j] != 0xff) atomicAdd(&S.cnt[S.cellof[j]], 1);
         sort_records<T, kBlk>(S, count);
         total = sorted_total(S);
+    } else {
+        for (int j = threadIdx.x; j < count; j += blockDim.x) {
+            const int c = S.scell[j];
+            if (j + 1 == count || S.scell[j + 1] != c) {
+                S.off[c] = 0;
+                S.cnt[c] = j + 1;
+            }
+        }
+        __syncthreads();
     }
-    p2g_tasks<T, MOM, kBlk>(S, total);
+    p2g_runs<T, MOM, kBlk>(S, total);
     __syncthreads();
     p2g_flush<T, kBlk>(P, S, org, grid);
     if (MOM) mark_around(P, D.gmark, it.x);
@@ -1522,6 +1564,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
 #pragma unroll
             for (int a = 0; a < 3; ++a) p.x[a] = clampx(p.x[a] + p.v[a] * P.dt, P.xlo, P.xhi[a]);
             store_particle_front(pout, n, s, p);
+            if (D.slot_of && p.id < (uint32_t)n) D.slot_of[p.id] = (uint32_t)s;
             {
                 T sum = (p.x[0] + p.x[1]) + (p.x[2] + p.v[0]) + (p.v[1] + p.v[2]);
 #pragma unroll

@@ -159,15 +159,18 @@ __global__ void __launch_bounds__(kIoThreads)
 // Pass 2 (after the scan): each particle goes straight to its sorted slot -
 // the scan's cursor of its key, taken as k_scatter takes it - so the
 // permutation is the identity and the first step's P2G reads the particles
-// in order.  The host link bounds the pass; the scattered 16-byte stores
-// merge in L2.
+// in order; with `stress`, also its P F^T (stress_PFt, P the scene's
+// material), which that P2G then reads instead of computing.  The host link
+// bounds the pass, so the SVD costs nothing here; the scattered 16-byte
+// stores merge in L2.
 template <typename T>
 __global__ void __launch_bounds__(kIoThreads)
     k_pack_place(int n, const T* __restrict__ x, const T* __restrict__ v, const T* __restrict__ B,
                  const T* __restrict__ FE, const T* __restrict__ FP, const T* __restrict__ Jp,
                  const T* __restrict__ mass, const T* __restrict__ vol, vec4<T>* __restrict__ pl, int track_fp,
                  const uint32_t* __restrict__ keys, uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm,
-                 uint32_t* __restrict__ flags) {
+                 uint32_t* __restrict__ flags, DevParams<T> P, vec4<T>* __restrict__ stress,
+                 uint32_t* __restrict__ slot_of) {
     __shared__ T sh[9 * kIoThreads];
     const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
     Particle<T> p;
@@ -189,6 +192,12 @@ __global__ void __launch_bounds__(kIoThreads)
     store_particle(pl, (size_t)n, (size_t)slot, p);
     if (track_fp) store_fp(pl, (size_t)n, (size_t)slot, FPm);
     perm[slot] = slot;
+    slot_of[i] = slot;
+    if (stress) {
+        T G[9];
+        stress_PFt(P, p.F, p.Jp, G);
+        store_stress(stress, (size_t)n, (size_t)slot, G);
+    }
 }
 
 // The slot of each particle of a scene (particles off .. off + n - 1 in
@@ -397,6 +406,11 @@ struct rd_handle {
     int g = 0;                           // current grid buffer
     bool fgrid_valid = false;            // grid[g] holds P2G(x) for rd_step with fgrid_dt
     bool in_order = false;               // planes in the current sort's slot order (perm the identity)
+    bool clean_grids = false;            // both grid buffers zero and unmarked (cleared during an upload)
+    void* stress = nullptr;              // P F^T of each particle by slot (3 vec4), from an upload
+    bool stress_valid = false;           // stress holds the current state's
+    bool slot_of_valid = false;          // slot_of holds the current state's (single scene)
+    bool after_upload = false;           // the next step is the first after rd_set_particles
     double fgrid_dt = 0.0;
     void* gforce = nullptr;
     uint32_t* flags = nullptr;
@@ -747,9 +761,11 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
     DevParams<T> P = make_params<T>(h, dt, (T)dt);
     long t;
     if (rebuild) {  // P2G of the current state
-        t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
-        RD_TRY(clear_grid<T>(h, h->g));
-        tmark_end(h, t);
+        if (!h->clean_grids) {
+            t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
+            RD_TRY(clear_grid<T>(h, h->g));
+            tmark_end(h, t);
+        }
         DevBufs D = bufs<T>(h);
         // particles not yet in sorted order (an upload): k_p2g, which reads
         // them all through the permutation, also writes them to the other
@@ -761,6 +777,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
             D.reorder_out = h->pl[h->cur ^ 1];
             D.perm_reset = h->perm;
         }
+        if (h->stress_valid) D.stress = h->stress;
         t = tmark_begin(h, RD_KERNEL_P2G);
         const unsigned pg = persistent_grid<T>(h, h->occ_p2g);
         if (batch)
@@ -773,12 +790,21 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
     }
     if (fork) {
         RD_TRY(check_cuda(h, cudaStreamWaitEvent(h->stream, h->ev_join, 0), "join"));
-    } else {
+    } else if (!h->clean_grids) {
         t = tmark_begin(h, RD_KERNEL_GRID_CLEAR);
         RD_TRY(clear_grid<T>(h, h->g ^ 1));
         tmark_end(h, t);
     }
+    h->clean_grids = false;
+    h->stress_valid = false;
+    h->slot_of_valid = false;
     DevBufs D = bufs<T>(h);
+    // the first step after an upload keeps slot_of current, so that a download
+    // right after it (a caller moving the state in and out every step) needs
+    // no k_slot_of_id; steady steps do not pay for the scattered stores
+    const bool keep_slots = !batch && h->after_upload;
+    if (keep_slots) D.slot_of = h->slot_of;
+    h->after_upload = false;
     t = tmark_begin(h, RD_KERNEL_G2P2G);
     const unsigned fg = persistent_grid<T>(h, h->occ_g2p);
     if (batch)
@@ -787,6 +813,7 @@ template <typename T> rd_status step_fused(rd_handle* h, double dt) {
         single_fused_kernel<T>(h)<<<fg, kFusedThreads, fused_smem_bytes<T>(), h->stream>>>(P, D, h->smaps[h->g]);
     tmark_end(h, t);
     RD_TRY(launched(h, "k_g2p2g"));
+    h->slot_of_valid = keep_slots;
     h->cur ^= 1;
     h->g ^= 1;
     h->keys_valid = true;  // k_g2p2g wrote keys[cur] and counted them
@@ -804,6 +831,9 @@ template <typename T> rd_status stage_impl(rd_handle* h, int stage, double dt) {
     const unsigned cb = blocks_for(nc, 256);
     DevParams<T> P = make_params<T>(h, dt, T(1));
     h->fgrid_valid = false;
+    h->clean_grids = false;
+    h->stress_valid = false;
+    h->slot_of_valid = false;
     switch (stage) {
         case RD_STAGE_RASTERIZE: {
             if (!h->sorted) RD_TRY(sort_particles<T>(h));
@@ -951,15 +981,37 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, cons
         h->keys_valid = true;
         h->sorted = false;
         RD_TRY(sort_particles<T>(h, false));
+        // both grid buffers cleared on the second stream while the link is busy
+        const bool side = h->side && !h->timing;
+        if (side) {
+            RD_TRY(check_cuda(h, cudaEventRecord(h->ev_fork, h->stream), "fork"));
+            RD_TRY(check_cuda(h, cudaStreamWaitEvent(h->side, h->ev_fork, 0), "fork"));
+        }
+        RD_TRY(clear_grid<T>(h, 0, side ? h->side : h->stream));
+        RD_TRY(clear_grid<T>(h, 1, side ? h->side : h->stream));
+        if (side) RD_TRY(check_cuda(h, cudaEventRecord(h->ev_join, h->side), "join"));
+        if (!h->stress) {  // on the first such upload: the first P2G's stress, 3 vec4 a particle
+            const cudaError_t e = cudaMalloc(&h->stress, 3 * n * sizeof(vec4<T>));
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                h->stress = nullptr;  // the P2G computes it then
+            }
+        }
         k_pack_place<T><<<nb, kIoThreads, 0, h->stream>>>(
             (int)n, d[0], ptr[1], ptr[2], ptr[3], ptr[4], ptr[5], ptr[6], ptr[7], static_cast<vec4<T>*>(h->pl[h->cur]),
-            h->prm.track_fp, h->keys[h->cur], h->cursor, h->perm, h->flags);
+            h->prm.track_fp, h->keys[h->cur], h->cursor, h->perm, h->flags, P, static_cast<vec4<T>*>(h->stress),
+            h->slot_of);
         RD_TRY(launched(h, "k_pack_place"));
+        if (side) RD_TRY(check_cuda(h, cudaStreamWaitEvent(h->stream, h->ev_join, 0), "join"));
         sc.set = true;
         h->keys_valid = false;
         h->sorted = true;
         h->in_order = true;
         h->fgrid_valid = false;
+        h->clean_grids = true;
+        h->stress_valid = h->stress != nullptr;
+        h->slot_of_valid = true;
+        h->after_upload = true;
         h->grid_mode = GRID_NONE;
         return RD_OK;
     }
@@ -971,9 +1023,13 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, cons
         RD_TRY(launched(h, "k_pack"));
     }
     sc.set = true;
+    h->after_upload = true;
     h->keys_valid = keys;
     h->sorted = false;
     h->fgrid_valid = false;
+    h->clean_grids = false;
+    h->stress_valid = false;
+    h->slot_of_valid = false;
     h->grid_mode = GRID_NONE;
     return RD_OK;
 }
@@ -994,11 +1050,15 @@ template <typename T> rd_status get_particles_impl(rd_handle* h, int scene, rd_p
         if (dst[k] && where == RD_HOST) (staged[k] ? h->io_staged : h->io_direct) += cnt[k] * sizeof(T);
     }
     const vec4<T>* pl = static_cast<const vec4<T>*>(h->pl[h->cur]);
-    k_slot_of_id<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, (int)sc.poff, h->n, pl, h->slot_of);
+    if (batched(h) || !h->slot_of_valid) {
+        k_slot_of_id<T><<<blocks_for(n, 256), 256, 0, h->stream>>>((int)n, (int)sc.poff, h->n, pl, h->slot_of);
+        RD_TRY(launched(h, "k_slot_of_id"));
+        h->slot_of_valid = !batched(h);
+    }
     k_unpack<T><<<blocks_for(n, kIoThreads), kIoThreads, 0, h->stream>>>((int)n, (int)sc.poff, h->n, pl, h->slot_of,
                                                                          tgt[0], tgt[1], tgt[2], tgt[3], tgt[4],
                                                                          tgt[5], tgt[6], tgt[7], h->prm.track_fp);
-    RD_TRY(launched(h, "k_unpack", 2));
+    RD_TRY(launched(h, "k_unpack"));
     if (where == RD_HOST) {
         for (int k = 0; k < 8; ++k)
             if (staged[k])
@@ -1090,6 +1150,9 @@ template <typename T> rd_status init_volumes_impl(rd_handle* h) {
     RD_TRY(ensure_table<T>(h, h->table_valid ? h->table_dt : 0.0, T(h->table_valid ? h->table_fs : 0.0)));
     if (!h->sorted) RD_TRY(sort_particles<T>(h));
     h->fgrid_valid = false;
+    h->clean_grids = false;
+    h->stress_valid = false;
+    h->slot_of_valid = false;
     RD_TRY(clear_grid<T>(h, h->g));
     const DevParams<T> P = make_params<T>(h, 0.0, T(1));
     const DevBufs D = bufs<T>(h);
@@ -1176,7 +1239,7 @@ void release(rd_handle* h) {
     void* ptrs[] = {h->pl[0], h->pl[1], h->keys[0], h->keys[1], h->perm, h->slot_of, h->counts, h->bcount, h->gmark[0],
                     h->gmark[1], h->cursor, h->work,
                     h->nwork2, h->tile_sums, h->tile_list, h->grid[0], h->grid[1], h->gforce, h->flags, h->xyzs, h->io, h->grid_io,
-                    h->d_col, h->rgba, h->zid, h->img,
+                    h->d_col, h->rgba, h->zid, h->img, h->stress,
                     h->d_scenes, h->d_sblock, h->d_spoff};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -1580,6 +1643,9 @@ template <typename T> rd_status autotune_impl(rd_handle* h, double dt, int steps
         h->keys_valid = false;
         h->sorted = false;
         h->fgrid_valid = false;
+        h->clean_grids = false;
+        h->stress_valid = false;
+        h->slot_of_valid = false;
         h->grid_mode = GRID_NONE;
         return check_cuda(h, cudaMemcpyAsync(h->pl[h->cur], saved, bytes, cudaMemcpyDeviceToDevice, h->stream),
                           "restore state");
@@ -2054,6 +2120,9 @@ rd_status begin_segment(rd_handle* h, const void* src, int b) {
     h->keys_valid = false;
     h->sorted = false;
     h->fgrid_valid = false;
+    h->clean_grids = false;
+    h->stress_valid = false;
+    h->slot_of_valid = false;
     h->grid_mode = GRID_NONE;
     return RD_OK;
 }
@@ -2080,6 +2149,9 @@ template <typename T> rd_status record_body(rd_handle* h, double dt, int steps, 
             h->keys_valid = false;
             h->sorted = false;
             h->fgrid_valid = false;
+            h->clean_grids = false;
+            h->stress_valid = false;
+            h->slot_of_valid = false;
             h->grid_mode = GRID_NONE;
             a.tail_valid = true;
         } else {
@@ -2172,6 +2244,9 @@ rd_status load_state(rd_handle* h, const void* src, size_t bytes) {
     h->keys_valid = false;
     h->sorted = false;
     h->fgrid_valid = false;
+    h->clean_grids = false;
+    h->stress_valid = false;
+    h->slot_of_valid = false;
     h->grid_mode = GRID_NONE;
     return RD_OK;
 }
@@ -2305,6 +2380,9 @@ template <typename T> rd_status sweep_graph(rd_handle* h) {
         h->keys_valid = false;
         h->sorted = false;
         h->fgrid_valid = false;
+        h->clean_grids = false;
+        h->stress_valid = false;
+        h->slot_of_valid = false;
         h->grid_mode = GRID_NONE;
         h->last_dt = a.dt;
     }
@@ -2487,6 +2565,9 @@ template <typename T> rd_status initialize_impl(rd_handle* h, const rd_init_spec
         h->keys_valid = false;
         h->sorted = false;
         h->fgrid_valid = false;
+        h->clean_grids = false;
+        h->stress_valid = false;
+        h->slot_of_valid = false;
         h->grid_mode = GRID_NONE;
     }
     return cleanup(st);
