@@ -42,11 +42,25 @@ enum GridMode { GRID_NONE = 0, GRID_FUSED = 1, GRID_MV = 2, GRID_V = 3 };
 // Called by every thread of a 256-thread block; rows r0 .. r0 + cnt - 1 are
 // the block's, thread t's row is r0 + t.
 constexpr int kIoThreads = 256;
+// `count` reals from src to dst by the whole block, as 16-byte vectors when
+// both addresses allow it (fewer, larger requests over the host link).
+template <typename T>
+__device__ __forceinline__ void block_copy(T* __restrict__ dst, const T* __restrict__ src, int count) {
+    constexpr int V = 16 / (int)sizeof(T);
+    int e0 = 0;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
+        const int nv = count / V;
+        const float4* __restrict__ s4 = reinterpret_cast<const float4*>(src);
+        float4* __restrict__ d4 = reinterpret_cast<float4*>(dst);
+        for (int e = threadIdx.x; e < nv; e += blockDim.x) d4[e] = s4[e];
+        e0 = nv * V;
+    }
+    for (int e = e0 + threadIdx.x; e < count; e += blockDim.x) dst[e] = src[e];
+}
 template <typename T, int K>
 __device__ __forceinline__ void load_rows(const T* __restrict__ src, int r0, int cnt, T (&val)[K], T* sh) {
     __syncthreads();  // the previous use of sh is done
-    const T* s = src + (size_t)r0 * K;
-    for (int e = threadIdx.x; e < cnt * K; e += blockDim.x) sh[e] = s[e];
+    block_copy(sh, src + (size_t)r0 * K, cnt * K);
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < K; ++k) val[k] = sh[threadIdx.x * K + k];  // rows past cnt: not used
@@ -57,8 +71,7 @@ __device__ __forceinline__ void store_rows(T* __restrict__ dst, int r0, int cnt,
 #pragma unroll
     for (int k = 0; k < K; ++k) sh[threadIdx.x * K + k] = val[k];
     __syncthreads();
-    T* d = dst + (size_t)r0 * K;
-    for (int e = threadIdx.x; e < cnt * K; e += blockDim.x) d[e] = sh[e];
+    block_copy(dst + (size_t)r0 * K, sh, cnt * K);
 }
 
 // The particle of row r0 + threadIdx.x of the caller's structure-of-arrays
@@ -117,7 +130,7 @@ __global__ void __launch_bounds__(kIoThreads)
            const T* __restrict__ vol, vec4<T>* __restrict__ pl, int track_fp, DevParams<T> P,
            uint32_t* __restrict__ keys, uint32_t* __restrict__ counts, uint32_t* __restrict__ bcount,
            uint32_t* __restrict__ flags) {
-    __shared__ T sh[9 * kIoThreads];
+    __shared__ __align__(16) T sh[9 * kIoThreads];
     const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
     Particle<T> p;
     T FPm[9];
@@ -142,7 +155,7 @@ template <typename T>
 __global__ void __launch_bounds__(kIoThreads)
     k_pack_keys(int n, const T* __restrict__ x, T* __restrict__ xcopy, DevParams<T> P, uint32_t* __restrict__ keys,
                 uint32_t* __restrict__ counts, uint32_t* __restrict__ bcount, uint32_t* __restrict__ flags) {
-    __shared__ T sh[3 * kIoThreads];
+    __shared__ __align__(16) T sh[3 * kIoThreads];
     const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
     const int cnt = min((int)blockDim.x, n - r0);
     T t3[3];
@@ -171,7 +184,7 @@ __global__ void __launch_bounds__(kIoThreads)
                  const uint32_t* __restrict__ keys, uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm,
                  uint32_t* __restrict__ flags, DevParams<T> P, vec4<T>* __restrict__ stress,
                  uint32_t* __restrict__ slot_of) {
-    __shared__ T sh[9 * kIoThreads];
+    __shared__ __align__(16) T sh[9 * kIoThreads];
     const int r0 = blockIdx.x * blockDim.x, i = r0 + threadIdx.x;
     Particle<T> p;
     T FPm[9];
@@ -218,7 +231,7 @@ __global__ void __launch_bounds__(kIoThreads)
     k_unpack(int n, int off, int ntot, const vec4<T>* __restrict__ pl, const uint32_t* __restrict__ slot,
              T* __restrict__ x, T* __restrict__ v, T* __restrict__ B, T* __restrict__ FE, T* __restrict__ FP,
              T* __restrict__ Jp, T* __restrict__ mass, T* __restrict__ vol, int track_fp) {
-    __shared__ T sh[9 * kIoThreads];
+    __shared__ __align__(16) T sh[9 * kIoThreads];
     const int r0 = blockIdx.x * blockDim.x, o = r0 + threadIdx.x;
     const int cnt = min((int)blockDim.x, n - r0);
     Particle<T> p;
@@ -948,9 +961,11 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, cons
     const void* src[8] = {in->x, in->v, in->B, in->FE, in->FP, in->Jp, in->mass, in->volume};
     const size_t cnt[8] = {3 * n, 3 * n, 9 * n, 9 * n, 9 * n, n, n, n};
     const T* ptr[8];
+    bool from_host = n > 0;  // every array page-locked host memory read in place (the link is the bound)
     for (int k = 0; k < 8; ++k) {
         if (!src[k] || n == 0) { ptr[k] = nullptr; continue; }
-        if (where == RD_HOST && !host_in_place(src[k], cnt[k] * sizeof(T))) {
+        const bool in_place = host_in_place(src[k], cnt[k] * sizeof(T));
+        if (where == RD_HOST && !in_place) {
             RD_TRY(check_cuda(h, cudaMemcpyAsync(d[k], src[k], cnt[k] * sizeof(T), cudaMemcpyHostToDevice, h->stream),
                               "upload"));
             ptr[k] = d[k];
@@ -959,6 +974,7 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, cons
             ptr[k] = static_cast<const T*>(src[k]);
             if (where == RD_HOST) h->io_direct += cnt[k] * sizeof(T);
         }
+        from_host = from_host && in_place;
     }
     // a single scene's first sort reads its keys and histogram from the pack
     const bool keys = !batched(h) && n > 0;
@@ -966,13 +982,15 @@ template <typename T> rd_status set_particles_impl(rd_handle* h, int scene, cons
         RD_TRY(check_cuda(h, cudaMemsetAsync(h->counts, 0, sizeof(uint32_t) * h->nkeys, h->stream), "memset counts"));
         RD_TRY(check_cuda(h, cudaMemsetAsync(h->bcount, 0, sizeof(uint32_t) * h->nblocks, h->stream), "memset counts"));
     }
-    // A single scene after its first step: the upload sorts the particles on
-    // the way in - keys from the positions, the scan, then every particle to
-    // its sorted slot - so the next step's P2G reads them in order.  It
-    // replaces the step's scatter, its permuted-read P2G and its reordering
-    // copy; the first upload keeps the one-pass route (k_pack), which costs
-    // less when the particles' order is not yet that of a sort.
-    if (keys && h->last_dt > 0.0 && !h->split_out) {
+    // A single scene after its first step, read in place from page-locked
+    // host memory: the upload sorts the particles on the way in - keys from
+    // the positions, the scan, then every particle to its sorted slot - so the
+    // next step's P2G reads them in order.  It replaces the step's scatter,
+    // its permuted-read P2G and its reordering copy, and its scattered stores
+    // and the first P2G's stress run while the link is the bound.  From device
+    // memory (or the staging buffer) nothing hides them, and the one-pass
+    // route (k_pack, coalesced) costs less, as it does on a first upload.
+    if (keys && from_host && h->last_dt > 0.0 && !h->split_out) {
         const DevParams<T> P = make_params<T>(h, 0.0, T(0));
         const unsigned nb = blocks_for(n, kIoThreads);
         k_pack_keys<T><<<nb, kIoThreads, 0, h->stream>>>((int)n, ptr[0], ptr[0] == d[0] ? nullptr : d[0], P,

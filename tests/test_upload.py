@@ -1,5 +1,5 @@
-"""rd_set_particles on a single-scene handle that has stepped: the upload
-sorts on the way in (k_pack_keys, the scan, k_pack_place puts every particle
+"""rd_set_particles from page-locked host memory on a single-scene handle
+that has stepped: the upload sorts on the way in (k_pack_keys, the scan, k_pack_place puts every particle
 straight into its sorted slot), so the first step's P2G reads the particles
 in order and nothing is reordered.  Checked against the same state uploaded to
 a fresh handle (one-pass k_pack; the first step sorts with k_scatter and
@@ -32,11 +32,12 @@ def stepped_state(pkg, sc, precision=0, steps=2):
     return sim, st
 
 
-def upload(sim, st, pinned=False):
+def upload(sim, st, pinned=False, mapped=False):
     if pinned:
         import torch
         st = {k: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy() for k, a in st.items()}
-    sim.set_particles(st["x"], st["v"], st["mass"], B=st["B"], FE=st["FE"], Jp=st["Jp"], volume=st["volume"])
+    sim.set_particles(st["x"], st["v"], st["mass"], B=st["B"], FE=st["FE"], Jp=st["Jp"], volume=st["volume"],
+                      mapped=mapped)
     return st
 
 
@@ -46,21 +47,27 @@ def same_state(a, b, h, tol):
     assert rel_floor(a["B"], b["B"], b_scale(b["v"], h)) < tol
 
 
-@pytest.mark.parametrize("route", ["pageable", "pinned"])
+@pytest.mark.parametrize("route", ["pageable", "pinned", "mapped"])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_upload_after_a_step_matches_a_fresh_handle(built_pkg, route, precision):
+    """Page-locked arrays (read in place, RD_HOST or as device pointers) take
+    the sorted upload; pageable ones go through the staging buffer and the
+    one-pass route."""
     from rd_gb300 import scenes
     sc = scenes.snowball(seed=5, n=6000, grid=32)
     a, st = stepped_state(built_pkg, sc, precision)
-    kept = upload(a, st, route == "pinned")
+    kept = upload(a, st, route != "pageable", mapped=route == "mapped")
     with pytest.raises(built_pkg.RDError):
         a.get_grid()  # nothing to export before a step, as after any upload
     b = make(built_pkg, sc, precision)
     upload(b, st)
     l0 = a.launch_count()
     a.step(sc.dt, 1)
-    # sorted, and both grids cleared, during the upload: the step is k_p2g and the fused kernel
-    assert a.launch_count() - l0 == 2
+    if route == "pageable":
+        assert a.launch_count() - l0 > 2
+    else:
+        # sorted, and both grids cleared, during the upload: the step is k_p2g and the fused kernel
+        assert a.launch_count() - l0 == 2
     a.step(sc.dt, 2)
     b.step(sc.dt, 3)
     same_state(a.get_particles(FIELDS), b.get_particles(FIELDS), sc.h, 1e-10 if precision else 1e-5)
@@ -76,20 +83,21 @@ def test_upload_then_another_dt(built_pkg):
     from rd_gb300 import scenes
     sc = scenes.snowball(seed=6, n=5000, grid=32)
     a, st = stepped_state(built_pkg, sc)
-    upload(a, st)
+    kept = upload(a, st, pinned=True)
     b = make(built_pkg, sc)
     upload(b, st)
     for dt, k in ((0.5 * sc.dt, 2), (sc.dt, 2)):
         a.step(dt, k)
         b.step(dt, k)
     same_state(a.get_particles(FIELDS), b.get_particles(FIELDS), sc.h, 2e-5)
+    del kept
 
 
 def test_upload_after_a_step_matches_oracle(built_pkg, orc):
     from rd_gb300 import scenes
     sc = scenes.snowball(seed=7, n=6000, grid=32)
     a, st = stepped_state(built_pkg, sc)
-    upload(a, st)
+    upload(a, st, pinned=True)
     a.step(sc.dt, 1)
     kw = dict(sc.params())
     kw.pop("track_fp", None)
@@ -115,10 +123,11 @@ def test_upload_with_a_particle_outside_the_domain(built_pkg):
     sc = scenes.snowball(seed=8, n=3000, grid=32)
     a, st = stepped_state(built_pkg, sc)
     st["x"][17] = (0.3 * sc.h, 0.5, 0.5)
-    upload(a, st)
+    kept = upload(a, st, pinned=True)
     b = make(built_pkg, sc)
     upload(b, st)
     a.step(sc.dt, 2)
     b.step(sc.dt, 2)
     assert a.flags() == b.flags() and a.flags() & built_pkg.FLAG_OUT_OF_DOMAIN
     same_state(a.get_particles(FIELDS), b.get_particles(FIELDS), sc.h, 1e-5)
+    del kept
