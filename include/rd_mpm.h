@@ -203,6 +203,14 @@ rd_status rd_debug_sort(rd_handle* h, uint32_t* keys, uint32_t* order, int where
  * RD_FLAG_WAIT_TIMEOUT and returns; *gave_up = 1 when the wait ran out.  No
  * copy is issued, so nothing is left in flight. */
 rd_status rd_debug_wait_timeout(rd_handle* h, int32_t tries, int32_t* gave_up);
+/* The bounds-checked build of the library (compiled with RD_BOUNDS_CHECK,
+ * librd_mpm_checked.so; no counterpart in the reference) tests the indexes of
+ * the fused kernel's and the P2G's shared tiles, records, particles and grid
+ * nodes before each access, skips an access out of range and counts it: the
+ * count of this process so far into *count, after the handles' work has
+ * finished (rd_synchronize), and *checked = 1.  The normal build reports
+ * *count = 0 and *checked = 0. */
+rd_status rd_debug_bounds_violations(uint64_t* count, int32_t* checked);
 /* Kernel ids for the per-kernel event timing below. */
 enum {
     RD_KERNEL_KEYS = 0,     /* block keys + histogram (when not fused into G2P) */

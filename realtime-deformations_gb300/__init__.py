@@ -25,7 +25,10 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 REPO_DIR = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
-LIB_PATH = os.path.join(PKG_DIR, "librd_mpm.so")
+# RD_BOUNDS_CHECK=1 in the environment selects the bounds-checked build
+# (librd_mpm_checked.so, compiled with -DRD_BOUNDS_CHECK) for this process.
+CHECKED = os.environ.get("RD_BOUNDS_CHECK") == "1"
+LIB_PATH = os.path.join(PKG_DIR, "librd_mpm_checked.so" if CHECKED else "librd_mpm.so")
 HEADER = os.path.join(REPO_DIR, "include", "rd_mpm.h")
 
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
@@ -45,6 +48,7 @@ STAGES = {"rasterize": 0, "forces": 1, "grid_velocities": 2, "collisions": 3,
 EXPORTS = ("rd_default_params", "rd_create", "rd_destroy", "rd_set_particles", "rd_get_particles",
            "rd_init_volumes", "rd_step", "rd_stage", "rd_get_grid", "rd_device_xyzs", "rd_get_flags",
            "rd_clear_flags", "rd_synchronize", "rd_get_stream", "rd_last_error", "rd_debug_sort", "rd_debug_wait_timeout",
+           "rd_debug_bounds_violations",
            "rd_set_kernel_timing", "rd_kernel_timing", "rd_launch_count", "rd_graph_replays", "rd_io_bytes", "rd_host_alloc", "rd_host_free", "rd_batch_create",
            "rd_batch_num_scenes", "rd_batch_set_particles", "rd_batch_get_particles", "rd_batch_get_grid",
            "rd_batch_step", "rd_set_graphs", "rd_autotune", "rd_tune_trials", "rd_tune_key", "rd_tune_cache_get",
@@ -60,13 +64,25 @@ def _sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC)) if f.endswith((".cu", ".cuh", ".h"))] + [HEADER]
 
 
+def bounds_violations():
+    """(count, checked): accesses out of range skipped so far in this process
+    by the bounds-checked build (rd_debug_bounds_violations); checked is False
+    for the normal build, whose count is 0."""
+    c, k = ctypes.c_uint64(), ctypes.c_int32()
+    st = lib().rd_debug_bounds_violations(ctypes.byref(c), ctypes.byref(k))
+    if st != RD_OK:
+        raise RuntimeError(f"rd_debug_bounds_violations: {STATUS_NAMES.get(st, st)}")
+    return c.value, bool(k.value)
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile ``csrc/rd_mpm.cu`` for sm_103a into ``librd_mpm.so`` (in-tree)."""
+    """Compile ``csrc/rd_mpm.cu`` for sm_103a into ``librd_mpm.so`` (in-tree;
+    ``librd_mpm_checked.so`` with RD_BOUNDS_CHECK=1 in the environment)."""
     newest = max(os.path.getmtime(f) for f in _sources())
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
         return LIB_PATH
     tmp = LIB_PATH + f".tmp{os.getpid()}"
-    cmd = ["nvcc", *NVCC_FLAGS, os.path.join(CSRC, "rd_mpm.cu"), "-o", tmp]
+    cmd = ["nvcc", *NVCC_FLAGS, *(["-DRD_BOUNDS_CHECK"] if CHECKED else []), os.path.join(CSRC, "rd_mpm.cu"), "-o", tmp]
     if verbose:
         print(" ".join(cmd))
     subprocess.check_call(cmd, cwd=CSRC)
@@ -255,6 +271,7 @@ def lib():
             L.rd_last_error.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
             L.rd_debug_sort.argtypes = [vp, vp, vp, ctypes.c_int]
             L.rd_debug_wait_timeout.argtypes = [vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+            L.rd_debug_bounds_violations.argtypes = [ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int32)]
             L.rd_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
             L.rd_graph_replays.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
             L.rd_io_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]

@@ -39,6 +39,25 @@ __device__ __forceinline__ void st_stream_half(dvec4* p, int k, double a, double
     __stcs(reinterpret_cast<double2*>(p) + k, make_double2(a, b));
 }
 
+// ---------------------------------------------------------------- bounds
+// Bounds-checked build (nvcc -DRD_BOUNDS_CHECK: librd_mpm_checked.so): before
+// each access at the checked sites - the fused kernel's and the P2G's shared
+// tiles and records, the particle and grid indexes they compute - the index is
+// tested against its buffer; one outside it is counted in rd_bounds_count
+// (rd_debug_bounds_violations reads it) and the access skipped.  In the
+// normal build RD_IN_BOUNDS is `true` and the tests compile away.
+#ifdef RD_BOUNDS_CHECK
+__device__ unsigned long long rd_bounds_count;
+__device__ __forceinline__ bool in_bounds(long long i, long long n) {
+    if (i >= 0 && i < n) return true;
+    atomicAdd(&rd_bounds_count, 1ull);
+    return false;
+}
+#define RD_IN_BOUNDS(i, n) ::rd::in_bounds((long long)(i), (long long)(n))
+#else
+#define RD_IN_BOUNDS(i, n) true
+#endif
+
 // ---------------------------------------------------------------- state
 // Particle state: 7 planes of vec4 (structure of arrays of 16/32-byte
 // vectors, so every plane access of a warp is one fully coalesced request):

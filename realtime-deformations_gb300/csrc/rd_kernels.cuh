@@ -879,6 +879,7 @@ __device__ __forceinline__ void p2g_flush_lane(P2GTile<T, CA>& S, int c, int ox,
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         const int node = ((cx + ox) * TS + (cy + oy)) * TS + (cz + oz0 + 2 * k);
+        if (!RD_IN_BOUNDS(node, TC) || !RD_IN_BOUNDS(c, (P2GTile<T, CA>::NC))) continue;
         if (mom) atomicAdd(&S.tile[node], am[k]);
         atomicAdd(&S.tile[TC + node], aq[k][0]);
         atomicAdd(&S.tile[2 * TC + node], aq[k][1]);
@@ -920,10 +921,12 @@ __device__ __forceinline__ void sort_ranked(P2GTile<T, CA>& S, int j, int cell, 
         }
     }
     __syncthreads();
-    if (cell != 0xff) {
+    if (cell != 0xff && RD_IN_BOUNDS(cell, NC)) {
         const int k = S.off[cell] + rank;
-        S.order[k] = (uint16_t)j;
-        S.scell[k] = (uint8_t)cell;
+        if (RD_IN_BOUNDS(k, WorkP<T>::value)) {
+            S.order[k] = (uint16_t)j;
+            S.scell[k] = (uint8_t)cell;
+        }
     }
     __syncthreads();
 }
@@ -1028,11 +1031,13 @@ __device__ __forceinline__ void p2g_runs(P2GTile<T, CA>& S, int total) {
         const float2 fzz = make_float2(fz, fz + 2.f);
         while (k < k1) {
             const int c = S.scell[k];
+            if (!RD_IN_BOUNDS(c, (P2GTile<T, CA>::NC))) break;
             const int e = min(S.off[c] + S.cnt[c], k1);
             float2 am2 = make_float2(0.f, 0.f), qx2 = am2, qy2 = am2, qz2 = am2;
 #pragma unroll 1
             for (; k < e; ++k) {
                 const int j = S.order[k];
+                if (!RD_IN_BOUNDS(j, WorkP<T>::value)) continue;
                 const T* rs = recs + j * (4 * kRecV4);
                 const float wxy = rs[ox] * rs[4 + oy];
                 const float2 w = __fmul2_rn(make_float2(wxy, wxy), *reinterpret_cast<const float2*>(rs + 8 + 2 * oz0));
@@ -1056,10 +1061,12 @@ __device__ __forceinline__ void p2g_runs(P2GTile<T, CA>& S, int total) {
     } else {
         while (k < k1) {
             const int c = S.scell[k];
+            if (!RD_IN_BOUNDS(c, (P2GTile<T, CA>::NC))) break;
             const int e = min(S.off[c] + S.cnt[c], k1);
             T am[2] = {T(0), T(0)}, aq[2][3] = {{T(0), T(0), T(0)}, {T(0), T(0), T(0)}};
             for (; k < e; ++k) {
                 const int j = S.order[k];
+                if (!RD_IN_BOUNDS(j, WorkP<T>::value)) continue;
                 const T* rs = recs + j * (4 * kRecV4);
                 const T wxy = rs[ox] * rs[4 + oy];
                 const T w0 = wxy * rs[8 + 2 * oz0], w1 = wxy * rs[9 + 2 * oz0];
@@ -1102,11 +1109,13 @@ __device__ __forceinline__ void p2g_runs_pairs(P2GTile<float, CA>& S, int total)
     int k = k0;
     while (k < k1) {
         const int c = S.scell[k];
+        if (!RD_IN_BOUNDS(c, (P2GTile<float, CA>::NC))) break;
         const int e = min(S.off[c] + S.cnt[c], k1);
         float2 m0 = make_float2(0.f, 0.f), x0 = m0, y0 = m0, z0 = m0, m1 = m0, x1 = m0, y1 = m0, z1 = m0;
         for (int kb = k; kb < e; kb += 2) {
             const bool mine = kb + hw < e;
             const int kk = S.order[mine ? kb + hw : kb];
+            if (!RD_IN_BOUNDS(kk, WorkP<float>::value)) continue;
             const float* rs = recs + kk * (4 * kRecV4);
             const float wxy = mine ? rs[ox] * rs[4 + oy] : 0.f;
             const float2 w0 = __fmul2_rn(make_float2(wxy, wxy), *reinterpret_cast<const float2*>(rs + wz0));
@@ -1151,8 +1160,9 @@ __device__ __forceinline__ void p2g_flush(const DevParams<T>& P, const P2GTile<T
         const int gx = org[0] + ix, gy = org[1] + iy, gz = org[2] + iz;
         if (gx < 0 || gy < 0 || gz < 0 || gx >= P.M[0] || gy >= P.M[1] || gz >= P.M[2]) continue;
         const vec4<T> v = mk4<T>(S.tile[c], S.tile[TC + c], S.tile[2 * TC + c], S.tile[3 * TC + c]);
-        if (v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0))
-            red_add4(grid + ((size_t)gx * P.M[1] + gy) * P.M[2] + gz, v);
+        const size_t lin = ((size_t)gx * P.M[1] + gy) * P.M[2] + gz;
+        if (!RD_IN_BOUNDS(lin, (size_t)P.M[0] * P.M[1] * P.M[2])) continue;
+        if (v.x != T(0) || v.y != T(0) || v.z != T(0) || v.w != T(0)) red_add4(grid + lin, v);
     }
 }
 
@@ -1193,6 +1203,12 @@ __device__ __forceinline__ void p2g_item(const DevParams<T>& P, const DevBufs& D
     bool stray = false;  // a record outside the cell space, or one whose cell is not its key's
     // phase 1: a record per particle
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
+        if (!RD_IN_BOUNDS(it.y + j, n) || !RD_IN_BOUNDS(D.perm[it.y + j], n)) {
+            S.cellof[j] = 0xff;
+            S.scell[j] = 0;
+            stray = true;
+            continue;
+        }
         Particle<T> p;
         load_particle(pl, n, D.perm[it.y + j], p);
         if (D.reorder_out) {  // the particle to its sorted position
@@ -1415,7 +1431,7 @@ __device__ __forceinline__ void g2p_gather(const vec4<T>* __restrict__ gv, const
                 float2 c0 = make_float2(0.f, 0.f), c1 = c0, c2 = c0;
 #pragma unroll
                 for (int oz = 0; oz < 4; ++oz) {
-                    const vec4<T> v = gv[rowc + oz];
+                    const vec4<T> v = RD_IN_BOUNDS(rowc + oz, kTileCells) ? gv[rowc + oz] : mk4<T>(T(0), T(0), T(0), T(0));
                     const float2 wz2 = make_float2(St.w[2][oz], wzd[oz]);
                     c0 = __ffma2_rn(wz2, make_float2(v.x, v.x), c0);
                     c1 = __ffma2_rn(wz2, make_float2(v.y, v.y), c1);
@@ -1425,7 +1441,7 @@ __device__ __forceinline__ void g2p_gather(const vec4<T>* __restrict__ gv, const
             } else {
 #pragma unroll
                 for (int oz = 0; oz < 4; ++oz) {
-                    const vec4<T> v = gv[rowc + oz];
+                    const vec4<T> v = RD_IN_BOUNDS(rowc + oz, kTileCells) ? gv[rowc + oz] : mk4<T>(T(0), T(0), T(0), T(0));
                     col[0] += St.w[2][oz] * v.x; col[1] += St.w[2][oz] * v.y; col[2] += St.w[2][oz] * v.z;
                     colz[0] += wzd[oz] * v.x; colz[1] += wzd[oz] * v.y; colz[2] += wzd[oz] * v.z;
                 }
@@ -1495,9 +1511,10 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         // one particle per thread (WorkP == blockDim): start its loads before
         // the tile is staged so the two latencies overlap
         const int j = threadIdx.x;
+        const bool mine = j < count && RD_IN_BOUNDS(it.y + j, n) && RD_IN_BOUNDS(D.perm[it.y + j], n);
         Particle<T> p;
         T FP[9];
-        if (j < count) {
+        if (mine) {
             const uint32_t src = D.perm[it.y + j];
             load_particle(pin, n, src, p);
             if (TRACK_FP) load_fp(pin, n, src, FP);
@@ -1540,7 +1557,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             }
         }
         int rcell = 0xff, rrank = 0;  // this thread's record: cell and rank within it
-        if (j < count) {
+        if (mine) {
             const int s = it.y + j;
             // the plastic split first: the stress of the next P2G (6 entries)
             // and the F_E / J_P / F_P planes are final after it, so none of the
@@ -1588,7 +1605,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             for (int a = 0; a < 3; ++a) mv[a] = p.m * p.v[a];
             vec4<T>* rec = &S.p.rec[j * kRecV4];
             write_record<T, true>(rec, S2, p.x, A, mv, p.m, P.h);
-            if (in_space) {
+            if (in_space && RD_IN_BOUNDS((S2.rel[0] * CA + S2.rel[1]) * CA + S2.rel[2], (P2GTile<T, CA>::NC))) {
                 rcell = (S2.rel[0] * CA + S2.rel[1]) * CA + S2.rel[2];
                 S.p.cellof[j] = (uint8_t)rcell;
                 rrank = atomicAdd(&S.p.cnt[rcell], 1);

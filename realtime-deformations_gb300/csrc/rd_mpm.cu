@@ -2972,6 +2972,20 @@ rd_status rd_last_error(rd_handle* h, char* buf, size_t len) {
     return RD_OK;
 }
 
+rd_status rd_debug_bounds_violations(uint64_t* count, int32_t* checked) {
+    if (!count || !checked) return RD_INVALID_ARG;
+#ifdef RD_BOUNDS_CHECK
+    unsigned long long v = 0;
+    if (cudaMemcpyFromSymbol(&v, rd::rd_bounds_count, sizeof v) != cudaSuccess) return RD_CUDA_ERROR;
+    *count = (uint64_t)v;
+    *checked = 1;
+#else
+    *count = 0;
+    *checked = 0;
+#endif
+    return RD_OK;
+}
+
 rd_status rd_debug_wait_timeout(rd_handle* h, int32_t tries, int32_t* gave_up) {
     if (!h || !gave_up || tries < 1 || tries > kTileWaitTries) return RD_INVALID_ARG;
     cudaSetDevice(h->prm.device);
