@@ -944,7 +944,9 @@ __device__ __forceinline__ void p2g_tasks(P2GTile<T, CA>& S, int total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int ox = lane >> 3, oy = (lane >> 1) & 3, oz0 = lane & 1;
     const T fx = (T)ox, fy = (T)oy, fz = (T)oz0;
-    const int k0 = (int)(((long long)total * warp) / nwarps), k1 = (int)(((long long)total * (warp + 1)) / nwarps);
+    // a warp's share of the slots (total <= WorkP, so 32-bit products)
+    const int k0 = (int)((unsigned)(total * warp) / (unsigned)nwarps);
+    const int k1 = (int)((unsigned)(total * (warp + 1)) / (unsigned)nwarps);
     const T* recs = reinterpret_cast<const T*>(S.rec);
     int cur = -1;
     if constexpr (sizeof(T) == 4) {
@@ -1024,7 +1026,9 @@ __device__ __forceinline__ void p2g_runs(P2GTile<T, CA>& S, int total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int ox = lane >> 3, oy = (lane >> 1) & 3, oz0 = lane & 1;
     const T fx = (T)ox, fy = (T)oy, fz = (T)oz0;
-    const int k0 = (int)(((long long)total * warp) / nwarps), k1 = (int)(((long long)total * (warp + 1)) / nwarps);
+    // a warp's share of the slots (total <= WorkP, so 32-bit products)
+    const int k0 = (int)((unsigned)(total * warp) / (unsigned)nwarps);
+    const int k1 = (int)((unsigned)(total * (warp + 1)) / (unsigned)nwarps);
     const T* recs = reinterpret_cast<const T*>(S.rec);
     int k = k0;
     if constexpr (sizeof(T) == 4) {
@@ -1104,7 +1108,9 @@ __device__ __forceinline__ void p2g_runs_pairs(P2GTile<float, CA>& S, int total)
     const float2 fz0 = hw ? make_float2(1.f, 3.f) : make_float2(0.f, 2.f);
     const float2 fz1 = hw ? make_float2(0.f, 2.f) : make_float2(1.f, 3.f);
     const int wz0 = 8 + 2 * hw, wz1 = 10 - 2 * hw;
-    const int k0 = (int)(((long long)total * warp) / nwarps), k1 = (int)(((long long)total * (warp + 1)) / nwarps);
+    // a warp's share of the slots (total <= WorkP, so 32-bit products)
+    const int k0 = (int)((unsigned)(total * warp) / (unsigned)nwarps);
+    const int k1 = (int)((unsigned)(total * (warp + 1)) / (unsigned)nwarps);
     const float* recs = reinterpret_cast<const float*>(S.rec);
     int k = k0;
     while (k < k1) {
@@ -1152,10 +1158,12 @@ __device__ __forceinline__ void p2g_runs_pairs(P2GTile<float, CA>& S, int total)
 // received anything.
 template <typename T, int CA>
 __device__ __forceinline__ void p2g_flush(const DevParams<T>& P, const P2GTile<T, CA>& S, const int org[3],
-                                          vec4<T>* __restrict__ grid) {
+                                          vec4<T>* __restrict__ grid, int x0 = 0,
+                                          int x1 = P2GTile<T, CA>::TS - 1) {
     constexpr int TS = P2GTile<T, CA>::TS;
     constexpr int TC = P2GTile<T, CA>::TC;
-    for (int c = threadIdx.x; c < TC; c += blockDim.x) {
+    // only the x layers x0..x1 of the tile can hold anything
+    for (int c = x0 * TS * TS + (int)threadIdx.x; c < (x1 + 1) * TS * TS; c += blockDim.x) {
         const int ix = c / (TS * TS), iy = (c / TS) % TS, iz = c % TS;
         const int gx = org[0] + ix, gy = org[1] + iy, gz = org[2] + iz;
         if (gx < 0 || gy < 0 || gz < 0 || gx >= P.M[0] || gy >= P.M[1] || gz >= P.M[2]) continue;
@@ -1616,10 +1624,15 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             }
         }
         sort_ranked<T, CA>(S.p, j, rcell, rrank);
-        if constexpr (PAIRS) p2g_runs_pairs<true, CA>(S.p, sorted_total(S.p));
-        else p2g_runs<T, true, CA>(S.p, sorted_total(S.p));
+        const int total = sorted_total(S.p);
+        if constexpr (PAIRS) p2g_runs_pairs<true, CA>(S.p, total);
+        else p2g_runs<T, true, CA>(S.p, total);
+        // the records are sorted by cell, x-major: the first and the last give
+        // the x layers of the tile the scatter touched (cell x .. x + 3)
+        const int x0 = total > 0 ? S.p.scell[0] / (CA * CA) : 0;
+        const int x1 = total > 0 ? S.p.scell[total - 1] / (CA * CA) + 3 : -1;
         __syncthreads();
-        p2g_flush<T, CA>(P, S.p, porg, gnext);
+        p2g_flush<T, CA>(P, S.p, porg, gnext, x0, x1);
         mark_around(P, D.gmark_next, it.x);
         // a single scene: the next item's first barrier (after its tile wait)
         // separates this flush from the next item's writes to shared memory; a
