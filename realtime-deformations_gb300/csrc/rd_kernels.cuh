@@ -671,14 +671,17 @@ __device__ __forceinline__ bool cell_of_tile(const DevParams<T>& P, const int or
 // Marks the blocks within one block of block key (a tile of P2G nodes
 // spans at most the neighbouring blocks).
 template <typename T>
-__device__ __forceinline__ void mark_around(const DevParams<T>& P, uint8_t* marks, int gkey) {
+__device__ __forceinline__ void mark_around_block(const DevParams<T>& P, uint8_t* marks, int bx, int by, int bz) {
     const int t = threadIdx.x;
     if (t >= 27) return;
-    const int key = gkey - (int)P.block_base;
-    const int bz = key % P.NB[2], by = (key / P.NB[2]) % P.NB[1], bx = key / (P.NB[1] * P.NB[2]);
     const int nx = bx + t / 9 - 1, ny = by + (t / 3) % 3 - 1, nz = bz + t % 3 - 1;
     if (nx < 0 || ny < 0 || nz < 0 || nx >= P.NB[0] || ny >= P.NB[1] || nz >= P.NB[2]) return;
     marks[P.block_base + (nx * P.NB[1] + ny) * P.NB[2] + nz] = 1;
+}
+template <typename T>
+__device__ __forceinline__ void mark_around(const DevParams<T>& P, uint8_t* marks, int gkey) {
+    const int key = gkey - (int)P.block_base;
+    mark_around_block(P, marks, key / (P.NB[1] * P.NB[2]), (key / P.NB[2]) % P.NB[1], key % P.NB[2]);
 }
 
 // Marks the blocks holding nodes b - 1 .. b + 2 (one particle's stencil).
@@ -1347,6 +1350,7 @@ template <typename T> struct FusedShared {
     P2GTile<T, kBlk + 2> p;
     DevParams<T> par;        // the item's scene (batches)
     uint64_t tbar;           // mbarrier of the tile copy
+    int org[3];              // tile origin of the item whose tile is (being) copied
 };
 // Dynamic shared memory of k_g2p2g: the struct plus room to align it to the
 // 128 bytes a TMA destination needs.
@@ -1389,11 +1393,14 @@ template <bool BATCH> using FusedMaps = TileMaps<BATCH ? kBatchMaps : 1>;
 // One thread (always thread 0): the grid tile of work item `it` (the kTile^3
 // nodes from its tile origin) into S.graw by TMA with `map`, the tensor map
 // of the item's scene region of this step's grid.
+// The origin also goes to S.org, where the item reads it (one set of
+// divisions per item instead of one per thread).
 template <typename T>
 __device__ __forceinline__ void issue_tile(const DevParams<T>& P, const CUtensorMap* map, FusedShared<T>& S,
                                            int4 it) {
     int org[3];
     tile_origin(P, it.x, org);
+    S.org[0] = org[0]; S.org[1] = org[1]; S.org[2] = org[2];
     tma_load_4d(S.graw, map, &S.tbar, (uint32_t)(kTileCells * sizeof(vec4<T>)), org[2], org[1], org[0]);
 }
 
@@ -1405,6 +1412,7 @@ template <typename T>
 __device__ __forceinline__ void load_tile(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S, int4 it) {
     int org[3];
     tile_origin(P, it.x, org);
+    if (threadIdx.x == 0) { S.org[0] = org[0]; S.org[1] = org[1]; S.org[2] = org[2]; }
     const vec4<T>* g = static_cast<const vec4<T>*>(D.grid) + P.goff;
     for (int c = threadIdx.x; c < kTileCells; c += blockDim.x) {
         size_t lin;
@@ -1512,8 +1520,10 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
     vec4<T>* __restrict__ gnext = static_cast<vec4<T>*>(D.grid_next) + P.goff;
     const size_t n = (size_t)P.n;
     {
-        int org[3];
-        tile_origin(P, it.x, org);
+        // the origin thread 0 stored when it copied this tile (published by
+        // the barrier after the tile wait); it writes the next item's only
+        // after the barrier that follows the tile conversion
+        const int org[3] = {S.org[0], S.org[1], S.org[2]};
         const int porg[3] = {org[0] - 1, org[1] - 1, org[2] - 1};
         const int count = min(it.z, min(WorkP<T>::value, P.n - it.y));
         // one particle per thread (WorkP == blockDim): start its loads before
@@ -1633,7 +1643,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         const int x1 = total > 0 ? S.p.scell[total - 1] / (CA * CA) + 3 : -1;
         __syncthreads();
         p2g_flush<T, CA>(P, S.p, porg, gnext, x0, x1);
-        mark_around(P, D.gmark_next, it.x);
+        mark_around_block(P, D.gmark_next, (org[0] + 1) / kBlk, (org[1] + 1) / kBlk, (org[2] + 1) / kBlk);
         // a single scene: the next item's first barrier (after its tile wait)
         // separates this flush from the next item's writes to shared memory; a
         // batch copies the next scene's parameters before that barrier
