@@ -52,6 +52,10 @@ struct DevBufs {
     const int4* work;
     const uint32_t* nwork;
     uint32_t work_cap;
+    // fused kernel: the counter its CTAs claim work items from (zero at the
+    // launch) and the next launch's, which this launch zeroes
+    uint32_t* claim;
+    uint32_t* claim_next;
     void* grid;        // vec4 per cell
     void* grid_next;   // vec4 per cell: P2G of the next step (fused kernel)
     void* gforce;      // vec4 per cell (stage mode forces)
@@ -1351,6 +1355,7 @@ template <typename T> struct FusedShared {
     DevParams<T> par;        // the item's scene (batches)
     uint64_t tbar;           // mbarrier of the tile copy
     int org[3];              // tile origin of the item whose tile is (being) copied
+    uint32_t wi_next;        // the work item this CTA claimed next
 };
 // Dynamic shared memory of k_g2p2g: the struct plus room to align it to the
 // 128 bytes a TMA destination needs.
@@ -1512,7 +1517,7 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
 // is the item's scene copied to shared memory, and the item ends on a barrier.
 template <typename T, bool TRACK_FP, bool LAGGED, bool PAIRS, bool BATCH>
 __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
-                                           const int4 it, bool has_next, int4 nit, const CUtensorMap* maps) {
+                                           const int4 it, uint32_t nw, const CUtensorMap* maps) {
     static_assert(!PAIRS || sizeof(T) == 4, "the record-pairs scatter is FP32");
     constexpr int CA = kBlk + 2;
     const vec4<T>* __restrict__ pin = static_cast<const vec4<T>*>(D.pin);
@@ -1565,13 +1570,19 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         zero_tile(S.p);
         for (int c = threadIdx.x; c < P2GTile<T, CA>::NC; c += blockDim.x) S.p.cnt[c] = 0;
         __syncthreads();
-        // S.graw is free again: copy the next item's tile while this one runs
-        if (threadIdx.x == 0 && has_next) {
-            if constexpr (BATCH) {
-                if (nit.w < kBatchMaps)
-                    issue_tile(static_cast<const DevParams<T>*>(D.scenes)[nit.w], maps + nit.w, S, nit);
-            } else {
-                issue_tile(P, maps, S, nit);
+        // S.graw is free again: claim the next item and copy its tile while
+        // this one runs (the later barriers of this item publish S.wi_next)
+        if (threadIdx.x == 0) {
+            const uint32_t wn = atomicAdd(D.claim, 1u);
+            S.wi_next = wn;
+            if (wn < nw) {
+                const int4 nit = D.work[wn];
+                if constexpr (BATCH) {
+                    if (nit.w < kBatchMaps)
+                        issue_tile(static_cast<const DevParams<T>*>(D.scenes)[nit.w], maps + nit.w, S, nit);
+                } else {
+                    issue_tile(P, maps, S, nit);
+                }
             }
         }
         int rcell = 0xff, rrank = 0;  // this thread's record: cell and rank within it
@@ -1664,21 +1675,29 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
         *reinterpret_cast<FusedShared<T>*>(smem_fused + ((128u - (smem_addr(smem_fused) & 127u)) & 127u));
     const DevParams<T>* scenes = static_cast<const DevParams<T>*>(D.scenes);
     const uint32_t nw = min(*D.nwork, D.work_cap);
-    if (threadIdx.x == 0) mbar_init(&S.tbar);
-    __syncthreads();
-    uint32_t wi = blockIdx.x;
-    if (threadIdx.x == 0 && wi < nw) {
-        const int4 it0 = D.work[wi];
-        if constexpr (BATCH) {
-            if (it0.w < kBatchMaps) issue_tile(scenes[it0.w], &maps.m[it0.w], S, it0);
-        } else {
-            issue_tile(P0, &maps.m[0], S, it0);
+    // items are claimed one at a time from D.claim, so CTAs that drew small
+    // items take more of them; the next launch's counter is this launch's
+    // predecessor's, finished, and is zeroed here
+    if (blockIdx.x == 0 && threadIdx.x == 0) *D.claim_next = 0u;
+    if (threadIdx.x == 0) {
+        mbar_init(&S.tbar);
+        const uint32_t w0 = atomicAdd(D.claim, 1u);
+        S.wi_next = w0;
+        if (w0 < nw) {
+            const int4 it0 = D.work[w0];
+            if constexpr (BATCH) {
+                if (it0.w < kBatchMaps) issue_tile(scenes[it0.w], &maps.m[it0.w], S, it0);
+            } else {
+                issue_tile(P0, &maps.m[0], S, it0);
+            }
         }
     }
+    __syncthreads();
     // the k-th TMA tile of this CTA completes phase k & 1 of the mbarrier; the
-    // next item's copy is issued inside g2p2g_item once this tile is converted
+    // next item is claimed and its copy issued inside g2p2g_item once this
+    // tile is converted
     uint32_t parity = 0u;
-    for (; wi < nw; wi += gridDim.x) {
+    for (uint32_t wi = S.wi_next; wi < nw; wi = S.wi_next) {
         const int4 it = D.work[wi];
         bool arrived = true;
         if constexpr (BATCH) {
@@ -1703,13 +1722,10 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
             }
             return;
         }
-        const uint32_t wn = wi + gridDim.x;
-        const bool has_next = wn < nw;
-        const int4 nit = has_next ? D.work[wn] : make_int4(0, 0, 0, 0);
         if constexpr (BATCH)
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, true>(S.par, D, S, it, has_next, nit, &maps.m[0]);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, true>(S.par, D, S, it, nw, &maps.m[0]);
         else
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, false>(P0, D, S, it, has_next, nit, &maps.m[0]);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, false>(P0, D, S, it, nw, &maps.m[0]);
     }
 }
 

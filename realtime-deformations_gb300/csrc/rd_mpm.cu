@@ -410,7 +410,8 @@ struct rd_handle {
     uint8_t* gmark[2] = {nullptr, nullptr};  // blocks of grid[0] / grid[1] holding data
     uint32_t* cursor = nullptr;
     int4* work = nullptr;
-    uint32_t* nwork2 = nullptr;  // two item counters: the current sort's and the next's
+    uint32_t* nwork2 = nullptr;  // two item counters: the current sort's and the next's; then the
+                                 // fused kernel's two claim counters, by grid buffer (h->g)
     int nb = 0;                  // nwork2[nb] belongs to the last sort
     uint32_t* tile_sums = nullptr;
     uint32_t* tile_list = nullptr;  // non-empty tiles of the current sort, their count last
@@ -563,6 +564,8 @@ template <typename T> DevBufs bufs(rd_handle* h) {
     D.counts = h->counts;
     D.work = h->work;
     D.nwork = h->nwork2 + h->nb;
+    D.claim = h->nwork2 + 2 + h->g;
+    D.claim_next = h->nwork2 + 2 + (h->g ^ 1);
     D.work_cap = (uint32_t)h->work_cap;
     D.grid = h->grid[h->g];
     D.grid_next = h->grid[h->g ^ 1];
@@ -1439,7 +1442,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
         {(void**)&h->gmark[1], (size_t)h->nblocks, true},
         {(void**)&h->cursor, (size_t)h->nkeys * 4, true},
         {(void**)&h->work, h->work_cap * sizeof(int4), true},
-        {(void**)&h->nwork2, 8, true},
+        {(void**)&h->nwork2, 16, true},
         {(void**)&h->tile_sums, (size_t)((h->nkeys + kScanTile - 1) / kScanTile + 1) * 4, true},
         {(void**)&h->tile_list, (size_t)((h->nkeys + kScanTile - 1) / kScanTile + 1) * 4, true},
         {&h->grid[0], h->ncells * v4, true},
@@ -1486,7 +1489,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
     cudaMemsetAsync(h->gmark[1], 0, (size_t)h->nblocks, h->stream);
     cudaMemsetAsync(h->perm, 0, n * 4, h->stream);  // every entry is a valid index from the start
     cudaMemsetAsync(h->flags, 0, 4, h->stream);
-    cudaMemsetAsync(h->nwork2, 0, 8, h->stream);
+    cudaMemsetAsync(h->nwork2, 0, 16, h->stream);
     cudaMemsetAsync(h->rgba, 0xff, n * sizeof(uint32_t), h->stream);  // white
     rd_status st = encode_tile_maps(h);
     if (st == RD_OK) st = p.precision == RD_FP64 ? occupancy<double>(h) : occupancy<float>(h);
