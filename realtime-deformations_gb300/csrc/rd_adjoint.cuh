@@ -456,9 +456,11 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks<T>) k_adj_g2p(DevPa
                                                         const vec4<T>* __restrict__ split) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
     AdjG2PShared<T>& S = *reinterpret_cast<AdjG2PShared<T>*>(smem_raw);
-    const uint32_t nw = min(*D.nwork, D.work_cap);
+    uint32_t nf, nb;
+    work_counts(D, nf, nb);
+    const uint32_t nw = nf + nb;
     for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
-        const int4 it = D.work[wi];
+        const int4 it = work_item(D, nf, wi);
         if constexpr (BATCH) {
             copy_scene(S.par, D.scenes, it.w);
             __syncthreads();
@@ -616,9 +618,11 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjMinBlocks<T>) k_adj_p2g(DevPa
                                                         const vec4<T>* __restrict__ prev_split) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
     AdjP2GShared<T>& S = *reinterpret_cast<AdjP2GShared<T>*>(smem_raw);
-    const uint32_t nw = min(*D.nwork, D.work_cap);
+    uint32_t nf, nb;
+    work_counts(D, nf, nb);
+    const uint32_t nw = nf + nb;
     for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
-        const int4 it = D.work[wi];
+        const int4 it = work_item(D, nf, wi);
         if constexpr (BATCH) {
             copy_scene(S.par, D.scenes, it.w);
             __syncthreads();

@@ -50,7 +50,10 @@ struct DevBufs {
     uint32_t* keys_out;
     uint32_t* counts;
     const int4* work;
+    // items from the front of `work` (nwork) and, when nwork_back is set, from
+    // its back (work_item)
     const uint32_t* nwork;
+    const uint32_t* nwork_back;
     uint32_t work_cap;
     // fused kernel: the counter its CTAs claim work items from (zero at the
     // launch) and the next launch's, which this launch zeroes
@@ -87,6 +90,18 @@ struct DevBufs {
     int nscenes;
     const void* colliders;  // Collider<T>[ncol]
 };
+
+// The work list: `nf` items from the front of D.work and `nb` from its back,
+// the back ones stored from index work_cap - 1 downwards (work_item maps a
+// claim 0 .. work_items - 1 to its entry).  Without a back counter all items
+// are at the front.
+__device__ __forceinline__ void work_counts(const DevBufs& D, uint32_t& nf, uint32_t& nb) {
+    nf = min(*D.nwork, D.work_cap);
+    nb = D.nwork_back ? min(*D.nwork_back, D.work_cap - nf) : 0u;
+}
+__device__ __forceinline__ int4 work_item(const DevBufs& D, uint32_t nf, uint32_t c) {
+    return D.work[c < nf ? c : D.work_cap - 1u - (c - nf)];
+}
 
 // A box collider on the device: R (world from box, row-major), centre t, half
 // extents s, velocity v.
@@ -287,11 +302,16 @@ __global__ void __launch_bounds__(1024) k_tile_prefix(uint32_t* __restrict__ sum
                                                       uint32_t* __restrict__ nwork_next_sort, uint32_t n_expected,
                                                       uint32_t* flags, uint32_t* __restrict__ list,
                                                       const uint32_t* __restrict__ bcount = nullptr,
-                                                      int nblocks = 0) {
+                                                      int nblocks = 0,
+                                                      uint32_t* __restrict__ nwork_next_back = nullptr) {
     __shared__ uint2 s_w[32];   // per warp: (particles, non-empty tiles)
     __shared__ uint2 s_carry;   // totals of the previous trips
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) { s_carry = make_uint2(0u, 0u); *nwork_next_sort = 0u; }
+    if (tid == 0) {
+        s_carry = make_uint2(0u, 0u);
+        *nwork_next_sort = 0u;
+        if (nwork_next_back) *nwork_next_back = 0u;
+    }
     if (bcount) {
         for (int t = wid; t < ntiles; t += 32) {
             const int b0 = t * kBlocksPerTile + 2 * lane;
@@ -358,7 +378,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
                                                        const uint32_t* __restrict__ tile_list, int ntiles, int nkeys,
                                                        int4* __restrict__ work, uint32_t* __restrict__ nwork,
                                                        uint32_t work_cap, uint32_t wp, uint32_t* flags,
-                                                       const uint32_t* __restrict__ sblock, int nscenes) {
+                                                       const uint32_t* __restrict__ sblock, int nscenes,
+                                                       uint32_t* __restrict__ nwork_back = nullptr) {
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_blk[kBlocksPerTile];  // particles per block of this tile
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -408,11 +429,16 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(uint32_t* __restrict__ co
             if (ni) {
                 const uint32_t blk = (uint32_t)(t * kBlocksPerTile + b);
                 const int scene = nscenes > 1 ? scene_of(sblock, nscenes, blk) : 0;
-                uint32_t oi = atomicAdd(nwork, ni);
+                // with a back counter, items of more than half the work-item
+                // size fill the list from the front and smaller ones from the
+                // back, so a kernel claiming items in list order takes the
+                // large ones first and ends on small ones
+                const bool back = nwork_back && 2u * (bc / ni) <= wp;
+                uint32_t oi = atomicAdd(back ? nwork_back : nwork, ni);
                 uint32_t st = st0;
                 for (uint32_t j = 0; j < ni; ++j, ++oi) {
                     const uint32_t cnt = bc / ni + (j < bc % ni ? 1u : 0u);
-                    if (oi < work_cap) work[oi] = make_int4((int)blk, (int)st, (int)cnt, scene);
+                    if (oi < work_cap) work[back ? work_cap - 1u - oi : oi] = make_int4((int)blk, (int)st, (int)cnt, scene);
                     else atomicOr(flags, 4u);
                     st += cnt;
                 }
@@ -1311,9 +1337,11 @@ template <typename T, bool MOM, bool FORCE, bool BATCH>
 __global__ void __launch_bounds__(kP2GThreads<T>, sizeof(T) == 4 ? 3 : 1) k_p2g(DevParams<T> P0, DevBufs D) {
     extern __shared__ __align__(32) unsigned char smem_raw[];
     P2GShared<T>& S = *reinterpret_cast<P2GShared<T>*>(smem_raw);
-    const uint32_t nw = min(*D.nwork, D.work_cap);
+    uint32_t nf, nb;
+    work_counts(D, nf, nb);
+    const uint32_t nw = nf + nb;
     for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
-        const int4 it = D.work[wi];
+        const int4 it = work_item(D, nf, wi);
         if constexpr (BATCH) {
             copy_scene(S.par, D.scenes, it.w);
             __syncthreads();
@@ -1517,7 +1545,7 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
 // is the item's scene copied to shared memory, and the item ends on a barrier.
 template <typename T, bool TRACK_FP, bool LAGGED, bool PAIRS, bool BATCH>
 __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
-                                           const int4 it, uint32_t nw, const CUtensorMap* maps) {
+                                           const int4 it, uint32_t nf, uint32_t nw, const CUtensorMap* maps) {
     static_assert(!PAIRS || sizeof(T) == 4, "the record-pairs scatter is FP32");
     constexpr int CA = kBlk + 2;
     const vec4<T>* __restrict__ pin = static_cast<const vec4<T>*>(D.pin);
@@ -1576,7 +1604,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             const uint32_t wn = atomicAdd(D.claim, 1u);
             S.wi_next = wn;
             if (wn < nw) {
-                const int4 nit = D.work[wn];
+                const int4 nit = work_item(D, nf, wn);
                 if constexpr (BATCH) {
                     if (nit.w < kBatchMaps)
                         issue_tile(static_cast<const DevParams<T>*>(D.scenes)[nit.w], maps + nit.w, S, nit);
@@ -1674,7 +1702,9 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
     FusedShared<T>& S =
         *reinterpret_cast<FusedShared<T>*>(smem_fused + ((128u - (smem_addr(smem_fused) & 127u)) & 127u));
     const DevParams<T>* scenes = static_cast<const DevParams<T>*>(D.scenes);
-    const uint32_t nw = min(*D.nwork, D.work_cap);
+    uint32_t nf, nb;
+    work_counts(D, nf, nb);
+    const uint32_t nw = nf + nb;
     // items are claimed one at a time from D.claim, so CTAs that drew small
     // items take more of them; the next launch's counter is this launch's
     // predecessor's, finished, and is zeroed here
@@ -1684,7 +1714,7 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
         const uint32_t w0 = atomicAdd(D.claim, 1u);
         S.wi_next = w0;
         if (w0 < nw) {
-            const int4 it0 = D.work[w0];
+            const int4 it0 = work_item(D, nf, w0);
             if constexpr (BATCH) {
                 if (it0.w < kBatchMaps) issue_tile(scenes[it0.w], &maps.m[it0.w], S, it0);
             } else {
@@ -1698,7 +1728,7 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
     // tile is converted
     uint32_t parity = 0u;
     for (uint32_t wi = S.wi_next; wi < nw; wi = S.wi_next) {
-        const int4 it = D.work[wi];
+        const int4 it = work_item(D, nf, wi);
         bool arrived = true;
         if constexpr (BATCH) {
             copy_scene(S.par, D.scenes, it.w);
@@ -1723,9 +1753,9 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
             return;
         }
         if constexpr (BATCH)
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, true>(S.par, D, S, it, nw, &maps.m[0]);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, true>(S.par, D, S, it, nf, nw, &maps.m[0]);
         else
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, false>(P0, D, S, it, nw, &maps.m[0]);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, false>(P0, D, S, it, nf, nw, &maps.m[0]);
     }
 }
 
@@ -1795,10 +1825,12 @@ __global__ void __launch_bounds__(kThreads) k_g2p_stage(DevParams<T> P, DevBufs 
     __shared__ T sv[3 * kTileCells];
     vec4<T>* __restrict__ pl = static_cast<vec4<T>*>(D.pout);
     const vec4<T>* __restrict__ grid = static_cast<const vec4<T>*>(D.grid);
-    const uint32_t nw = min(*D.nwork, D.work_cap);
+    uint32_t nf, nb;
+    work_counts(D, nf, nb);
+    const uint32_t nw = nf + nb;
     const size_t n = (size_t)P.n;
     for (uint32_t wi = blockIdx.x; wi < nw; wi += gridDim.x) {
-        const int4 it = D.work[wi];
+        const int4 it = work_item(D, nf, wi);
         int org[3];
         tile_origin(P, it.x, org);
         for (int c = threadIdx.x; c < kTileCells; c += blockDim.x) {

@@ -331,7 +331,7 @@ struct rd_adjoint_data {
     void* gstore[2] = {nullptr, nullptr};    // nseg grids (m, p) of those states
     uint32_t* sperm[2] = {nullptr, nullptr}; // nseg sorted permutations of those states
     int4* swork[2] = {nullptr, nullptr};     // nseg work lists
-    uint32_t* snwork[2] = {nullptr, nullptr};// nseg work-item counts
+    uint32_t* snwork[2] = {nullptr, nullptr};// nseg (front, back) work-item counts
     void* ssplit[2] = {nullptr, nullptr};    // nseg plastic splits (U, s, V per sorted slot)
     int tail_store = 0;                 // the store the record's last segment is in
     cudaStream_t stream2 = nullptr;     // the reverse kernels
@@ -410,8 +410,10 @@ struct rd_handle {
     uint8_t* gmark[2] = {nullptr, nullptr};  // blocks of grid[0] / grid[1] holding data
     uint32_t* cursor = nullptr;
     int4* work = nullptr;
-    uint32_t* nwork2 = nullptr;  // two item counters: the current sort's and the next's; then the
-                                 // fused kernel's two claim counters, by grid buffer (h->g)
+    // item counters: front [0..1] and back [2..3] of the current sort's list
+    // and the next's (by nb), then the fused kernel's claim counters [4..5]
+    // (by grid buffer, h->g)
+    uint32_t* nwork2 = nullptr;
     int nb = 0;                  // nwork2[nb] belongs to the last sort
     uint32_t* tile_sums = nullptr;
     uint32_t* tile_list = nullptr;  // non-empty tiles of the current sort, their count last
@@ -564,8 +566,9 @@ template <typename T> DevBufs bufs(rd_handle* h) {
     D.counts = h->counts;
     D.work = h->work;
     D.nwork = h->nwork2 + h->nb;
-    D.claim = h->nwork2 + 2 + h->g;
-    D.claim_next = h->nwork2 + 2 + (h->g ^ 1);
+    D.nwork_back = h->nwork2 + 2 + h->nb;
+    D.claim = h->nwork2 + 4 + h->g;
+    D.claim_next = h->nwork2 + 4 + (h->g ^ 1);
     D.work_cap = (uint32_t)h->work_cap;
     D.grid = h->grid[h->g];
     D.grid_next = h->grid[h->g ^ 1];
@@ -646,7 +649,7 @@ template <typename T> int work_size(const rd_handle* h) {
 // particles by the scan's cursors itself: scatter false).
 template <typename T> rd_status sort_particles(rd_handle* h, bool scatter = true) {
     if (h->n == 0) {
-        RD_TRY(check_cuda(h, cudaMemsetAsync(h->nwork2, 0, 2 * sizeof(uint32_t), h->stream), "memset nwork"));
+        RD_TRY(check_cuda(h, cudaMemsetAsync(h->nwork2, 0, 4 * sizeof(uint32_t), h->stream), "memset nwork"));
         h->sorted = true;
         return RD_OK;
     }
@@ -672,22 +675,24 @@ template <typename T> rd_status sort_particles(rd_handle* h, bool scatter = true
     // creation) and clears nwork2[nb] for the next one
     uint32_t* nw = h->nwork2 + (h->nb ^ 1);
     uint32_t* nw_next = h->nwork2 + h->nb;
+    uint32_t* nw_back = h->nwork2 + 2 + (h->nb ^ 1);
+    uint32_t* nw_next_back = h->nwork2 + 2 + h->nb;
     long t = tmark_begin(h, RD_KERNEL_SCAN);
     if (ntiles <= kTileSumsInPrefix) {  // small grids: the prefix kernel sums the tiles itself
         k_tile_prefix<<<1, 1024, 0, h->stream>>>(h->tile_sums, ntiles, nw_next, (uint32_t)h->n, h->flags,
-                                                 h->tile_list, h->bcount, h->nblocks);
+                                                 h->tile_list, h->bcount, h->nblocks, nw_next_back);
     } else {
         k_tile_sums<<<blocks_for((size_t)ntiles * 32, 256), 256, 0, h->stream>>>(h->bcount, h->nblocks, ntiles,
                                                                                  h->tile_sums);
         RD_TRY(launched(h, "k_tile_sums"));
         k_tile_prefix<<<1, 1024, 0, h->stream>>>(h->tile_sums, ntiles, nw_next, (uint32_t)h->n, h->flags,
-                                                 h->tile_list);
+                                                 h->tile_list, nullptr, 0, nw_next_back);
     }
     const unsigned scan_grid = (unsigned)std::min<size_t>((size_t)ntiles, (size_t)h->sms * 2);
     k_scan<<<scan_grid, kScanThreads, 0, h->stream>>>(h->counts, h->cursor, h->bcount, h->tile_sums, h->tile_list,
                                                       ntiles, h->nkeys, h->work, nw, (uint32_t)h->work_cap,
                                                       (uint32_t)work_size<T>(h), h->flags, h->d_sblock,
-                                                      (int)h->scenes.size());
+                                                      (int)h->scenes.size(), nw_back);
     tmark_end(h, t);
     RD_TRY(launched(h, "k_scan", 2));
     h->nb ^= 1;
@@ -1442,7 +1447,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
         {(void**)&h->gmark[1], (size_t)h->nblocks, true},
         {(void**)&h->cursor, (size_t)h->nkeys * 4, true},
         {(void**)&h->work, h->work_cap * sizeof(int4), true},
-        {(void**)&h->nwork2, 16, true},
+        {(void**)&h->nwork2, 6 * sizeof(uint32_t), true},
         {(void**)&h->tile_sums, (size_t)((h->nkeys + kScanTile - 1) / kScanTile + 1) * 4, true},
         {(void**)&h->tile_list, (size_t)((h->nkeys + kScanTile - 1) / kScanTile + 1) * 4, true},
         {&h->grid[0], h->ncells * v4, true},
@@ -1489,7 +1494,7 @@ rd_status create_impl(const rd_params* params, int nscenes, rd_handle** out) {
     cudaMemsetAsync(h->gmark[1], 0, (size_t)h->nblocks, h->stream);
     cudaMemsetAsync(h->perm, 0, n * 4, h->stream);  // every entry is a valid index from the start
     cudaMemsetAsync(h->flags, 0, 4, h->stream);
-    cudaMemsetAsync(h->nwork2, 0, 16, h->stream);
+    cudaMemsetAsync(h->nwork2, 0, 6 * sizeof(uint32_t), h->stream);
     cudaMemsetAsync(h->rgba, 0xff, n * sizeof(uint32_t), h->stream);  // white
     rd_status st = encode_tile_maps(h);
     if (st == RD_OK) st = p.precision == RD_FP64 ? occupancy<double>(h) : occupancy<float>(h);
@@ -2071,7 +2076,7 @@ rd_status adj_alloc(rd_handle* h, int steps, int every) {
             RD_TRY(grow(&a.gstore[b], nseg * a.grid_bytes));
             RD_TRY(grow((void**)&a.sperm[b], nseg * n * sizeof(uint32_t)));
             RD_TRY(grow((void**)&a.swork[b], nseg * h->work_cap * sizeof(int4)));
-            RD_TRY(grow((void**)&a.snwork[b], nseg * sizeof(uint32_t)));
+            RD_TRY(grow((void**)&a.snwork[b], 2 * nseg * sizeof(uint32_t)));
             RD_TRY(grow(&a.ssplit[b], nseg * a.split_bytes));
         }
         a.nseg = nseg;
@@ -2120,8 +2125,13 @@ template <typename T> rd_status stored_segment(rd_handle* h, double dt, int len,
             st = check_cuda(h, cudaMemcpyAsync(at(a.gstore[b], (size_t)j, a.grid_bytes), h->grid[h->g ^ 1], a.grid_bytes,
                                                cudaMemcpyDeviceToDevice, h->stream),
                             "segment grid");
+        // the step's list counts, front and back
         if (st == RD_OK)
-            st = check_cuda(h, cudaMemcpyAsync(a.snwork[b] + j, h->nwork2 + h->nb, sizeof(uint32_t),
+            st = check_cuda(h, cudaMemcpyAsync(a.snwork[b] + 2 * j, h->nwork2 + h->nb, sizeof(uint32_t),
+                                               cudaMemcpyDeviceToDevice, h->stream),
+                            "segment sort");
+        if (st == RD_OK)
+            st = check_cuda(h, cudaMemcpyAsync(a.snwork[b] + 2 * j + 1, h->nwork2 + 2 + h->nb, sizeof(uint32_t),
                                                cudaMemcpyDeviceToDevice, h->stream),
                             "segment sort");
     }
@@ -2334,7 +2344,8 @@ template <typename T> rd_status adjoint_sweep(rd_handle* h, int nxt) {
             DevBufs D = bufs<T>(h);
             D.perm = a.sperm[b] + (size_t)j * n;
             D.work = a.swork[b] + (size_t)j * h->work_cap;
-            D.nwork = a.snwork[b] + j;
+            D.nwork = a.snwork[b] + 2 * j;
+            D.nwork_back = a.snwork[b] + 2 * j + 1;
             RD_TRY(check_cuda(h, cudaMemsetAsync(a.agrid, 0, a.grid_bytes, rs), "adjoint grid"));
             const AdjState<T> An = adj_view<T>(h, nxt), Ap = adj_view<T>(h, 2), Ac = adj_view<T>(h, cur);
             long t = tmark_begin(h, RD_KERNEL_ADJ_G2P);
