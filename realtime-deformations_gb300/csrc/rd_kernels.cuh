@@ -1563,6 +1563,10 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         // the tile is staged so the two latencies overlap
         const int j = threadIdx.x;
         const bool mine = j < count && RD_IN_BOUNDS(it.y + j, n) && RD_IN_BOUNDS(D.perm[it.y + j], n);
+        // thread 0 claims the next item now, so the atomic's round trip passes
+        // while the tile is converted
+        uint32_t wn = 0u;
+        if (threadIdx.x == 0) wn = atomicAdd(D.claim, 1u);
         Particle<T> p;
         T FP[9];
         if (mine) {
@@ -1595,16 +1599,16 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             }
             S.gv[c] = mk4<T>(v0, v1, v2, T(0));
         }
+        int4 nit = make_int4(0, 0, 0, 0);
+        if (threadIdx.x == 0 && wn < nw) nit = work_item(D, nf, wn);
         zero_tile(S.p);
         for (int c = threadIdx.x; c < P2GTile<T, CA>::NC; c += blockDim.x) S.p.cnt[c] = 0;
         __syncthreads();
-        // S.graw is free again: claim the next item and copy its tile while
-        // this one runs (the later barriers of this item publish S.wi_next)
+        // S.graw is free again: copy the next item's tile while this one runs
+        // (the later barriers of this item publish S.wi_next)
         if (threadIdx.x == 0) {
-            const uint32_t wn = atomicAdd(D.claim, 1u);
             S.wi_next = wn;
             if (wn < nw) {
-                const int4 nit = work_item(D, nf, wn);
                 if constexpr (BATCH) {
                     if (nit.w < kBatchMaps)
                         issue_tile(static_cast<const DevParams<T>*>(D.scenes)[nit.w], maps + nit.w, S, nit);
