@@ -29,6 +29,7 @@ template <typename T> struct DevParams {
     T hinv_pow2;   // 1 / h when h is a power of two (x / h == x * hinv_pow2 exactly), else 0
     T mu0, lambda0, xi;
     T lo, hi;      // singular value clamp
+    T elo, ehi;    // eigenvalues of F^T F - I for stress_direct (elo >= ehi: not used)
     T g[3];
     T xlo, xhi[3]; // position clamp (material_point_method.cpp:381-388)
     T fscale;      // force scale in P2G: dt when fused with the momentum, 1 alone
@@ -568,17 +569,21 @@ template <typename T> struct Split {
 // F_P <- F_E^-1 Fhat with Fhat = F_E* F_P); with the full F_P,
 // F_P <- V (S / clamp(S)) V^T F_P.  s_i - 1 for an unclamped value comes
 // from svd3_near without cancellation.
-template <typename T, bool TRACK_FP>
-__device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T F[9], T& Jp, T FP[9],
-                                         Split<T>& sp, T* s_out = nullptr, T* sm1_out = nullptr,
-                                         T* V_out = nullptr) {
+template <typename T>
+__device__ __forceinline__ void f_star(const DevParams<T>& P, const T Bm[9], const T F[9], T Fs[9]) {
     T A[9];
     const T ddt = P.dinv * P.dt;
 #pragma unroll
     for (int e = 0; e < 9; ++e) A[e] = Bm[e] * ddt;
     A[0] += T(1); A[4] += T(1); A[8] += T(1);
-    T Fs[9];
     matmul3(Fs, A, F);
+}
+
+// The split of a given F_E* (Fs), as update_F makes it.
+template <typename T, bool TRACK_FP>
+__device__ __forceinline__ void update_F_star(const DevParams<T>& P, const T Fs[9], T F[9], T& Jp, T FP[9],
+                                              Split<T>& sp, T* s_out = nullptr, T* sm1_out = nullptr,
+                                              T* V_out = nullptr) {
     T s[3], sm1[3], V[9];
     svd3_near(Fs, sp.U, s, sm1, V);
     if (s_out) {
@@ -629,6 +634,15 @@ __device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T
     }
 }
 
+template <typename T, bool TRACK_FP>
+__device__ __forceinline__ void update_F(const DevParams<T>& P, const T Bm[9], T F[9], T& Jp, T FP[9],
+                                         Split<T>& sp, T* s_out = nullptr, T* sm1_out = nullptr,
+                                         T* V_out = nullptr) {
+    T Fs[9];
+    f_star(P, Bm, F, Fs);
+    update_F_star<T, TRACK_FP>(P, Fs, F, Jp, FP, sp, s_out, sm1_out, V_out);
+}
+
 // scale * P F^T of F = U sc V^T (the split just made), as stress_PFt computes
 // it from an SVD of F: U diag(2 mu (sc - d) sc) U^T + lambda (J - 1) J I with
 // J = sgn prod sc and J - 1 expanded in sc - 1 so nothing cancels.  The
@@ -665,6 +679,101 @@ __device__ __forceinline__ void stress_from_split(const DevParams<T>& P, const S
 // Index into the 6 entries of a symmetric 3x3 matrix (00 01 02 11 12 22).
 __host__ __device__ constexpr int sym6(int r, int c) {
     return r <= c ? (r == 0 ? c : (r == 1 ? 2 + c : 5)) : (c == 0 ? r : (c == 1 ? 2 + r : 5));
+}
+
+// ---------------------------------------------------------------- stress without an SVD
+// S = F^T F - I as 6 entries (sym6), formed from G = F - I as svd3_near forms
+// it, and det F - 1 expanded in G (trace, principal 2x2 minors,
+// determinant), so neither cancels when F is near the identity.
+template <typename T>
+__device__ __forceinline__ void strain_of(const T F[9], T S[6], T& jm1) {
+    T G[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) G[e] = F[e];
+    G[0] -= T(1); G[4] -= T(1); G[8] -= T(1);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = r; c < 3; ++c)
+            S[sym6(r, c)] = (G[3 * r + c] + G[3 * c + r]) + (G[r] * G[c] + G[3 + r] * G[3 + c] + G[6 + r] * G[6 + c]);
+    jm1 = (G[0] + G[4] + G[8]) + ((G[0] * G[4] - G[1] * G[3]) + (G[0] * G[8] - G[2] * G[6]) +
+                                  (G[4] * G[8] - G[5] * G[7])) + det3(G);
+}
+
+// Sylvester's criterion: the symmetric matrix is positive definite when its
+// leading principal minors are positive (false for NaN).
+template <typename T>
+__device__ __forceinline__ bool pos_def(T m00, T m01, T m02, T m11, T m12, T m22) {
+    const T d2 = m00 * m11 - m01 * m01;
+    const T d3 = m00 * (m11 * m22 - m12 * m12) - m01 * (m01 * m22 - m12 * m02) + m02 * (m01 * m12 - m11 * m02);
+    return m00 > T(0) && d2 > T(0) && d3 > T(0);
+}
+
+// Whether an F_E* with strain S and det - 1 jm1 (strain_of) is clamped
+// nowhere: every eigenvalue e_i = s_i^2 - 1 of S inside (P.elo, P.ehi), that
+// is S - elo I and ehi I - S positive definite, and det F_E* > 0.  The host
+// sets elo = lo^2 - 1 and ehi = hi^2 - 1 moved inwards by 1e-5, far more than
+// the rounding of this test or of the singular values svd3_near finds, so a
+// particle accepted here is one that update_F would leave unclamped too.
+template <typename T>
+__device__ __forceinline__ bool inside_clamp(const DevParams<T>& P, const T S[6], T jm1) {
+    const T a = P.elo, b = P.ehi;
+    return jm1 > T(-1) && pos_def(S[0] - a, S[1], S[2], S[3] - a, S[4], S[5] - a) &&
+           pos_def(b - S[0], -S[1], -S[2], b - S[3], -S[4], b - S[5]);
+}
+
+// scale * P F^T for an F that inside_clamp accepted (so F_E = F_E*, J_P and
+// F_P unchanged), without an SVD.  The polar factor is R = F (I + S)^(-1/2),
+// so F - R = F Q with Q = I - (I + S)^(-1/2) = sum_k q_k S^k,
+// q_k = (-1)^(k+1) C(2k, k) / 4^k (the binomial series, exact binary
+// fractions), and 2 mu (F - R) F^T = 2 mu F Q F^T; with F = U S V^T this is
+// the U diag(2 mu (s - 1) s) U^T of stress_from_split.  The series is summed
+// through the Cayley-Hamilton theorem: S^3 = I1 S^2 - I2 S + I3 I with the
+// invariants of S, so S^k = a_k I + b_k S + c_k S^2 with scalar recurrences
+// and Q = alpha I + beta S + gamma S^2.  Seven terms: the host uses this
+// only while |e_i| <= 0.1, where the first term left out, q_8 e^8, is below
+// 4e-8 of Q's eigenvalue (about e / 2).  The isotropic part lambda (J - 1) J uses J - 1 from strain_of.
+template <typename T>
+__device__ __forceinline__ void stress_direct(const DevParams<T>& P, const T F[9], const T S[6], T jm1, T Jp,
+                                              T scale, T out[6]) {
+    const T I1 = S[0] + S[3] + S[5];
+    const T c00 = S[3] * S[5] - S[4] * S[4], c11 = S[0] * S[5] - S[2] * S[2], c22 = S[0] * S[3] - S[1] * S[1];
+    const T I2 = c00 + c11 + c22;
+    const T I3 = S[0] * c00 - S[1] * (S[1] * S[5] - S[4] * S[2]) + S[2] * (S[1] * S[4] - S[3] * S[2]);
+    constexpr T q[8] = {T(0), T(1) / T(2), T(-3) / T(8), T(5) / T(16), T(-35) / T(128), T(63) / T(256),
+                        T(-231) / T(1024), T(429) / T(2048)};
+    // S^2 is (a, b, c) = (0, 0, 1); S^1 and S^2 give beta = q1, gamma = q2
+    T a = T(0), b = T(0), c = T(1);
+    T al = T(0), be = q[1], ga = q[2];
+#pragma unroll
+    for (int k = 3; k <= 7; ++k) {
+        const T an = c * I3, bn = a - c * I2, cn = b + c * I1;
+        a = an; b = bn; c = cn;
+        al += q[k] * a; be += q[k] * b; ga += q[k] * c;
+    }
+    T Q[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = r; cc < 3; ++cc) {
+            const T s2 = S[sym6(r, 0)] * S[sym6(0, cc)] + S[sym6(r, 1)] * S[sym6(1, cc)] +
+                         S[sym6(r, 2)] * S[sym6(2, cc)];
+            const T v = be * S[sym6(r, cc)] + ga * s2 + (r == cc ? al : T(0));
+            Q[3 * r + cc] = v;
+            Q[3 * cc + r] = v;
+        }
+    T FQ[9];
+    matmul3(FQ, F, Q);
+    const T hard = exp_(P.xi * (T(1) - Jp));
+    const T mu2 = T(2) * (P.mu0 * hard), lam = P.lambda0 * hard;
+    const T iso = lam * jm1 * (T(1) + jm1);
+    int k = 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int cc = r; cc < 3; ++cc, ++k)
+            out[k] = scale * (mu2 * (FQ[3 * r] * F[3 * cc] + FQ[3 * r + 1] * F[3 * cc + 1] +
+                                     FQ[3 * r + 2] * F[3 * cc + 2]) + (r == cc ? iso : T(0)));
 }
 
 template <typename T>
@@ -1517,15 +1626,37 @@ __device__ __forceinline__ void g2p_gather(const vec4<T>* __restrict__ gv, const
 // lagged B, or the one just gathered): F_E, J_P (and F_P) updated and
 // stored (planes 5-6 and the F_P planes), the finite check of those, and
 // the scaled stress sc P F^T of the next P2G as 6 symmetric entries.
+// FP32, when the split is not kept for the adjoint: a warp whose particles
+// are all clamped nowhere (inside_clamp) takes F_E = F_E* and the stress from
+// stress_direct, with no SVD; any other warp runs the SVD for all its
+// particles, so the two paths never run one after the other in a warp.
 template <typename T, bool TRACK_FP>
 __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T>& p, T FP[9], const T Bm[9],
                                                vec4<T>* __restrict__ pout, size_t n, size_t s, T G6[6],
                                                bool& finite, void* split_out) {
-    Split<T> sp;
-    T sv[3], svm1[3], V[9];
-    update_F<T, TRACK_FP>(P, Bm, p.F, p.Jp, FP, sp, sv, svm1, V);
-    if (split_out) store_split(static_cast<vec4<T>*>(split_out), n, s, sp.U, sv, svm1, V);
-    stress_from_split(P, sp, p.Jp, P.fscale * (p.vol * P.dinv), G6);
+    T Fs[9];
+    f_star(P, Bm, p.F, Fs);
+    const T scale = P.fscale * (p.vol * P.dinv);
+    bool direct = false;
+    if constexpr (sizeof(T) == 4) {
+        if (!split_out && P.elo < P.ehi) {
+            T S6[6], jm1;
+            strain_of(Fs, S6, jm1);
+            direct = __all_sync(__activemask(), inside_clamp(P, S6, jm1));
+            if (direct) {
+                stress_direct(P, Fs, S6, jm1, p.Jp, scale, G6);
+#pragma unroll
+                for (int e = 0; e < 9; ++e) p.F[e] = Fs[e];
+            }
+        }
+    }
+    if (!direct) {
+        Split<T> sp;
+        T sv[3], svm1[3], V[9];
+        update_F_star<T, TRACK_FP>(P, Fs, p.F, p.Jp, FP, sp, sv, svm1, V);
+        if (split_out) store_split(static_cast<vec4<T>*>(split_out), n, s, sp.U, sv, svm1, V);
+        stress_from_split(P, sp, p.Jp, scale, G6);
+    }
     store_particle_back(pout, n, s, p);
     if (TRACK_FP) store_fp(pout, n, s, FP);
     // a NaN or infinity anywhere makes the sum non-finite (the values are far

@@ -517,6 +517,12 @@ DevParams<T> params_of(const rd_params& p, const int NB[3], int nkeys, int n, do
     // material_point_method.cpp:320: (float)(1 - theta) evaluated in double
     P.lo = (T)(1.0 - p.theta_c);
     P.hi = (T)(1.0 + p.theta_s);
+    // the stress without an SVD (stress_direct): FP32 only, and while the
+    // clamp keeps every |s_i^2 - 1| <= 0.1, where its series converges fast
+    const double elo = (double)P.lo * (double)P.lo - 1.0 + 1e-5, ehi = (double)P.hi * (double)P.hi - 1.0 - 1e-5;
+    const bool direct = sizeof(T) == 4 && elo >= -0.1 && ehi <= 0.1 && elo < ehi;
+    P.elo = direct ? (T)elo : T(1);
+    P.ehi = direct ? (T)ehi : T(-1);
     for (int a = 0; a < 3; ++a) P.g[a] = (T)p.gravity[a];
     volatile T xl = T(3) * hh;
     P.xlo = xl;

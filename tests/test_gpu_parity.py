@@ -167,6 +167,53 @@ def test_one_step_perturbed_matches_oracle(built_pkg, orc, seed):
     compare_particles(sim.get_particles(), o, float(h), TOL1)
 
 
+@pytest.mark.parametrize("track_fp", [0, 1])
+def test_unclamped_and_clamped_warps_match_oracle(built_pkg, orc, track_fp):
+    """The fused step's two ways to the stress: warps whose particles are all
+    inside the clamp take F_E = F_E* and the stress without an SVD, other
+    warps the SVD.  The half x < 0.5 of the ball holds F_E within 1e-3 of a
+    rotation (no particle clamped, so its warps go the direct way), the other
+    half F_E spread past both clamp bounds (most warps there have a clamped
+    particle).  Three steps against the FP64 oracle: with strong stresses and
+    random velocities the FP32 oracle's own grid velocities are ~1e-5 from
+    the FP64 ones, so the FP32 step is held to the FP64 oracle and to no
+    larger an error than the FP32 oracle makes."""
+    h, x, v, m, B, FE, FP = perturbed_inputs(orc, 17, 5000, 32, scale_B=0.1, scale_F=1e-3)
+    rng = np.random.default_rng(18)
+    ang = rng.normal(0, 1.0, (len(m), 3))
+    for i in range(len(m)):  # a rotation times a stretch
+        a = ang[i]
+        K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+        t = np.linalg.norm(a)
+        R = np.eye(3) + np.sin(t) / t * K + (1 - np.cos(t)) / t ** 2 * K @ K
+        spread = 1e-3 if x[i, 0] < 0.5 else 2e-2
+        FE[i] = (R @ (np.eye(3) + rng.normal(0, spread, (3, 3)))).reshape(9).astype(np.float32)
+    right = x[:, 0] >= 0.5
+    sv = np.linalg.svd(FE.reshape(-1, 3, 3).astype(np.float64), compute_uv=False)
+    assert np.all((sv[~right] > 0.98) & (sv[~right] < 1.005))
+    assert np.mean(np.any((sv[right] < 0.975) | (sv[right] > 1.0075), axis=1)) > 0.3
+    sim = make_sim(built_pkg, (32, 32, 32), len(m), float(h), track_fp=track_fp)
+    sim.set_particles(x, v, m, B=B, FE=FE, FP=FP)
+    sim.init_volumes()
+    P = orc.Params(32, 32, 32, float(h))
+    o64 = orc.OracleSim(P, x, v, m, B, FE, FP, dtype=np.float64)
+    o32 = orc.OracleSim(P, x, v, m, B, FE, FP)
+    for o in (o64, o32):
+        o.init()
+        o.step(1e-4, 3)
+    sim.step(1e-4, 3)
+    got = sim.get_particles()
+    compare_particles(got, o64, float(h), TOL1)
+    if track_fp:
+        assert rel(got["FP"], o64.FP) < 5e-5
+    grd = sim.get_grid()
+    assert rel(grd["mass"], o64.gmass) < 1e-6
+    for k, own in (("v", rel(o32.v, o64.v)), ("gvel", rel(o32.gvel, o64.gvel))):
+        err = rel(got["v"], o64.v) if k == "v" else rel(grd["vel"], o64.gvel)
+        assert err < TOL1 and err <= 1.5 * own, (k, err, own)
+    assert sim.flags() == 0
+
+
 def test_stagewise_matches_oracle(built_pkg, orc):
     """rd_stage runs the reference's seven stages one at a time; each one's grid
     and particle state agree with the oracle's same stage."""
