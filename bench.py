@@ -66,10 +66,12 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--cpu-baseline", type=int, default=1, help="time the single-core CPU baseline (rank 0, N=1)")
     ap.add_argument("--adjoint", type=int, default=1, help="measure forward + adjoint on the 65,536-particle cube")
-    ap.add_argument("--only", choices=("batched", "adjoint", "batched_adjoint", "snowball", "implicit", "profile"),
+    ap.add_argument("--only", choices=("batched", "adjoint", "batched_adjoint", "snowball", "implicit", "profile",
+                                       "profile_batched"),
                     default=None,
                     help="run one secondary measurement alone and print its JSON; 'profile' only initialises "
-                         "the workload and runs --warmup + --steps steps (for ncu captures)")
+                         "the workload and runs --warmup + --steps steps (for ncu captures), 'profile_batched' "
+                         "the same for the 64-scene batch at its default tuning")
     ap.add_argument("--snowball", type=int, default=1, help="measure the 8,192-particle snowball on 64^3")
     ap.add_argument("--link", type=int, default=1, help="measure the host link (pinned copies each way)")
     ap.add_argument("--implicit", type=int, default=1, help="time timeIntegration (implicit L-BFGS)")
@@ -924,6 +926,19 @@ def run_only(args):
         sim.synchronize()
         out = {"workload": sc.name, "particles": sc.n, "steps": args.warmup + args.steps, "flags": sim.flags()}
         sim.close()
+    elif args.only == "profile_batched":
+        from rd_gb300 import scenes
+        batch = scenes.uneven_snowballs(seed=0)
+        b = pkg.Batch([pkg.make_params(*s.grid, s.n, s.h, **s.params()) for s in batch])
+        for i, s in enumerate(batch):
+            b.set_particles(i, s.x, s.v, s.mass)
+        b.init_volumes()
+        b.step(batch[0].dt, args.warmup)
+        b.step(batch[0].dt, args.steps)
+        b.synchronize()
+        out = {"workload": "uneven_snowballs", "scenes": len(batch), "particles": b.n,
+               "steps": args.warmup + args.steps, "flags": b.flags()}
+        b.close()
     elif args.only == "snowball":
         out = measure_snowball(pkg, 0, max(args.warmup, 3))
     elif args.only == "implicit":

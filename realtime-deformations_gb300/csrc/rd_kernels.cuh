@@ -1756,7 +1756,15 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             // split is live across the gather
             T G6[6];
             bool finite = true;
-            if constexpr (LAGGED) split_particle<T, TRACK_FP>(P, p, FP, p.B, pout, n, s, G6, finite, D.split_out);
+            // the stress, m, V, the id and x wait in this thread's record slot
+            // (written only after the gather), holding no registers across it
+            vec4<T>* stash = &S.p.rec[j * kRecV4 + 4];
+            if constexpr (LAGGED) {
+                split_particle<T, TRACK_FP>(P, p, FP, p.B, pout, n, s, G6, finite, D.split_out);
+                stash[0] = mk4<T>(G6[0], G6[1], G6[2], G6[3]);
+                stash[1] = mk4<T>(G6[4], G6[5], p.m, p.vol);
+                stash[2] = mk4<T>(id_to_real<T>(p.id), p.x[0], p.x[1], p.x[2]);
+            }
             Stencil<T> St;
             const bool ok = make_stencil(P, p.x, org, St);
             if (!ok) raise_flag(D.flags, 4u);
@@ -1765,6 +1773,12 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
 #pragma unroll
             for (int e = 0; e < 9; ++e) Bp[e] = T(0);
             if (ok) g2p_gather(S.gv, St, vp, Bp);
+            if constexpr (LAGGED) {
+                const vec4<T> a = stash[0], b = stash[1], c = stash[2];
+                G6[0] = a.x; G6[1] = a.y; G6[2] = a.z; G6[3] = a.w; G6[4] = b.x; G6[5] = b.y;
+                p.m = b.z; p.vol = b.w; p.id = real_to_id<T>(c.x);
+                p.x[0] = c.y; p.x[1] = c.z; p.x[2] = c.w;
+            }
             if constexpr (!LAGGED) split_particle<T, TRACK_FP>(P, p, FP, Bp, pout, n, s, G6, finite, D.split_out);
 #pragma unroll
             for (int a = 0; a < 3; ++a) p.v[a] = vp[a];
