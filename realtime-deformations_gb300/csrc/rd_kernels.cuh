@@ -1493,6 +1493,7 @@ template <typename T> struct FusedShared {
     uint64_t tbar;           // mbarrier of the tile copy
     int org[3];              // tile origin of the item whose tile is (being) copied
     uint32_t wi_next;        // the work item this CTA claimed next
+    uint32_t wi_ahead;       // thread 0: the one claimed after it
 };
 // Dynamic shared memory of k_g2p2g: the struct plus room to align it to the
 // 128 bytes a TMA destination needs.
@@ -1672,8 +1673,10 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
 // gathered.  The item's grid tile is in S.graw; once it is converted,
 // thread 0 copies the next item's tile (nit) in by TMA while this item runs,
 // with maps[0] for a single scene or maps[scene] for a batch scene that has a
-// map (the next item's scene parameters from the batch's table).  BATCH: P
-// is the item's scene copied to shared memory, and the item ends on a barrier.
+// map (the next item's scene parameters from the batch's table).  The next
+// item was claimed one item ago (S.wi_ahead); this item's flush claims the
+// one after it.  BATCH: P is the item's scene copied to shared memory, and
+// the item ends on a barrier.
 template <typename T, bool TRACK_FP, bool LAGGED, bool PAIRS, bool BATCH>
 __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
                                            const int4 it, uint32_t nf, uint32_t nw, const CUtensorMap* maps) {
@@ -1694,16 +1697,21 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         // the tile is staged so the two latencies overlap
         const int j = threadIdx.x;
         const bool mine = j < count && RD_IN_BOUNDS(it.y + j, n) && RD_IN_BOUNDS(D.perm[it.y + j], n);
-        // thread 0 claims the next item now, so the atomic's round trip passes
-        // while the tile is converted
-        uint32_t wn = 0u;
-        if (threadIdx.x == 0) wn = atomicAdd(D.claim, 1u);
         Particle<T> p;
         T FP[9];
         if (mine) {
             const uint32_t src = D.perm[it.y + j];
             load_particle(pin, n, src, p);
             if (TRACK_FP) load_fp(pin, n, src, FP);
+        }
+        // thread 0 holds the next item's index, claimed during the previous
+        // item's flush: its work item is read now, the load passing while the
+        // tile is converted
+        uint32_t wn = 0u;
+        int4 nit = make_int4(0, 0, 0, 0);
+        if (threadIdx.x == 0) {
+            wn = S.wi_ahead;
+            if (wn < nw) nit = work_item(D, nf, wn);
         }
         // the (m, p) tile arrived by TMA (nodes outside the grid read as
         // zero): the grid update, walls and colliders into velocities
@@ -1730,8 +1738,6 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
             }
             S.gv[c] = mk4<T>(v0, v1, v2, T(0));
         }
-        int4 nit = make_int4(0, 0, 0, 0);
-        if (threadIdx.x == 0 && wn < nw) nit = work_item(D, nf, wn);
         zero_tile(S.p);
         for (int c = threadIdx.x; c < P2GTile<T, CA>::NC; c += blockDim.x) S.p.cnt[c] = 0;
         __syncthreads();
@@ -1830,8 +1836,13 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         const int x0 = total > 0 ? S.p.scell[0] / (CA * CA) : 0;
         const int x1 = total > 0 ? S.p.scell[total - 1] / (CA * CA) + 3 : -1;
         __syncthreads();
+        // thread 0 claims the item after the next one; the atomic's round trip
+        // passes during the flush
+        uint32_t claim = nw;
+        if (threadIdx.x == 0 && S.wi_next < nw) claim = atomicAdd(D.claim, 1u);
         p2g_flush<T, CA>(P, S.p, porg, gnext, x0, x1);
         mark_around_block(P, D.gmark_next, (org[0] + 1) / kBlk, (org[1] + 1) / kBlk, (org[2] + 1) / kBlk);
+        if (threadIdx.x == 0) S.wi_ahead = claim;
         // a single scene: the next item's first barrier (after its tile wait)
         // separates this flush from the next item's writes to shared memory; a
         // batch copies the next scene's parameters before that barrier
@@ -1855,13 +1866,15 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
     work_counts(D, nf, nb);
     const uint32_t nw = nf + nb;
     // items are claimed one at a time from D.claim, so CTAs that drew small
-    // items take more of them; the next launch's counter is this launch's
-    // predecessor's, finished, and is zeroed here
+    // items take more of them (each CTA holds the next item and the one after
+    // it); the next launch's counter is this launch's predecessor's,
+    // finished, and is zeroed here
     if (blockIdx.x == 0 && threadIdx.x == 0) *D.claim_next = 0u;
     if (threadIdx.x == 0) {
         mbar_init(&S.tbar);
         const uint32_t w0 = atomicAdd(D.claim, 1u);
         S.wi_next = w0;
+        S.wi_ahead = w0 < nw ? atomicAdd(D.claim, 1u) : nw;
         if (w0 < nw) {
             const int4 it0 = work_item(D, nf, w0);
             if constexpr (BATCH) {
@@ -1873,8 +1886,8 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
     }
     __syncthreads();
     // the k-th TMA tile of this CTA completes phase k & 1 of the mbarrier; the
-    // next item is claimed and its copy issued inside g2p2g_item once this
-    // tile is converted
+    // next item's copy is issued inside g2p2g_item once this tile is
+    // converted, and the item after it claimed
     uint32_t parity = 0u;
     for (uint32_t wi = S.wi_next; wi < nw; wi = S.wi_next) {
         const int4 it = work_item(D, nf, wi);
