@@ -1494,6 +1494,7 @@ template <typename T> struct FusedShared {
     int org[3];              // tile origin of the item whose tile is (being) copied
     uint32_t wi_next;        // the work item this CTA claimed next
     uint32_t wi_ahead;       // thread 0: the one claimed after it
+    int2 next_span;          // first sorted slot and particle count of the next item
 };
 // Dynamic shared memory of k_g2p2g: the struct plus room to align it to the
 // 128 bytes a TMA destination needs.
@@ -1675,11 +1676,12 @@ __device__ __forceinline__ void split_particle(const DevParams<T>& P, Particle<T
 // with maps[0] for a single scene or maps[scene] for a batch scene that has a
 // map (the next item's scene parameters from the batch's table).  The next
 // item was claimed one item ago (S.wi_ahead); this item's flush claims the
-// one after it.  BATCH: P is the item's scene copied to shared memory, and
+// one after it and reads the next item's permutation entries into pf.  BATCH: P is the item's scene copied to shared memory, and
 // the item ends on a barrier.
 template <typename T, bool TRACK_FP, bool LAGGED, bool PAIRS, bool BATCH>
 __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs& D, FusedShared<T>& S,
-                                           const int4 it, uint32_t nf, uint32_t nw, const CUtensorMap* maps) {
+                                           const int4 it, uint32_t nf, uint32_t nw, const CUtensorMap* maps,
+                                           uint32_t& pf, bool& pf_ok) {
     static_assert(!PAIRS || sizeof(T) == 4, "the record-pairs scatter is FP32");
     constexpr int CA = kBlk + 2;
     const vec4<T>* __restrict__ pin = static_cast<const vec4<T>*>(D.pin);
@@ -1695,12 +1697,14 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         const int count = min(it.z, min(WorkP<T>::value, P.n - it.y));
         // one particle per thread (WorkP == blockDim): start its loads before
         // the tile is staged so the two latencies overlap
+        // (the permutation entry was read during the previous item's flush
+        // when this CTA had one)
         const int j = threadIdx.x;
-        const bool mine = j < count && RD_IN_BOUNDS(it.y + j, n) && RD_IN_BOUNDS(D.perm[it.y + j], n);
+        const uint32_t src = pf_ok ? pf : (j < count ? D.perm[it.y + j] : 0u);
+        const bool mine = j < count && RD_IN_BOUNDS(it.y + j, n) && RD_IN_BOUNDS(src, n);
         Particle<T> p;
         T FP[9];
         if (mine) {
-            const uint32_t src = D.perm[it.y + j];
             load_particle(pin, n, src, p);
             if (TRACK_FP) load_fp(pin, n, src, FP);
         }
@@ -1745,6 +1749,7 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         // (the later barriers of this item publish S.wi_next)
         if (threadIdx.x == 0) {
             S.wi_next = wn;
+            S.next_span = make_int2(nit.y, wn < nw ? max(0, min(nit.z, min(WorkP<T>::value, P.n - nit.y))) : 0);
             if (wn < nw) {
                 if constexpr (BATCH) {
                     if (nit.w < kBatchMaps)
@@ -1840,6 +1845,12 @@ __device__ __forceinline__ void g2p2g_item(const DevParams<T>& P, const DevBufs&
         // passes during the flush
         uint32_t claim = nw;
         if (threadIdx.x == 0 && S.wi_next < nw) claim = atomicAdd(D.claim, 1u);
+        // each thread reads its particle's permutation entry for the next item
+        {
+            const int2 sp = S.next_span;
+            pf = j < sp.y ? D.perm[sp.x + j] : 0u;
+            pf_ok = true;
+        }
         p2g_flush<T, CA>(P, S.p, porg, gnext, x0, x1);
         mark_around_block(P, D.gmark_next, (org[0] + 1) / kBlk, (org[1] + 1) / kBlk, (org[2] + 1) / kBlk);
         if (threadIdx.x == 0) S.wi_ahead = claim;
@@ -1889,6 +1900,8 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
     // next item's copy is issued inside g2p2g_item once this tile is
     // converted, and the item after it claimed
     uint32_t parity = 0u;
+    uint32_t pf = 0u;    // this thread's permutation entry of the next item
+    bool pf_ok = false;  // (read during the previous item's flush)
     for (uint32_t wi = S.wi_next; wi < nw; wi = S.wi_next) {
         const int4 it = work_item(D, nf, wi);
         bool arrived = true;
@@ -1915,9 +1928,9 @@ __global__ void __launch_bounds__(kFusedThreads, sizeof(T) == 4 ? kFusedMinBlock
             return;
         }
         if constexpr (BATCH)
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, true>(S.par, D, S, it, nf, nw, &maps.m[0]);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, true>(S.par, D, S, it, nf, nw, &maps.m[0], pf, pf_ok);
         else
-            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, false>(P0, D, S, it, nf, nw, &maps.m[0]);
+            g2p2g_item<T, TRACK_FP, LAGGED, PAIRS, false>(P0, D, S, it, nf, nw, &maps.m[0], pf, pf_ok);
     }
 }
 
