@@ -54,7 +54,7 @@ def test_oracle_matches_reference_scene_golden(orc):
     o.step(float(g["dt"]), 2)  # P4 split from here on (the fixture's s3)
     for k, a in (("x", o.x), ("v", o.v), ("FE", o.FE), ("FP", o.FP)):
         assert rel(a, g[f"s3_{k}"]) < 1e-5, k
-    # a rigid fall: B is rounding noise, judged against its scale ||v|| h
+    # a rigid fall: B is rounding noise, measured against its scale ||v|| h
     assert rel_floor(o.B, g["s3_B"], b_scale(g["s3_v"], float(g["h"]))) < 1e-6
 
 
