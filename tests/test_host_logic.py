@@ -76,6 +76,29 @@ def test_captured_traffic_scales_by_particles():
     assert abs(rec[1] / (bpp * rec[0]) - 1.0) < 0.10
 
 
+def test_captured_issue_scales_by_particles_and_fits_the_kernel():
+    """profiles/issue.txt: the warp instructions of the fused kernel's launch
+    (mean over the bench's timed launches), scaled by particle count, with the
+    record it came from; between 60 and 200 warp instructions a particle (a
+    gather, a split and a scatter per particle cannot take fewer, and more would
+    mean a capture of another kernel)."""
+    rec = None
+    for line in open(bench.os.path.join(bench.REPO, "profiles", "issue.txt")):
+        f = line.split()
+        if line.startswith("#") or len(f) < 5:
+            continue
+        if f[0] == "k_g2p2g" and f[1] == "two_balls_1m":
+            rec = (int(f[2]), int(f[3]), f[4])
+    assert rec is not None
+    inst, src = bench.captured_issue("k_g2p2g", "two_balls_1m", rec[0])
+    assert inst == pytest.approx(rec[1]) and src == rec[2]
+    assert bench.os.path.exists(bench.os.path.join(bench.REPO, src))
+    half, _ = bench.captured_issue("k_g2p2g", "two_balls_1m", rec[0] // 2)
+    assert half == pytest.approx(rec[1] / 2, rel=1e-6)
+    assert bench.captured_issue("k_g2p2g", "no_such_workload", 10) == (None, None)
+    assert 60.0 <= rec[1] / rec[0] <= 200.0
+
+
 def test_peak_reads_the_measured_file_or_falls_back(tmp_path, monkeypatch):
     monkeypatch.setattr(bench, "REPO", str(tmp_path))
     assert bench.measured_peak_hbm() == (6800.0, "fallback")
