@@ -67,7 +67,7 @@ def parse_args():
     ap.add_argument("--cpu-baseline", type=int, default=1, help="time the single-core CPU baseline (rank 0, N=1)")
     ap.add_argument("--adjoint", type=int, default=1, help="measure forward + adjoint on the 65,536-particle cube")
     ap.add_argument("--only", choices=("batched", "adjoint", "batched_adjoint", "snowball", "implicit", "profile",
-                                       "profile_batched"),
+                                       "profile_batched", "next_rows"),
                     default=None,
                     help="run one secondary measurement alone and print its JSON; 'profile' only initialises "
                          "the workload and runs --warmup + --steps steps (for ncu captures), 'profile_batched' "
@@ -75,6 +75,8 @@ def parse_args():
     ap.add_argument("--snowball", type=int, default=1, help="measure the 8,192-particle snowball on 64^3")
     ap.add_argument("--link", type=int, default=1, help="measure the host link (pinned copies each way)")
     ap.add_argument("--implicit", type=int, default=1, help="time timeIntegration (implicit L-BFGS)")
+    ap.add_argument("--next-rows", type=int, default=1,
+                    help="time the colliders, the initialiser and the viewer feed against the reference")
     ap.add_argument("--batch-steps", type=int, default=-1,
                     help="timed steps of the batched-forward workload (64 uneven scenes); -1: as many as "
                          "--steps, so the batch and the plain forward it is compared with run equally long; "
@@ -429,6 +431,201 @@ def measure_implicit(pkg, local, reps=5):
                        "energy_start": res["energy_start"], "energy": res["energy"],
                        "converged": res["converged"],
                        "particle_evaluations_per_s": sc.n * res["evaluations"] / best, "flags": flags}
+    return out
+
+
+def _next_rows_reference_worker(conn, what, core):
+    """Child process (spawned): times the reference's own code for one of
+    measure_next_rows' rows on one pinned core and sends the result back."""
+    try:
+        graft.load_package()
+        from rd_gb300 import scenes
+        orc = graft.load_oracle()
+        pin_to_core(core)
+        if what in ("colliders", "colliders_port"):
+            sc = scenes.snowball()
+            kw = sc.params()
+            P = orc.Params(*sc.grid, float(sc.h), **{k: v for k, v in kw.items()
+                                                     if k in ("E", "nu", "xi", "theta_c", "theta_s", "gravity")})
+            if what == "colliders":
+                r = orc.RefSim(P, sc.x, sc.v, sc.mass, p4=1)
+                r.set_colliders(_NEXT_ROWS_COLLIDERS)
+            else:
+                orc.build_oracle()
+                r = orc.OracleSim(P, sc.x, sc.v, sc.mass)
+                r.set_colliders(_NEXT_ROWS_COLLIDERS, 0, 0.5)
+            r.init()
+            nref = 10
+            t0 = time.perf_counter()
+            for _ in range(nref):
+                r.move_colliders(sc.dt)
+                r.step(sc.dt, 1)
+            el = time.perf_counter() - t0
+            conn.send({"value": sc.n * nref / el, "ms_per_step": el / nref * 1e3, "cores": 1,
+                       "kind": "reference" if what == "colliders" else "port",
+                       "sample": f"{nref} steps from the initial state"})
+        else:
+            G, n = 20, 2147
+            r = orc.RefSim(orc.Params(G, G, G, 1.0 / G), n=n, p4=1)
+            t0 = time.perf_counter()
+            r.initialize_particles((0.5, 0.6, 0.5), (0.0, -200.0, 0.0), seed=1)
+            el = time.perf_counter() - t0
+            conn.send({"ms_per_call": el * 1e3, "cores": 1, "kind": "reference"})
+    except Exception as e:
+        conn.send({"unavailable": f"{type(e).__name__}: {e}"})
+    conn.close()
+
+
+def _next_rows_reference(what, timeout_s=120.0):
+    """_next_rows_reference_worker in its own spawned process, so that a failure
+    of the reference's code cannot end the benchmark."""
+    import multiprocessing as mp
+    orc = graft.load_oracle()
+    if what != "colliders_port" and not orc.ref_available():
+        return {"unavailable": "the headless reference build is not present on this host"}
+    core = sorted(os.sched_getaffinity(0))[-1] if hasattr(os, "sched_getaffinity") else 0
+    ctx = mp.get_context("spawn")
+    parent, child = ctx.Pipe(duplex=False)
+    proc = ctx.Process(target=_next_rows_reference_worker, args=(child, what, core))
+    proc.start()
+    child.close()
+    res = None
+    try:
+        if parent.poll(timeout_s):
+            res = parent.recv()
+    except EOFError:  # the child ended without a result
+        res = None
+    proc.join(10.0)
+    if proc.is_alive():
+        proc.kill()
+        proc.join()
+    if res is None:
+        return {"unavailable": f"the reference's process ended with exit code {proc.exitcode} and no result"}
+    return res
+
+
+_S22, _C22 = float(np.sin(np.radians(22.5))), float(np.cos(np.radians(22.5)))
+# the colliders of measure_next_rows: a floor box under the falling snowball and a
+# turned box moving through its path (MeshCollider boxes, material_point_method.hpp:74-93)
+_NEXT_ROWS_COLLIDERS = [
+    dict(translation=(0.5, 0.28, 0.5), rotation=(1, 0, 0, 0), scale=(0.3, 0.2, 0.3), velocity=(0, 0, 0)),
+    dict(translation=(0.36, 0.52, 0.5), rotation=(_C22, 0, 0, _S22), scale=(0.05, 0.05, 0.2), velocity=(0.5, 0, 0))]
+
+
+def measure_next_rows(pkg, local, reps=3):
+    """The rows that widen the path beyond the step, each on the GPU and, where
+    the reference has the code, against the reference compiled on this host
+    and timed on one core:
+    * box colliders (gridBasedCollisions with the reference's MeshCollider
+      boxes, moved every step as main.cpp:188 does): the 8,192-particle
+      snowball falling on a floor box beside a turned, moving box, 200 fused
+      steps (CUDA events), against the same scene without colliders and
+      against the reference's step with the same boxes;
+    * the particle initialiser (initializeParticles): the reference's rand()
+      stream replayed on the device for its own scene (2,147 particles, 20^3,
+      seed 1), and the parallel generator filling a 0.2-radius ball on 128^3,
+      against the reference's initializeParticles on the same scenes;
+    * the viewer feed: the xyzs stream and the point-splat image (1280 x 720,
+      to host memory) of the 1.1M-particle two-ball state, host wall time per
+      frame, beside a numpy fill of the same xyzs and rgba arrays."""
+    import torch
+    graft.load_package()
+    from rd_gb300 import scenes
+    out = {}
+    # box colliders
+    sc = scenes.snowball()
+    kw = sc.params(bc=pkg.RD_BC_NONE)
+    cols = _NEXT_ROWS_COLLIDERS
+    steps = 200
+    res = {}
+    for name, cl in (("with_colliders", cols), ("without", [])):
+        best = None
+        for _ in range(reps):
+            sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, device=local, **kw))
+            sim.set_particles(sc.x, sc.v, sc.mass)
+            sim.set_colliders(cl, pkg.RD_COLLIDE_REFERENCE, 0.5)
+            sim.init_volumes()
+            st = torch.cuda.ExternalStream(sim.stream(), device=local)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            sim.synchronize()
+            e0.record(st)
+            for _ in range(steps):
+                if cl:
+                    sim.move_colliders(sc.dt)
+                sim.step(sc.dt, 1)
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            best = ms if best is None or ms < best else best
+            flags = sim.flags()
+            sim.close()
+        res[name] = {"ms_per_step": best, "value": sc.n / (best / 1e3), "flags": flags}
+    colliders = {"workload": "snowball (8,192 particles, 64^3, no walls) falling on a floor box and past a turned box "
+                             "moving at 0.5 m/s, the reference's collision rule, friction 0.5, 200 steps",
+                 "unit": "particle-steps/s", "value": res["with_colliders"]["value"],
+                 "ms_per_step": res["with_colliders"]["ms_per_step"],
+                 "ms_per_step_without_colliders": res["without"]["ms_per_step"],
+                 "flags": res["with_colliders"]["flags"]}
+    colliders["reference"] = _next_rows_reference("colliders")
+    if "unavailable" in colliders["reference"]:
+        # the C restatement with the same boxes and rule, where the reference's
+        # own collision step did not run
+        colliders["port"] = _next_rows_reference("colliders_port")
+    out["colliders"] = colliders
+    # the particle initialiser
+    init = {}
+    for name, (G, n, origin, vel, radius, mode) in {
+            "reference_scene": (20, 2147, (0.5, 0.6, 0.5), (0.0, -200.0, 0.0), 0.2, pkg.RD_INIT_REFERENCE),
+            "ball_128": (128, 500000, (0.5, 0.5, 0.5), (0.0, -1.0, 0.0), 0.2, pkg.RD_INIT_PARALLEL)}.items():
+        sim = pkg.Simulation(pkg.make_params(G, G, G, n, 1.0 / G, device=local))
+        best = None
+        for _ in range(reps + 1):
+            sim.synchronize()
+            t0 = time.perf_counter()
+            more = sim.initialize_particles(origin, vel, radius=radius, mass=6e-5 if G == 20 else 1e-6, seed=1,
+                                            mode=mode)
+            sim.synchronize()
+            el = time.perf_counter() - t0
+            best = el if best is None or el < best else best
+        sim.close()
+        entry = {"particles": n, "grid": G, "ms_per_call": best * 1e3, "mode": "reference rand() stream" if
+                 mode == pkg.RD_INIT_REFERENCE else "parallel hash generator", "kept_without_particle": more}
+        if G == 20:
+            entry["reference"] = _next_rows_reference("initializer")
+        init[name] = entry
+    out["initializer"] = init
+    # the viewer feed
+    sc = scenes.two_balls_1m()
+    sim = pkg.Simulation(pkg.make_params(*sc.grid, sc.n, sc.h, device=local, **sc.params()))
+    sim.set_particles(sc.x, sc.v, sc.mass)
+    rgba = np.random.default_rng(0).integers(0, 256, (sc.n, 4), dtype=np.uint8)
+    sim.set_colors(rgba)
+    view = pkg.look_at_view((0.5, 0.6, 1.6), (0.5, 0.5, 0.5), width=1280, height=720)
+    best_x, best_s = None, None
+    for _ in range(reps + 1):
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.device_xyzs()
+        sim.synchronize()
+        ex = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        img = sim.splat(view)
+        es = time.perf_counter() - t0
+        best_x = ex if best_x is None or ex < best_x else best_x
+        best_s = es if best_s is None or es < best_s else best_s
+    covered = float(np.mean(img.view(np.uint32).reshape(720, 1280) != view.background))
+    sim.close()
+    x = sc.x
+    t0 = time.perf_counter()
+    xyzs = np.empty((sc.n, 4), np.float32)
+    xyzs[:, :3] = x
+    xyzs[:, 3] = 0.01
+    rgb = np.ascontiguousarray(rgba)
+    el = time.perf_counter() - t0
+    out["viewer_feed"] = {"workload": "1.1M-particle two-ball state, 1280 x 720 image to host memory",
+                          "ms_xyzs": best_x * 1e3, "ms_splat_to_host": best_s * 1e3, "image_covered": covered,
+                          "numpy_fill_ms": el * 1e3, "numpy_fill_kind": "port: the per-frame xyzs / rgba arrays "
+                          "main.cpp:257-271 fills, filled by numpy on one core", "rgba_bytes": int(rgb.nbytes)}
     return out
 
 
@@ -828,6 +1025,11 @@ def run_ours(args):
         out["snowball"] = measure_snowball(pkg, local, max(args.warmup, 3))
     if args.implicit and rank == 0:
         out["implicit"] = measure_implicit(pkg, local)
+    if args.next_rows and rank == 0:
+        try:
+            out["next_rows"] = measure_next_rows(pkg, local)
+        except Exception as e:  # a secondary measurement must not lose the headline line
+            out["next_rows"] = {"error": f"{type(e).__name__}: {e}"}
     batch_steps = args.steps if args.batch_steps < 0 else args.batch_steps
     if batch_steps > 0:
         out["batched_forward"] = measure_batched(pkg, local, batch_steps, max(args.warmup, 3), value)
@@ -943,6 +1145,8 @@ def run_only(args):
         out = measure_snowball(pkg, 0, max(args.warmup, 3))
     elif args.only == "implicit":
         out = measure_implicit(pkg, 0)
+    elif args.only == "next_rows":
+        out = measure_next_rows(pkg, 0)
     elif args.only == "batched":
         out = measure_batched(pkg, 0, args.steps, max(args.warmup, 3), float("nan"))
     elif args.only == "adjoint":
