@@ -476,9 +476,11 @@ def _next_rows_reference_worker(conn, what, core):
     conn.close()
 
 
-def _next_rows_reference(what, timeout_s=120.0):
-    """_next_rows_reference_worker in its own spawned process, so that a failure
-    of the reference's code cannot end the benchmark."""
+def _next_rows_reference(what, timeout_s=120.0, worker=None):
+    """_next_rows_reference_worker (or `worker`, with the same arguments) in its
+    own spawned process, so that a failure of the reference's code cannot end
+    the benchmark: a process that ends without sending a result, or runs past
+    timeout_s, is reported `unavailable` with its exit code."""
     import multiprocessing as mp
     orc = graft.load_oracle()
     if what != "colliders_port" and not orc.ref_available():
@@ -486,7 +488,7 @@ def _next_rows_reference(what, timeout_s=120.0):
     core = sorted(os.sched_getaffinity(0))[-1] if hasattr(os, "sched_getaffinity") else 0
     ctx = mp.get_context("spawn")
     parent, child = ctx.Pipe(duplex=False)
-    proc = ctx.Process(target=_next_rows_reference_worker, args=(child, what, core))
+    proc = ctx.Process(target=worker or _next_rows_reference_worker, args=(child, what, core))
     proc.start()
     child.close()
     res = None

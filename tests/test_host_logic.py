@@ -104,3 +104,27 @@ def test_peak_reads_the_measured_file_or_falls_back(tmp_path, monkeypatch):
     assert bench.measured_peak_hbm() == (6800.0, "fallback")
     (tmp_path / "MEASURED_PEAKS.json").write_text(json.dumps({"hbm_gbs": 6686.0}))
     assert bench.measured_peak_hbm() == (6686.0, "measured")
+
+
+def _worker_that_dies(conn, what, core):
+    """A reference run that ends without a result (exit code 3)."""
+    import os
+    os._exit(3)
+
+
+def _worker_that_answers(conn, what, core):
+    conn.send({"what": what, "kind": "test"})
+    conn.close()
+
+
+def test_next_rows_reference_runs_apart_and_survives_a_dying_child(monkeypatch):
+    """bench.measure_next_rows times the reference's code in a spawned process:
+    a child that answers is passed through, one that dies is reported
+    unavailable with its exit code and the caller goes on."""
+    orc = bench.graft.load_oracle()
+    monkeypatch.setattr(orc, "ref_available", lambda: True)
+    assert bench._next_rows_reference("colliders", 60.0, _worker_that_answers) == {"what": "colliders",
+                                                                                   "kind": "test"}
+    out = bench._next_rows_reference("colliders", 60.0, _worker_that_dies)
+    assert "unavailable" in out and "exit code 3" in out["unavailable"]
+
